@@ -1,0 +1,143 @@
+/*
+ * psi.h -- C ABI of the GB300 parity-game strategy-improvement engine.
+ *
+ * This is the drop-in boundary for the reference's GPU solver path.  Each entry
+ * point names the reference interface it replaces (paths within the reference
+ * project).  Conventions:
+ *   - every function returns PSI_OK (0) or a PSI_ERR_* status; the message of
+ *     the last failure on the calling thread is psi_last_error();
+ *   - ids, priorities and CSR offsets are int32, as in the reference's Game and
+ *     GPUGame (game.h:9-34, gpu_game.h:9-20);
+ *   - the library owns all device memory and frees it in the destroy calls;
+ *     a solver runs on its own CUDA stream and its calls are synchronous with
+ *     respect to the host (results are ready when a call returns);
+ *   - a solver handle is used from one host thread at a time.
+ * No function falls back to a CPU implementation: without a usable CUDA device
+ * the solver calls fail with PSI_ERR_NO_DEVICE / PSI_ERR_CUDA.
+ */
+#ifndef PSI_H
+#define PSI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    PSI_OK = 0,
+    PSI_ERR_INVALID = 1,    /* bad argument or malformed game */
+    PSI_ERR_PARSE = 2,      /* .gm syntax error (the reference throws const char*) */
+    PSI_ERR_IO = 3,         /* file cannot be opened or read */
+    PSI_ERR_TOO_LARGE = 4,  /* sizes beyond the int32 layout */
+    PSI_ERR_CUDA = 5,       /* a CUDA call failed (the reference exits in gpu_assert) */
+    PSI_ERR_NO_DEVICE = 6,  /* no CUDA device */
+    PSI_ERR_STATE = 7,      /* call out of order (e.g. switch before any evaluation) */
+    PSI_ERR_LIMIT = 8,      /* a device-side step cap was hit (never expected) */
+    PSI_ERR_NOMEM = 9       /* device or host allocation failed */
+};
+
+typedef struct psi_game psi_game;
+typedef struct psi_solver psi_solver;
+
+const char *psi_last_error(void);
+const char *psi_version(void);
+
+/* ---------------------------------------------------------------- games
+ * Host-side game in CSR form: successors of v are
+ * targets[offsets[v] .. offsets[v+1]) in file order. */
+
+/* Game::parse_pgsolver(std::string) (game.cpp:38-50) and the .gz input path of
+ * main.cpp:140-151 (.bz2 is not supported). */
+int psi_game_load_gm(const char *path, psi_game **out);
+/* Game::parse_pgsolver(std::istream&) (game.cpp:51-107) on an in-memory text. */
+int psi_game_parse_gm(const char *text, int64_t len, psi_game **out);
+/* The CSR that GPUGame builds (gpu_game.cpp:11-41), supplied directly.  The
+ * arrays are copied. */
+int psi_game_from_csr(int32_t n, const int32_t *owner, const int32_t *priority,
+                      const int32_t *offsets, const int32_t *targets, psi_game **out);
+/* Writes pgsolver .gm text ("parity N;" then one line per vertex). */
+int psi_game_write_gm(const psi_game *g, const char *path);
+/* Seeded synthetic games: random (owner uniform, priority uniform in
+ * [0, pri_hi), out-degree uniform in [deg_lo, deg_hi], distinct non-self
+ * successors) and long-path (chain v->v+1 plus one back-edge to a uniform
+ * earlier vertex, owner alternating). */
+int psi_game_generate_random(int32_t n, int32_t deg_lo, int32_t deg_hi, int32_t pri_hi,
+                             uint64_t seed, psi_game **out);
+int psi_game_generate_longpath(int32_t n, int32_t pri_hi, uint64_t seed, psi_game **out);
+/* Game::get_n_vertices / get_max_pri (game.h:25-26) and the edge count. */
+int psi_game_info(const psi_game *g, int32_t *n, int64_t *m, int32_t *max_pri);
+/* Copies the CSR arrays out (each pointer may be NULL to skip it). */
+int psi_game_copy_csr(const psi_game *g, int32_t *owner, int32_t *priority, int32_t *offsets,
+                      int32_t *targets);
+void psi_game_free(psi_game *g);
+
+/* ---------------------------------------------------------------- solver */
+
+/* valuation_mode: how the evaluation represents valuations on the device.
+ *   PSI_VAL_PATH   per vertex: tour-ranked depth plus a parent/priority
+ *                  snapshot; comparisons walk the two paths to their lowest
+ *                  common ancestor (exact, O(n) memory).
+ * The reference's dense layout (gpu_parity.cu:26, one int per vertex and
+ * priority) is produced on demand by psi_get_valuation. */
+enum { PSI_VAL_PATH = 0 };
+
+typedef struct {
+    int32_t device;          /* CUDA device ordinal (default 0) */
+    int32_t valuation_mode;  /* PSI_VAL_* (default PSI_VAL_PATH) */
+    int32_t sublist_len;     /* Helman-JaJa node stride between sublist heads (default 64,
+                                the reference's gpu_list_ranking.cu:19) */
+    int32_t timing;          /* 1: record per-phase CUDA-event times (default 1) */
+    int32_t reserved[4];
+} psi_options;
+
+void psi_options_default(psi_options *opt);
+
+/* GPUGame(Game&) + GPUList(Game&, GPUGame&) (gpu_game.cpp:11-41,
+ * gpu_list_ranking.cu:14-36): uploads the game and allocates the solver's
+ * device state.  The game may be freed afterwards. */
+int psi_solver_create(const psi_game *g, const psi_options *opt, psi_solver **out);
+void psi_solver_destroy(psi_solver *s);
+
+/* StrategyImprovement (si.h:6-16) */
+int psi_init_strat(psi_solver *s);                                  /* si.h:9;  gpu_parity.cu:51-56 */
+int psi_compute_valuation(psi_solver *s);                           /* si.h:10; gpu_list_ranking.cu:279-326 */
+int psi_compute_first_val(psi_solver *s);                           /* si.h:11; gpu_list_ranking.cu:328-331 */
+int psi_mark_solved(psi_solver *s, int32_t player);                 /* si.h:12; cpu_parity.cpp:265-274 */
+/* si.h:13; gpu_parity.cu:303-317.  *switched receives the number of strict
+ * improvements taken during the scan, as CPUParity::switch_strategy counts them
+ * (cpu_parity.cpp:239-263); 0 means the player's strategy is unchanged. */
+int psi_switch_strategy(psi_solver *s, int32_t player, int64_t *switched);
+/* si.h:14; gpu_parity.cu:340-354: winning set of `player` in increasing vertex
+ * order (player 0: valuation +inf; player 1: every other vertex).  Writes at
+ * most cap ids to out (out may be NULL), *count receives the set size. */
+int psi_get_winning(psi_solver *s, int32_t player, int32_t *out, int64_t cap, int64_t *count);
+int psi_reset_opponent_strategy(psi_solver *s);                     /* si.h:15; cpu_parity.cpp:300-307 */
+
+/* State access (n ints each). Strategy: successor id, -1 = sink. Infinite:
+ * +1 / -1 / 0 as CPUParity's infinite[] (cpu_parity.h:15). */
+int psi_get_strategy(psi_solver *s, int32_t *out);
+int psi_set_strategy(psi_solver *s, const int32_t *in);
+int psi_get_infinite(psi_solver *s, int32_t *out);
+int psi_get_solved(psi_solver *s, int32_t *out);
+/* Dense valuation rows of vertices [v0, v0+count): count x (max_pri+1) ints in
+ * the reference's layout (cpu_parity.h:17, gpu_parity.cu:61-106); rows of
+ * infinite vertices are zero. */
+int psi_get_valuation(psi_solver *s, int32_t v0, int32_t count, int32_t *out);
+
+/* solve_si (main.cpp:20-55, gpumain.cpp:18-53): init_strat, then Odd's best
+ * response (evaluate, mark_solved(1), switch(1) until no switch), then
+ * mark_solved(0) and switch(0), until Even makes no switch.  reset != 0 is the
+ * "cpu-reset" variant (main.cpp:27-28).  max_evals > 0 caps the number of
+ * evaluations (PSI_ERR_LIMIT when reached); 0 means no cap. */
+int psi_solve(psi_solver *s, int32_t reset, int32_t *iter_count, int32_t *br_count, int64_t max_evals);
+
+/* Device time spent in evaluations and switch steps since creation or the last
+ * reset (milliseconds, CUDA events on the solver stream). */
+int psi_solver_times(psi_solver *s, double *eval_ms, double *switch_ms, int64_t *evals, int64_t *switches);
+int psi_solver_reset_times(psi_solver *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,278 @@
+"""Parity oracle -- TEST INFRASTRUCTURE ONLY.
+
+ctypes bindings of the C restatement of the reference CPUParity solver
+(psi_oracle.c) and, where it was built, of the reference's own CPUParity compiled
+from its sources (oracle/_ref/libpsi_ref.so, see build_ref.sh).  Only the tests,
+the smoke check and bench.py's CPU-baseline leg use this package, and only as a
+checker or a timed baseline; the product never calls it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_LIB = os.path.join(HERE, "_build", "libpsi_oracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libpsi_ref.so")
+
+
+def build(ref_dir: str = "/root/reference") -> None:
+    """Compile the oracle (and the reference driver when ref_dir exists)."""
+    env = dict(os.environ, REF_DIR=ref_dir)
+    subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True, env=env)
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+_olib = None
+_rlib = None
+
+
+def _oracle_lib():
+    global _olib
+    if _olib is None:
+        if not os.path.exists(ORACLE_LIB):
+            build()
+        L = C.CDLL(ORACLE_LIB)
+        vp = C.c_void_p
+        L.oracle_create.restype = vp
+        L.oracle_create.argtypes = [C.c_int, vp, vp, vp, vp]
+        for f in ("oracle_destroy", "oracle_init_strat", "oracle_reset_opponent_strategy",
+                  "oracle_compute_valuation"):
+            getattr(L, f).argtypes = [vp]
+            getattr(L, f).restype = None
+        L.oracle_max_pri.argtypes = [vp]
+        L.oracle_mark_solved.argtypes = [vp, C.c_int]
+        L.oracle_mark_solved.restype = None
+        L.oracle_switch_strategy.argtypes = [vp, C.c_int]
+        L.oracle_switch_strategy.restype = C.c_int64
+        L.oracle_get_winning.argtypes = [vp, C.c_int, vp]
+        L.oracle_get_winning.restype = C.c_int64
+        L.oracle_compare.argtypes = [vp, C.c_int, C.c_int]
+        for f in ("oracle_get_strategy", "oracle_set_strategy", "oracle_get_infinite", "oracle_get_solved"):
+            getattr(L, f).argtypes = [vp, vp]
+            getattr(L, f).restype = None
+        L.oracle_get_vals.argtypes = [vp, C.c_int, C.c_int, vp]
+        L.oracle_get_vals.restype = None
+        L.oracle_solve.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int64]
+        _olib = L
+    return _olib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def _ref_lib():
+    global _rlib
+    if _rlib is None:
+        L = C.CDLL(REF_LIB)
+        vp = C.c_void_p
+        L.ref_create_from_gm.restype = vp
+        L.ref_create_from_gm.argtypes = [C.c_char_p, C.c_char_p, C.c_int]
+        for f in ("ref_destroy", "ref_init_strat", "ref_compute_valuation", "ref_compute_first_val",
+                  "ref_reset_opponent_strategy"):
+            getattr(L, f).argtypes = [vp]
+            getattr(L, f).restype = None
+        L.ref_n.argtypes = [vp]
+        L.ref_max_pri.argtypes = [vp]
+        L.ref_n_edges.argtypes = [vp]
+        L.ref_n_edges.restype = C.c_longlong
+        L.ref_game_arrays.argtypes = [vp, vp, vp, vp, vp]
+        L.ref_game_arrays.restype = None
+        L.ref_mark_solved.argtypes = [vp, C.c_int]
+        L.ref_mark_solved.restype = None
+        L.ref_switch_strategy.argtypes = [vp, C.c_int]
+        L.ref_switch_strategy.restype = C.c_longlong
+        L.ref_get_winning.argtypes = [vp, C.c_int, vp]
+        L.ref_get_winning.restype = C.c_longlong
+        for f in ("ref_get_strategy", "ref_get_infinite"):
+            getattr(L, f).argtypes = [vp, vp]
+            getattr(L, f).restype = None
+        L.ref_get_vals.argtypes = [vp, C.c_int, C.c_int, vp]
+        L.ref_get_vals.restype = None
+        L.ref_compare.argtypes = [vp, C.c_int, C.c_int]
+        L.ref_solve.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_longlong]
+        _rlib = L
+    return _rlib
+
+
+class Oracle:
+    """The C restatement of CPUParity, with the StrategyImprovement methods."""
+
+    def __init__(self, owner, priority, offsets, targets):
+        self.L = _oracle_lib()
+        self._keep = [np.ascontiguousarray(a, dtype=np.int32) for a in (owner, priority, offsets, targets)]
+        self.n = len(self._keep[0])
+        self.h = self.L.oracle_create(self.n, *[_ptr(a) for a in self._keep])
+        if not self.h:
+            raise MemoryError("oracle_create failed (dense n*(max_pri+1) valuation table)")
+        self.max_pri = self.L.oracle_max_pri(self.h)
+
+    def init_strat(self):
+        self.L.oracle_init_strat(self.h)
+
+    def compute_valuation(self):
+        self.L.oracle_compute_valuation(self.h)
+
+    compute_first_val = compute_valuation
+
+    def mark_solved(self, p):
+        self.L.oracle_mark_solved(self.h, p)
+
+    def switch_strategy(self, p):
+        return self.L.oracle_switch_strategy(self.h, p)
+
+    def reset_opponent_strategy(self):
+        self.L.oracle_reset_opponent_strategy(self.h)
+
+    def get_winning(self, p):
+        out = np.empty(self.n, np.int32)
+        k = self.L.oracle_get_winning(self.h, p, _ptr(out))
+        return out[:k]
+
+    def get_strategy(self):
+        out = np.empty(self.n, np.int32)
+        self.L.oracle_get_strategy(self.h, _ptr(out))
+        return out
+
+    def set_strategy(self, s):
+        s = np.ascontiguousarray(s, dtype=np.int32)
+        self.L.oracle_set_strategy(self.h, _ptr(s))
+
+    def get_infinite(self):
+        out = np.empty(self.n, np.int32)
+        self.L.oracle_get_infinite(self.h, _ptr(out))
+        return out
+
+    def get_solved(self):
+        out = np.empty(self.n, np.int32)
+        self.L.oracle_get_solved(self.h, _ptr(out))
+        return out
+
+    def get_valuation(self, v0=0, count=None):
+        count = self.n - v0 if count is None else count
+        out = np.empty((count, self.max_pri + 1), np.int32)
+        self.L.oracle_get_vals(self.h, v0, count, _ptr(out))
+        return out
+
+    def compare(self, v, u):
+        return self.L.oracle_compare(self.h, v, u)
+
+    def solve(self, reset=False, max_evals=0):
+        it = C.c_int()
+        br = C.c_int()
+        rc = self.L.oracle_solve(self.h, int(reset), C.byref(it), C.byref(br), max_evals)
+        if rc != 0:
+            raise RuntimeError("oracle evaluation cap reached")
+        return it.value, br.value
+
+    def close(self):
+        if self.h:
+            self.L.oracle_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class RefSolver:
+    """The reference's own CPUParity (compiled from its sources), fed .gm text
+    through the reference parser."""
+
+    def __init__(self, gm_text: str):
+        self.L = _ref_lib()
+        err = C.create_string_buffer(256)
+        self.h = self.L.ref_create_from_gm(gm_text.encode(), err, 256)
+        if not self.h:
+            raise ValueError("reference parser: " + err.value.decode())
+        self.n = self.L.ref_n(self.h)
+        self.max_pri = self.L.ref_max_pri(self.h)
+
+    def game_arrays(self):
+        m = self.L.ref_n_edges(self.h)
+        ow = np.empty(self.n, np.int32)
+        pr = np.empty(self.n, np.int32)
+        off = np.empty(self.n + 1, np.int32)
+        tg = np.empty(max(m, 1), np.int32)
+        self.L.ref_game_arrays(self.h, _ptr(ow), _ptr(pr), _ptr(off), _ptr(tg))
+        return ow, pr, off, tg[:m]
+
+    def init_strat(self):
+        self.L.ref_init_strat(self.h)
+
+    def compute_valuation(self):
+        self.L.ref_compute_valuation(self.h)
+
+    def compute_first_val(self):
+        self.L.ref_compute_first_val(self.h)
+
+    def mark_solved(self, p):
+        self.L.ref_mark_solved(self.h, p)
+
+    def switch_strategy(self, p):
+        return self.L.ref_switch_strategy(self.h, p)
+
+    def reset_opponent_strategy(self):
+        self.L.ref_reset_opponent_strategy(self.h)
+
+    def get_winning(self, p):
+        out = np.empty(self.n, np.int32)
+        k = self.L.ref_get_winning(self.h, p, _ptr(out))
+        return out[:k]
+
+    def get_strategy(self):
+        out = np.empty(self.n, np.int32)
+        self.L.ref_get_strategy(self.h, _ptr(out))
+        return out
+
+    def get_infinite(self):
+        out = np.empty(self.n, np.int32)
+        self.L.ref_get_infinite(self.h, _ptr(out))
+        return out
+
+    def get_valuation(self, v0=0, count=None):
+        count = self.n - v0 if count is None else count
+        out = np.empty((count, self.max_pri + 1), np.int32)
+        self.L.ref_get_vals(self.h, v0, count, _ptr(out))
+        return out
+
+    def compare(self, v, u):
+        return self.L.ref_compare(self.h, v, u)
+
+    def solve(self, reset=False, max_evals=0):
+        it = C.c_int()
+        br = C.c_int()
+        rc = self.L.ref_solve(self.h, int(reset), C.byref(it), C.byref(br), max_evals)
+        if rc != 0:
+            raise RuntimeError("reference evaluation cap reached")
+        return it.value, br.value
+
+    def close(self):
+        if self.h:
+            self.L.ref_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def to_gm(owner, priority, offsets, targets) -> str:
+    """pgsolver text of a CSR game (header + one line per vertex)."""
+    n = len(owner)
+    lines = [f"parity {n - 1};"]
+    for v in range(n):
+        succ = ",".join(str(int(x)) for x in targets[offsets[v]:offsets[v + 1]])
+        lines.append(f"{v} {int(priority[v])} {int(owner[v])} {succ};")
+    return "\n".join(lines) + "\n"

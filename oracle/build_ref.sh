@@ -1,0 +1,20 @@
+#!/bin/sh
+# Builds the checkers under oracle/ (TEST INFRASTRUCTURE ONLY):
+#   oracle/_build/libpsi_oracle.so  -- the C restatement (psi_oracle.c), always;
+#   oracle/_ref/libpsi_ref.so       -- the reference's own CPUParity, compiled from
+#                                      its sources where they lie, when the
+#                                      reference tree is present (REF_DIR).
+# The reference is compiled from game.cpp and cpu_parity.cpp only (its CMake
+# build needs boost and a CUDA 3.5 target, neither used here).
+set -e
+HERE=$(cd "$(dirname "$0")" && pwd)
+REF_DIR=${REF_DIR:-/root/reference}
+CC=${CC:-gcc}
+CXX=${CXX:-g++}
+mkdir -p "$HERE/_build"
+$CC -O2 -std=c99 -fPIC -shared -o "$HERE/_build/libpsi_oracle.so" "$HERE/psi_oracle.c"
+if [ -f "$REF_DIR/cpu_parity.cpp" ] && [ -f "$REF_DIR/game.cpp" ]; then
+    mkdir -p "$HERE/_ref"
+    $CXX -O2 -std=c++11 -fPIC -shared -pthread -w -I"$REF_DIR" -o "$HERE/_ref/libpsi_ref.so" \
+        "$REF_DIR/game.cpp" "$REF_DIR/cpu_parity.cpp" "$HERE/ref_driver.cpp"
+fi

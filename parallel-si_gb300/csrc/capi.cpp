@@ -1,0 +1,275 @@
+// capi.cpp -- the extern "C" boundary (include/psi.h) over the native
+// game and solver classes.  Every entry point validates its handles, converts
+// C++ failures into status codes and never exits the process (the reference
+// calls exit(1) on CUDA errors, gpu_util.cpp:10-17, and throws const char* on
+// parse errors, game.cpp:68-105).
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "game.h"
+#include "psi.h"
+#include "psi_internal.h"
+#include "solver.h"
+
+struct psi_game {
+    psi::HostGame g;
+};
+
+struct psi_solver {
+    psi::Solver *s;
+};
+
+namespace psi {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+int fail(int code, const std::string &msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+}  // namespace psi
+
+#define PSI_GUARD_BEGIN try {
+#define PSI_GUARD_END                                                        \
+    }                                                                        \
+    catch (const std::bad_alloc &) {                                         \
+        return psi::fail(PSI_ERR_NOMEM, "host allocation failed");           \
+    }                                                                        \
+    catch (const std::exception &e) {                                        \
+        return psi::fail(PSI_ERR_INVALID, std::string("exception: ") + e.what()); \
+    }
+
+extern "C" {
+
+const char *psi_last_error(void) { return psi::g_last_error.c_str(); }
+
+const char *psi_version(void) { return "psi-gb300 0.1 (sm_103a)"; }
+
+static int wrap_game(psi::HostGame &&g, psi_game **out)
+{
+    psi_game *h = new psi_game();
+    h->g = std::move(g);
+    *out = h;
+    return PSI_OK;
+}
+
+int psi_game_load_gm(const char *path, psi_game **out)
+{
+    if (!out || !path) return psi::fail(PSI_ERR_INVALID, "null argument");
+    *out = nullptr;
+    PSI_GUARD_BEGIN
+    psi::HostGame g;
+    int rc = psi::load_gm(path, g);
+    if (rc) return rc;
+    return wrap_game(std::move(g), out);
+    PSI_GUARD_END
+}
+
+int psi_game_parse_gm(const char *text, int64_t len, psi_game **out)
+{
+    if (!out || (!text && len > 0) || len < 0) return psi::fail(PSI_ERR_INVALID, "null argument");
+    *out = nullptr;
+    PSI_GUARD_BEGIN
+    psi::HostGame g;
+    int rc = psi::parse_gm(text, len, g);
+    if (rc) return rc;
+    return wrap_game(std::move(g), out);
+    PSI_GUARD_END
+}
+
+int psi_game_from_csr(int32_t n, const int32_t *owner, const int32_t *priority, const int32_t *offsets,
+                      const int32_t *targets, psi_game **out)
+{
+    if (!out || !owner || !priority || !offsets || !targets) return psi::fail(PSI_ERR_INVALID, "null argument");
+    *out = nullptr;
+    PSI_GUARD_BEGIN
+    psi::HostGame g;
+    int rc = psi::make_game(n, owner, priority, offsets, targets, g);
+    if (rc) return rc;
+    return wrap_game(std::move(g), out);
+    PSI_GUARD_END
+}
+
+int psi_game_write_gm(const psi_game *g, const char *path)
+{
+    if (!g || !path) return psi::fail(PSI_ERR_INVALID, "null argument");
+    PSI_GUARD_BEGIN
+    return psi::write_gm(g->g, path);
+    PSI_GUARD_END
+}
+
+int psi_game_generate_random(int32_t n, int32_t deg_lo, int32_t deg_hi, int32_t pri_hi, uint64_t seed,
+                             psi_game **out)
+{
+    if (!out) return psi::fail(PSI_ERR_INVALID, "null argument");
+    *out = nullptr;
+    PSI_GUARD_BEGIN
+    psi::HostGame g;
+    int rc = psi::generate_random(n, deg_lo, deg_hi, pri_hi, seed, g);
+    if (rc) return rc;
+    return wrap_game(std::move(g), out);
+    PSI_GUARD_END
+}
+
+int psi_game_generate_longpath(int32_t n, int32_t pri_hi, uint64_t seed, psi_game **out)
+{
+    if (!out) return psi::fail(PSI_ERR_INVALID, "null argument");
+    *out = nullptr;
+    PSI_GUARD_BEGIN
+    psi::HostGame g;
+    int rc = psi::generate_longpath(n, pri_hi, seed, g);
+    if (rc) return rc;
+    return wrap_game(std::move(g), out);
+    PSI_GUARD_END
+}
+
+int psi_game_info(const psi_game *g, int32_t *n, int64_t *m, int32_t *max_pri)
+{
+    if (!g) return psi::fail(PSI_ERR_INVALID, "null game");
+    if (n) *n = g->g.n;
+    if (m) *m = g->g.m;
+    if (max_pri) *max_pri = g->g.max_pri;
+    return PSI_OK;
+}
+
+int psi_game_copy_csr(const psi_game *g, int32_t *owner, int32_t *priority, int32_t *offsets, int32_t *targets)
+{
+    if (!g) return psi::fail(PSI_ERR_INVALID, "null game");
+    const psi::HostGame &h = g->g;
+    if (owner && h.n) std::memcpy(owner, h.owner.data(), 4 * (size_t)h.n);
+    if (priority && h.n) std::memcpy(priority, h.priority.data(), 4 * (size_t)h.n);
+    if (offsets) std::memcpy(offsets, h.offsets.data(), 4 * ((size_t)h.n + 1));
+    if (targets && h.m) std::memcpy(targets, h.targets.data(), 4 * (size_t)h.m);
+    return PSI_OK;
+}
+
+void psi_game_free(psi_game *g) { delete g; }
+
+void psi_options_default(psi_options *opt)
+{
+    if (!opt) return;
+    std::memset(opt, 0, sizeof *opt);
+    opt->device = 0;
+    opt->valuation_mode = PSI_VAL_PATH;
+    opt->sublist_len = 64;
+    opt->timing = 1;
+}
+
+int psi_solver_create(const psi_game *g, const psi_options *opt, psi_solver **out)
+{
+    if (!g || !out) return psi::fail(PSI_ERR_INVALID, "null argument");
+    *out = nullptr;
+    PSI_GUARD_BEGIN
+    psi_options o;
+    psi_options_default(&o);
+    if (opt) o = *opt;
+    psi::Solver *s = nullptr;
+    int rc = psi::Solver::create(g->g, o, &s);
+    if (rc) return rc;
+    psi_solver *h = new psi_solver();
+    h->s = s;
+    *out = h;
+    return PSI_OK;
+    PSI_GUARD_END
+}
+
+void psi_solver_destroy(psi_solver *s)
+{
+    if (!s) return;
+    delete s->s;
+    delete s;
+}
+
+#define PSI_SOLVER_CALL(expr)                                               \
+    do {                                                                    \
+        if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null solver");  \
+        PSI_GUARD_BEGIN                                                     \
+        return (expr);                                                      \
+        PSI_GUARD_END                                                       \
+    } while (0)
+
+int psi_init_strat(psi_solver *s) { PSI_SOLVER_CALL(s->s->init_strat()); }
+int psi_compute_valuation(psi_solver *s) { PSI_SOLVER_CALL(s->s->compute_valuation()); }
+int psi_compute_first_val(psi_solver *s) { PSI_SOLVER_CALL(s->s->compute_first_val()); }
+int psi_mark_solved(psi_solver *s, int32_t player) { PSI_SOLVER_CALL(s->s->mark_solved(player)); }
+int psi_switch_strategy(psi_solver *s, int32_t player, int64_t *switched)
+{
+    PSI_SOLVER_CALL(s->s->switch_strategy(player, switched));
+}
+int psi_reset_opponent_strategy(psi_solver *s) { PSI_SOLVER_CALL(s->s->reset_opponent_strategy()); }
+
+int psi_get_winning(psi_solver *s, int32_t player, int32_t *out, int64_t cap, int64_t *count)
+{
+    if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null solver");
+    PSI_GUARD_BEGIN
+    std::vector<int32_t> w;
+    int rc = s->s->get_winning(player, w);
+    if (rc) return rc;
+    if (out) {
+        int64_t k = (int64_t)w.size() < cap ? (int64_t)w.size() : cap;
+        if (k > 0) std::memcpy(out, w.data(), 4 * (size_t)k);
+    }
+    if (count) *count = (int64_t)w.size();
+    return PSI_OK;
+    PSI_GUARD_END
+}
+
+int psi_get_strategy(psi_solver *s, int32_t *out)
+{
+    if (!out) return psi::fail(PSI_ERR_INVALID, "null output");
+    PSI_SOLVER_CALL(s->s->get_strategy(out));
+}
+int psi_set_strategy(psi_solver *s, const int32_t *in)
+{
+    if (!in) return psi::fail(PSI_ERR_INVALID, "null input");
+    PSI_SOLVER_CALL(s->s->set_strategy(in));
+}
+int psi_get_infinite(psi_solver *s, int32_t *out)
+{
+    if (!out) return psi::fail(PSI_ERR_INVALID, "null output");
+    PSI_SOLVER_CALL(s->s->get_infinite(out));
+}
+int psi_get_solved(psi_solver *s, int32_t *out)
+{
+    if (!out) return psi::fail(PSI_ERR_INVALID, "null output");
+    PSI_SOLVER_CALL(s->s->get_solved(out));
+}
+int psi_get_valuation(psi_solver *s, int32_t v0, int32_t count, int32_t *out)
+{
+    if (!out && count > 0) return psi::fail(PSI_ERR_INVALID, "null output");
+    PSI_SOLVER_CALL(s->s->get_valuation(v0, count, out));
+}
+
+int psi_solve(psi_solver *s, int32_t reset, int32_t *iter_count, int32_t *br_count, int64_t max_evals)
+{
+    if (!iter_count || !br_count) return psi::fail(PSI_ERR_INVALID, "null output");
+    *iter_count = 0;
+    *br_count = 0;
+    PSI_SOLVER_CALL(s->s->solve(reset, iter_count, br_count, max_evals));
+}
+
+int psi_solver_times(psi_solver *s, double *eval_ms, double *switch_ms, int64_t *evals, int64_t *switches)
+{
+    if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null solver");
+    const psi::SolverTimes &t = s->s->times();
+    if (eval_ms) *eval_ms = t.eval_ms;
+    if (switch_ms) *switch_ms = t.switch_ms;
+    if (evals) *evals = t.evals;
+    if (switches) *switches = t.switches;
+    return PSI_OK;
+}
+
+int psi_solver_reset_times(psi_solver *s)
+{
+    if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null solver");
+    s->s->reset_times();
+    return PSI_OK;
+}
+
+}  // extern "C"

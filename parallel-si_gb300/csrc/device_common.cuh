@@ -1,0 +1,53 @@
+// device_common.cuh -- shared constants and helpers of the sm_103a kernels.
+#ifndef PSI_DEVICE_COMMON_CUH
+#define PSI_DEVICE_COMMON_CUH
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace psi {
+
+// Per-vertex status word written by an evaluation (and frozen for solved
+// vertices):  >= 1  finite valuation, the value is the length of the strategy
+// path from the vertex to the sink (its depth in the sink tree);
+//             -1    valuation -inf (the path ends in a cycle won by Odd);
+//             -2    valuation +inf (the path ends in a cycle won by Even);
+//              0    the sink itself (never stored for a vertex).
+constexpr int32_t ST_NEG_INF = -1;
+constexpr int32_t ST_POS_INF = -2;
+constexpr int32_t ST_UNRESOLVED = INT32_MIN;
+
+__host__ __device__ __forceinline__ int32_t st_infinite(int32_t st)
+{
+    return st == ST_POS_INF ? 1 : (st == ST_NEG_INF ? -1 : 0);
+}
+
+// Tour node ids (an Euler tour of the strategy forest, two nodes per vertex):
+// node 2v is v's "down" node (leaving v's subtree toward the sink), 2v+1 its
+// "up" node (entering it); 2n / 2n+1 are the sink's down / up nodes.  The list
+// starts at the sink's up node and ends at the sink's down node (successor -1).
+// A successor entry below -1 marks a sublist head: -2 - j names sublist j.
+constexpr int32_t TOUR_END = -1;
+__host__ __device__ __forceinline__ int32_t head_mark(int32_t j) { return -2 - j; }
+__host__ __device__ __forceinline__ int32_t head_of_mark(int32_t x) { return -2 - x; }
+
+// Device-side error bits (a word the host reads back at sync points).
+constexpr uint32_t DERR_SUBLIST_CAP = 1u << 0;   // a sublist walk exceeded the list length
+constexpr uint32_t DERR_WALK_CAP = 1u << 1;      // a valuation walk exceeded its step cap
+constexpr uint32_t DERR_PASS_CAP = 1u << 2;      // a comparison exceeded its pass cap
+constexpr uint32_t DERR_BAD_INPUT = 1u << 3;     // malformed strategy (target out of range)
+
+constexpr int kBlock = 256;
+
+__host__ __device__ __forceinline__ int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace psi
+
+#define PSI_CUDA_TRY(expr)                                                            \
+    do {                                                                              \
+        cudaError_t e__ = (expr);                                                     \
+        if (e__ != cudaSuccess)                                                       \
+            return ::psi::fail(PSI_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e__)); \
+    } while (0)
+
+#endif

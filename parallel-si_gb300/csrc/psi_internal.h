@@ -1,0 +1,27 @@
+// psi_internal.h -- shared declarations of the native library (host side).
+#ifndef PSI_INTERNAL_H
+#define PSI_INTERNAL_H
+
+#include <cstdint>
+#include <string>
+
+#include "psi.h"
+
+namespace psi {
+
+// Error reporting: the C-ABI returns a status code and keeps a per-thread
+// message readable through psi_last_error().
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+
+int gen_random_offsets(int32_t n, int32_t deg_lo, int32_t deg_hi, uint64_t seed, int32_t *offsets);
+int gen_random_fill(int32_t n, int32_t deg_lo, int32_t deg_hi, int32_t pri_hi, uint64_t seed,
+                    const int32_t *offsets, int32_t *owner, int32_t *priority, int32_t *targets);
+int gen_longpath(int32_t n, int32_t pri_hi, uint64_t seed, int32_t *owner, int32_t *priority,
+                 int32_t *offsets, int32_t *targets);
+int gen_batch_sizes(int32_t count, int32_t n_lo, int32_t n_hi, uint64_t seed, int32_t *sizes);
+uint64_t gen_game_seed(uint64_t seed, int32_t index);
+
+}  // namespace psi
+
+#endif

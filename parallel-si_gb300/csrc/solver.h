@@ -1,0 +1,91 @@
+// solver.h -- one parity game resident on one GB300, solved by strategy
+// improvement with GPU evaluation and all-switches steps.
+#ifndef PSI_SOLVER_H
+#define PSI_SOLVER_H
+
+#include <cstdint>
+#include <vector>
+#include <cuda_runtime.h>
+
+#include "game.h"
+#include "psi.h"
+
+namespace psi {
+
+struct SolverTimes {
+    double eval_ms = 0, switch_ms = 0;   // device time, summed over calls (CUDA events)
+    int64_t evals = 0, switches = 0;
+};
+
+class Solver {
+public:
+    static int create(const HostGame &g, const psi_options &opt, Solver **out);
+    ~Solver();
+
+    // The StrategyImprovement interface (si.h:6-16).
+    int init_strat();
+    int compute_valuation();
+    int compute_first_val() { return compute_valuation(); }
+    int mark_solved(int32_t player);
+    int switch_strategy(int32_t player, int64_t *switched);
+    int get_winning(int32_t player, std::vector<int32_t> &out);
+    int reset_opponent_strategy();
+
+    int get_strategy(int32_t *out);
+    int set_strategy(const int32_t *in);
+    int get_infinite(int32_t *out);
+    int get_solved(int32_t *out);
+    int get_depth(int32_t *out);
+    int get_valuation(int32_t v0, int32_t count, int32_t *out);
+    int solve(int32_t reset, int32_t *iters, int32_t *brs, int64_t max_evals);
+
+    int32_t n() const { return n_; }
+    int64_t m() const { return m_; }
+    int32_t max_pri() const { return max_pri_; }
+    int32_t sublists() const { return nsub_; }
+    cudaStream_t stream() const { return stream_; }
+    const SolverTimes &times() const { return times_; }
+    void reset_times() { times_ = SolverTimes(); }
+    int last_unreached() const { return last_unreached_; }
+
+private:
+    Solver() = default;
+    int alloc(const HostGame &g, const psi_options &opt);
+    int sync_and_check(const char *what);
+    int set_device();
+
+    int device_ = 0;
+    cudaStream_t stream_ = nullptr;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    bool timing_ = true;
+    SolverTimes times_;
+    const HostGame *game_ = nullptr;
+
+    int32_t n_ = 0, max_pri_ = 0, nsub_ = 0, stride_ = 64;
+    int64_t m_ = 0, L_ = 0;
+    bool strat_ready_ = false, val_ready_ = false;
+    int last_unreached_ = 0;
+
+    // game (device)
+    int8_t *owner_ = nullptr;
+    int32_t *pri_ = nullptr, *off_ = nullptr, *tgt_ = nullptr;
+    // state
+    int32_t *strat_ = nullptr, *st_ = nullptr;
+    uint8_t *solved_ = nullptr;
+    int2 *pp_ = nullptr;
+    // evaluation scratch
+    int32_t *succ_ = nullptr, *hsucc_ = nullptr, *ulist_ = nullptr;
+    int2 *vloc_ = nullptr, *redA_ = nullptr, *redB_ = nullptr, *jA_ = nullptr, *jB_ = nullptr;
+    // small device words + pinned host mirrors
+    struct Words {
+        unsigned long long count;
+        uint32_t err;
+        int32_t ucount;
+    };
+    Words *dw_ = nullptr, *hw_ = nullptr;
+    std::vector<void *> allocs_;
+};
+
+}  // namespace psi
+
+#endif

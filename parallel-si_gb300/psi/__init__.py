@@ -1,0 +1,248 @@
+"""Python mirror of the reference solver interface over the C ABI.
+
+``Game`` mirrors the reference's ``Game`` (game.h:9-34: ``parse_pgsolver``,
+``get_n_vertices``, ``get_max_pri``, ``get_player``, ``get_priority``,
+``get_edges``); ``GPUList`` mirrors the ``StrategyImprovement`` solver classes
+(si.h:6-16; ``GPUList`` in gpu_list_ranking.h:11-41); ``solve_si`` is the
+driver loop of main.cpp:20-55 and returns ``(iter_count, br_count)``.  All
+compute goes through ``libpsi_gb300.so``; nothing here runs a CPU solver.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import List, Optional
+
+import numpy as np
+
+from ._lib import (PSI_VAL_PATH, Options, PsiError, check, last_error, lib, ptr)
+
+__all__ = ["Game", "GPUList", "PsiError", "Options", "solve_si", "default_options", "version"]
+
+
+def version() -> str:
+    return lib.psi_version().decode()
+
+
+def default_options(**kw) -> Options:
+    o = Options()
+    lib.psi_options_default(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class Game:
+    """Host-side parity game in CSR form (owner 0 = Even, 1 = Odd)."""
+
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+        n = C.c_int32()
+        m = C.c_int64()
+        mp = C.c_int32()
+        check(lib.psi_game_info(self._h, C.byref(n), C.byref(m), C.byref(mp)))
+        self.n, self.m, self.max_pri = n.value, m.value, mp.value
+        self._csr = None
+
+    # ---- constructors
+    @classmethod
+    def parse_pgsolver(cls, source: str) -> "Game":
+        """Game::parse_pgsolver(std::string filename) (game.cpp:38-50)."""
+        h = C.c_void_p()
+        check(lib.psi_game_load_gm(source.encode(), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def parse_text(cls, text: str | bytes) -> "Game":
+        """Game::parse_pgsolver(std::istream&) (game.cpp:51-107) on a string."""
+        b = text.encode() if isinstance(text, str) else text
+        h = C.c_void_p()
+        check(lib.psi_game_parse_gm(b, len(b), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_csr(cls, owner, priority, offsets, targets) -> "Game":
+        ow = np.ascontiguousarray(owner, dtype=np.int32)
+        pr = np.ascontiguousarray(priority, dtype=np.int32)
+        off = np.ascontiguousarray(offsets, dtype=np.int32)
+        tg = np.ascontiguousarray(targets, dtype=np.int32)
+        h = C.c_void_p()
+        check(lib.psi_game_from_csr(len(ow), ptr(ow), ptr(pr), ptr(off), ptr(tg), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def random(cls, n: int, deg_lo: int, deg_hi: int, pri_hi: Optional[int] = None, seed: int = 1) -> "Game":
+        h = C.c_void_p()
+        check(lib.psi_game_generate_random(n, deg_lo, deg_hi, n if pri_hi is None else pri_hi,
+                                           C.c_uint64(seed), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def longpath(cls, n: int, pri_hi: int = 1024, seed: int = 1) -> "Game":
+        h = C.c_void_p()
+        check(lib.psi_game_generate_longpath(n, pri_hi, C.c_uint64(seed), C.byref(h)))
+        return cls(h)
+
+    # ---- accessors (game.h:25-29)
+    def get_n_vertices(self) -> int:
+        return self.n
+
+    def get_max_pri(self) -> int:
+        return self.max_pri
+
+    def csr(self):
+        """(owner, priority, offsets, targets) as int32 numpy arrays."""
+        if self._csr is None:
+            ow = np.empty(self.n, np.int32)
+            pr = np.empty(self.n, np.int32)
+            off = np.empty(self.n + 1, np.int32)
+            tg = np.empty(max(self.m, 1), np.int32)
+            check(lib.psi_game_copy_csr(self._h, ptr(ow), ptr(pr), ptr(off), ptr(tg)))
+            self._csr = (ow, pr, off, tg[: self.m])
+        return self._csr
+
+    def get_player(self, v: int) -> int:
+        return int(self.csr()[0][v])
+
+    def get_priority(self, v: int) -> int:
+        return int(self.csr()[1][v])
+
+    def get_edges(self, v: int) -> List[int]:
+        _, _, off, tg = self.csr()
+        return [int(x) for x in tg[off[v]:off[v + 1]]]
+
+    def write_pgsolver(self, path: str) -> None:
+        check(lib.psi_game_write_gm(self._h, path.encode()))
+
+    def close(self) -> None:
+        if self._h:
+            lib.psi_game_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GPUList:
+    """Strategy-improvement solver on one GB300 (StrategyImprovement, si.h:6-16).
+
+    Constructing it uploads the game (GPUGame, gpu_game.cpp:11-41) and
+    allocates the device state (GPUList, gpu_list_ranking.cu:14-36).
+    """
+
+    def __init__(self, game: Game, options: Optional[Options] = None, **kw):
+        o = options if options is not None else default_options(**kw)
+        self.n = game.n
+        self.max_pri = game.max_pri
+        self._h = C.c_void_p()
+        check(lib.psi_solver_create(game._h, C.byref(o), C.byref(self._h)))
+
+    # ---- StrategyImprovement
+    def init_strat(self) -> None:
+        check(lib.psi_init_strat(self._h))
+
+    def compute_valuation(self) -> None:
+        check(lib.psi_compute_valuation(self._h))
+
+    def compute_first_val(self) -> None:
+        check(lib.psi_compute_first_val(self._h))
+
+    def mark_solved(self, player: int) -> None:
+        check(lib.psi_mark_solved(self._h, player))
+
+    def switch_strategy(self, player: int) -> int:
+        k = C.c_int64()
+        check(lib.psi_switch_strategy(self._h, player, C.byref(k)))
+        return k.value
+
+    def get_winning(self, player: int) -> np.ndarray:
+        cnt = C.c_int64()
+        out = np.empty(self.n, np.int32)
+        check(lib.psi_get_winning(self._h, player, ptr(out), self.n, C.byref(cnt)))
+        return out[: cnt.value]
+
+    def reset_opponent_strategy(self) -> None:
+        check(lib.psi_reset_opponent_strategy(self._h))
+
+    # ---- state
+    def get_strategy(self) -> np.ndarray:
+        out = np.empty(self.n, np.int32)
+        check(lib.psi_get_strategy(self._h, ptr(out)))
+        return out
+
+    def set_strategy(self, strat) -> None:
+        s = np.ascontiguousarray(strat, dtype=np.int32)
+        check(lib.psi_set_strategy(self._h, ptr(s)))
+
+    def get_infinite(self) -> np.ndarray:
+        out = np.empty(self.n, np.int32)
+        check(lib.psi_get_infinite(self._h, ptr(out)))
+        return out
+
+    def get_solved(self) -> np.ndarray:
+        out = np.empty(self.n, np.int32)
+        check(lib.psi_get_solved(self._h, ptr(out)))
+        return out
+
+    def get_valuation(self, v0: int = 0, count: Optional[int] = None) -> np.ndarray:
+        count = self.n - v0 if count is None else count
+        out = np.empty((count, self.max_pri + 1), np.int32)
+        check(lib.psi_get_valuation(self._h, v0, count, ptr(out)))
+        return out
+
+    def solve(self, reset: bool = False, max_evals: int = 0):
+        it = C.c_int32()
+        br = C.c_int32()
+        check(lib.psi_solve(self._h, int(reset), C.byref(it), C.byref(br), max_evals))
+        return it.value, br.value
+
+    def times(self):
+        e = C.c_double()
+        s = C.c_double()
+        ne = C.c_int64()
+        ns = C.c_int64()
+        check(lib.psi_solver_times(self._h, C.byref(e), C.byref(s), C.byref(ne), C.byref(ns)))
+        return {"eval_ms": e.value, "switch_ms": s.value, "evals": ne.value, "switches": ns.value}
+
+    def reset_times(self) -> None:
+        check(lib.psi_solver_reset_times(self._h))
+
+    def close(self) -> None:
+        if self._h:
+            lib.psi_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def solve_si(si, reset: bool = False):
+    """The reference driver loop (main.cpp:20-55) over any object with the
+    StrategyImprovement methods; returns (iter_count, br_count)."""
+    br_count = 0
+    iter_count = 0
+    si.init_strat()
+    first = True
+    while True:
+        if not first and reset:
+            si.reset_opponent_strategy()
+        while True:
+            if first:
+                si.compute_first_val()
+            else:
+                si.compute_valuation()
+            br_count += 1
+            si.mark_solved(1)
+            if si.switch_strategy(1) == 0:
+                break
+        first = False
+        si.mark_solved(0)
+        iter_count += 1
+        if si.switch_strategy(0) == 0:
+            break
+    return iter_count, br_count

@@ -1,0 +1,76 @@
+"""GPU parity: the CUDA solver (through the C ABI) against the oracle and the
+reference's golden solves.  Integer results must be identical: strategies
+after every switch, infinite flags and dense valuations after every
+evaluation, switch counts, iteration/evaluation counts and winning sets."""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+import psi
+from games import make
+from lockstep import lockstep, traced_solve
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_solves.json")))["cases"]
+
+
+@pytest.mark.parametrize("case", GOLDEN, ids=lambda c: f"{c['family']}-{c['n']}-{c['seed']}-{int(c['reset'])}")
+def test_gpu_matches_reference_golden(case):
+    g = make(case["family"], case["n"], case["seed"])
+    gpu = psi.GPUList(g)
+    iters, brs, trace = traced_solve(gpu, reset=case["reset"])
+    assert (iters, brs) == (case["iters"], case["brs"])
+    assert trace == case["trace"]
+    w0 = gpu.get_winning(0)
+    assert hashlib.sha256(w0.tobytes()).hexdigest()[:16] == case["w0_digest"]
+    assert hashlib.sha256(gpu.get_strategy().tobytes()).hexdigest()[:16] == case["strategy_digest"]
+
+
+LOCKSTEP = [("c2", 4000, s, False) for s in range(31, 37)] + [
+    ("c1", 10000, 3, False), ("c3", 8000, 4, False), ("c3", 3000, 5, True),
+    ("smallpri", 5000, 6, False), ("smallpri", 2000, 7, True), ("c4", 250, 8, False),
+    ("ring10", 10, 0, False)]
+
+
+@pytest.mark.parametrize("fam,n,seed,reset", LOCKSTEP)
+def test_gpu_lockstep_with_oracle(fam, n, seed, reset):
+    g = make(fam, n, seed)
+    gpu = psi.GPUList(g)
+    ref = oracle.Oracle(*g.csr())
+    lockstep(gpu, ref, reset=reset, rows=(n * (g.max_pri + 1) <= 2e8))
+
+
+@pytest.mark.parametrize("stride", [2, 3, 17, 64, 500])
+def test_gpu_sublist_stride_does_not_change_results(stride):
+    g = make("c2", 3000, 41)
+    gpu = psi.GPUList(g, sublist_len=stride)
+    ref = oracle.Oracle(*g.csr())
+    lockstep(gpu, ref)
+
+
+def test_gpu_solve_entry_point_matches_driver_loop():
+    g = make("c2", 20000, 51)
+    a = psi.GPUList(g)
+    it, br = a.solve()
+    b = psi.GPUList(g)
+    it2, br2 = psi.solve_si(b)
+    assert (it, br) == (it2, br2)
+    assert np.array_equal(a.get_strategy(), b.get_strategy())
+    assert np.array_equal(a.get_winning(0), b.get_winning(0))
+
+
+def test_gpu_repeated_solves_are_identical():
+    g = make("c2", 50000, 61)
+    s = psi.GPUList(g)
+    first = s.solve()
+    strat = s.get_strategy()
+    w0 = s.get_winning(0)
+    for _ in range(3):
+        assert s.solve() == first
+        assert np.array_equal(s.get_strategy(), strat)
+        assert np.array_equal(s.get_winning(0), w0)
