@@ -1,0 +1,375 @@
+#!/usr/bin/env python
+"""bench.py -- strategy-improvement iterations per second on one random parity
+game of n = 2^24 vertices, solved on GB300 (one game replica per GPU).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+A step is one full solve (solve_si: init_strat until Even makes no switch) of
+the 2^24-vertex game resident in HBM.  value = SI iterations of all ranks /
+max-over-ranks device time of the K timed solves (CUDA events on the solver
+stream).  e2e repeats the solve through the C ABI from host buffers: upload of
+the game, the solve, and the read-back of the winning set and strategy are
+inside the timed region.  Prints one JSON line (rank 0).
+
+--impl reference times the reference algorithm's CPU implementation instead:
+the oracle (a C restatement of the reference's CPUParity), single thread, on a
+bounded sample of the same workload (the dense n*(max_pri+1) valuation table of
+CPUParity does not fit at n = 2^24).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "parallel-si_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "SI iters/s"
+UNIT = "SI iters/s"
+N_DEFAULT = 1 << 24
+DEG_LO, DEG_HI = 2, 5
+CPU_SAMPLE_N = 1 << 15          # bounded sample for the CPU reference algorithm
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+TRAFFIC_PATH = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
+
+
+def workload_config(n, m=None, seed=1):
+    cfg = {
+        "workload": f"single random parity game, n={n} (2^{n.bit_length() - 1}): owner uniform, priority "
+                    f"uniform in [0,n), out-degree uniform in [{DEG_LO},{DEG_HI}], distinct non-self successors",
+        "n": n,
+        "seed": seed,
+        "step": "one full solve_si (init_strat to convergence), game resident in HBM",
+        "l2": "inputs larger than L2 (game CSR + solver state ~1.3 GB at n=2^24), no flush",
+        "parallelism": "replicas: one independent game per GPU",
+    }
+    if m is not None:
+        cfg["m"] = m
+    return cfg
+
+
+# ------------------------------------------------------------------ helpers
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max/sum reductions over ranks (torch.distributed when
+    launched by torchrun, no-ops for one process)."""
+
+    def __init__(self, world, local):
+        self.world = world
+        self.t = None
+        if world > 1:
+            import torch
+            import torch.distributed as td
+
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            td.init_process_group(backend=backend)
+            self.t = (torch, td, backend, local)
+
+    def _reduce(self, x, op):
+        if self.t is None:
+            return x
+        torch, td, backend, local = self.t
+        dev = torch.device("cuda", local) if backend == "nccl" else torch.device("cpu")
+        v = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+        td.all_reduce(v, op=op)
+        return float(v.item())
+
+    def barrier(self):
+        if self.t is not None:
+            self.t[1].barrier()
+
+    def max(self, x):
+        return x if self.t is None else self._reduce(x, self.t[1].ReduceOp.MAX)
+
+    def sum(self, x):
+        return x if self.t is None else self._reduce(x, self.t[1].ReduceOp.SUM)
+
+    def close(self):
+        if self.t is not None:
+            self.t[1].destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=10)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS_PATH) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def traffic_per_launch(kernel, n):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (lines: kernel n bytes_per_launch), scaled linearly to n."""
+    try:
+        with open(TRAFFIC_PATH) as f:
+            for line in f:
+                p = line.split()
+                if len(p) >= 3 and not line.startswith("#") and p[0] == kernel:
+                    return float(p[2]) * n / float(p[1])
+    except OSError:
+        pass
+    return None
+
+
+def phase_bytes(phase, n, m, nsub, counters, calls, n_even, n_odd, iters, brs):
+    """Algorithmic bytes per call of a timed phase (roofline)."""
+    L = 2 * n + 2
+    if phase == "switch":
+        sw_calls = max(1, counters["switches"])
+        player_vertices = brs * n_odd + iters * n_even
+        total = (n * sw_calls + 12 * player_vertices + 12 * counters["sw_edges"] + 8 * counters["sw_loads"]
+                 + 4 * counters["sw_changed"])
+        return total / sw_calls
+    if phase == "sublist":
+        return 4 * L + 8 * n + 12 * nsub
+    if phase == "tour":
+        return 4 * L + 25 * n + 12 * nsub
+    if phase == "broadcast":
+        return 37 * n
+    if phase == "reduced":
+        rounds = (nsub - 1).bit_length() + 1
+        return 24 * nsub * rounds
+    return None
+
+
+KERNEL_OF_PHASE = {"switch": "k_switch", "sublist": "k_walk_sublists", "tour": "k_tour_link",
+                   "broadcast": "k_broadcast_depth", "reduced": "k_wyllie_round", "cycles": "k_jump_round"}
+
+
+def cpu_baseline_sample(solves=3, seed=1):
+    """The oracle (C restatement of CPUParity), single thread, on the bounded
+    sample: `solves` full solves of the n=2^15 game of the same distribution."""
+    import oracle
+    import psi
+
+    g = psi.Game.random(CPU_SAMPLE_N, DEG_LO, DEG_HI, CPU_SAMPLE_N, seed)
+    o = oracle.Oracle(*g.csr())
+    t0 = time.perf_counter()
+    iters = 0
+    for _ in range(solves):
+        it, _ = o.solve()
+        iters += it
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": iters / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{solves} full solves of the n=2^15 game of the same distribution (seed {seed}); "
+                      f"{dt:.1f} s; the reference's CPUParity keeps n*(max_pri+1) ints and cannot hold n=2^24"}
+
+
+# ------------------------------------------------------------------ arms
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    import oracle
+    import psi
+
+    g = psi.Game.random(CPU_SAMPLE_N, DEG_LO, DEG_HI, CPU_SAMPLE_N, args.seed)
+    o = oracle.Oracle(*g.csr())
+    for _ in range(args.warmup):
+        o.solve()
+    t0 = time.perf_counter()
+    iters = 0
+    for _ in range(args.steps):
+        it, _ = o.solve()
+        iters += it
+    dt = time.perf_counter() - t0
+    value = iters / dt
+    sample = (f"each step: one full solve of the n=2^15 game of the same distribution (seed {args.seed}) by "
+              f"the oracle (C restatement of the reference CPUParity, single thread; the reference's dense "
+              f"valuation table cannot hold n=2^24)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": workload_config(args.n, seed=args.seed),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args, rank, world, local):
+    import numpy as np
+
+    import psi
+
+    dist = Dist(world, local)
+    seed = args.seed + rank
+    game = psi.Game.random(args.n, DEG_LO, DEG_HI, args.n, seed)
+    owner, _, _, _ = game.csr()
+    n_odd = int(owner.sum())
+    n_even = game.n - n_odd
+    solver = psi.GPUList(game, device=local, sublist_len=args.sublist_len)
+
+    for _ in range(args.warmup):
+        solver.solve()
+    solver.reset_times()
+    dist.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    launches0 = psi.launch_count()
+    solver.timer_begin()
+    iters = brs = 0
+    for _ in range(args.steps):
+        it, br = solver.solve()
+        iters += it
+        brs += br
+    ms = solver.timer_end()
+    launches = psi.launch_count() - launches0
+    clocks = sampler.stop()
+    dist.barrier()
+    ms_max = dist.max(ms)
+    iters_all = dist.sum(iters)
+    phases = solver.phase_times()
+    counters = solver.counters()
+    nsub = (2 * game.n + 1 + args.sublist_len - 1) // args.sublist_len + 1
+
+    # roofline of the dominant kernel-level phase
+    kernel_phases = ("switch", "sublist", "tour", "broadcast", "reduced", "cycles")
+    dom = max(kernel_phases, key=lambda p: phases[p][0])
+    dom_ms, dom_calls = phases[dom]
+    bpc = phase_bytes(dom, game.n, game.m, nsub, counters, dom_calls, n_even, n_odd, iters, brs)
+    peak, peak_kind = hbm_peak()
+    roofline = None
+    if bpc is not None and dom_calls:
+        achieved = bpc / (dom_ms / dom_calls / 1e3) / 1e9
+        traffic = traffic_per_launch(KERNEL_OF_PHASE[dom], game.n)
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                    "traffic": traffic, "kernel": KERNEL_OF_PHASE[dom], "peak_source": peak_kind,
+                    "algorithmic_bytes_per_launch": bpc, "ms_per_launch": dom_ms / dom_calls}
+    lr = {}
+    for p in ("sublist", "tour", "broadcast"):
+        pm, pc = phases[p]
+        b = phase_bytes(p, game.n, game.m, nsub, counters, pc, n_even, n_odd, iters, brs)
+        if pc:
+            lr[p] = {"ms_per_call": pm / pc, "GBps": b / (pm / pc / 1e3) / 1e9, "frac": b / (pm / pc / 1e3) / 1e9 / peak}
+
+    # end to end through the C ABI from host buffers
+    csr = [np.ascontiguousarray(a) for a in game.csr()]
+    h2d = game.n * 1 + 4 * game.n + 4 * (game.n + 1) + 4 * game.m
+    d2h = 8 * game.n
+    del solver
+    dist.barrier()
+    t0 = time.perf_counter()
+    e2e_iters = 0
+    for _ in range(args.steps):
+        g2 = psi.Game.from_csr(*csr)
+        s2 = psi.GPUList(g2, device=local, sublist_len=args.sublist_len)
+        it, _ = s2.solve()
+        s2.get_winning(0)
+        s2.get_strategy()
+        s2.close()
+        g2.close()
+        e2e_iters += it
+    e2e_s = time.perf_counter() - t0
+    e2e_max = dist.max(e2e_s)
+    e2e_iters_all = dist.sum(e2e_iters)
+
+    cpu = cpu_baseline_sample(seed=args.seed) if (rank == 0 and world == 1 and not args.no_cpu) else None
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": iters_all / (ms_max / 1e3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic", "config": dict(workload_config(game.n, game.m, args.seed),
+                                                sublist_len=args.sublist_len,
+                                                iters_per_solve=iters // args.steps, brs_per_solve=brs // args.steps),
+            "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
+            "e2e": {"value": e2e_iters_all / e2e_max, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "list_ranking": lr,
+            "phase_ms_per_solve": {k: v[0] / args.steps for k, v in phases.items()},
+            "counters_per_solve": {k: v / args.steps for k, v in counters.items()},
+        }
+        print(json.dumps(line), flush=True)
+    dist.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--sublist-len", type=int, default=64)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_gb300(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

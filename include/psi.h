@@ -136,6 +136,29 @@ int psi_solve(psi_solver *s, int32_t reset, int32_t *iter_count, int32_t *br_cou
  * reset (milliseconds, CUDA events on the solver stream). */
 int psi_solver_times(psi_solver *s, double *eval_ms, double *switch_ms, int64_t *evals, int64_t *switches);
 int psi_solver_reset_times(psi_solver *s);
+/* Per-phase device times (ms) and call counts, phases in this order:
+ * 0 evaluation (whole), 1 switch step, 2 tour build, 3 sublist walk,
+ * 4 reduced-list ranking, 5 broadcast, 6 cycle parity. */
+enum { PSI_PHASE_EVAL = 0, PSI_PHASE_SWITCH, PSI_PHASE_TOUR, PSI_PHASE_SUBLIST, PSI_PHASE_REDUCED,
+       PSI_PHASE_BROADCAST, PSI_PHASE_CYCLES, PSI_PHASE_COUNT };
+int psi_solver_phase_times(psi_solver *s, double *ms, int64_t *calls, int32_t nphases);
+/* The solver's CUDA stream (a cudaStream_t), so callers can order their own
+ * work or record events against it. */
+int psi_solver_stream(psi_solver *s, void **stream);
+/* Number of non-solved vertices the sink did not reach in the last evaluation. */
+int psi_solver_unreached(psi_solver *s, int64_t *count);
+/* Work counters since the last reset, in this order: evaluations, switch
+ * steps, compared edges, parent/priority loads of the comparison walks,
+ * vertices whose strategy changed, unreached vertices (summed over
+ * evaluations), pointer-jumping rounds.  Writes min(k, 7) values. */
+int psi_solver_counters(psi_solver *s, int64_t *out, int32_t k);
+/* Kernel launches issued by this library in this process so far. */
+int64_t psi_launch_count(void);
+/* Region timer on the solver stream: begin synchronises the stream and records
+ * a CUDA event; end records a second one, waits for it and returns the elapsed
+ * device time in ms (host gaps between the solver's launches included). */
+int psi_solver_timer_begin(psi_solver *s);
+int psi_solver_timer_end(psi_solver *s, double *ms);
 
 #ifdef __cplusplus
 }

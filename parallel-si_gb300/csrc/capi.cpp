@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "game.h"
+#include "kernels.h"
 #include "psi.h"
 #include "psi_internal.h"
 #include "solver.h"
@@ -258,10 +259,62 @@ int psi_solver_times(psi_solver *s, double *eval_ms, double *switch_ms, int64_t 
 {
     if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null solver");
     const psi::SolverTimes &t = s->s->times();
-    if (eval_ms) *eval_ms = t.eval_ms;
-    if (switch_ms) *switch_ms = t.switch_ms;
+    if (eval_ms) *eval_ms = t.ms[psi::PH_EVAL];
+    if (switch_ms) *switch_ms = t.ms[psi::PH_SWITCH];
     if (evals) *evals = t.evals;
     if (switches) *switches = t.switches;
+    return PSI_OK;
+}
+
+int psi_solver_phase_times(psi_solver *s, double *ms, int64_t *calls, int32_t nphases)
+{
+    if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null solver");
+    const psi::SolverTimes &t = s->s->times();
+    for (int32_t i = 0; i < nphases && i < psi::PH_COUNT; i++) {
+        if (ms) ms[i] = t.ms[i];
+        if (calls) calls[i] = t.calls[i];
+    }
+    return PSI_OK;
+}
+
+int psi_solver_counters(psi_solver *s, int64_t *out, int32_t k)
+{
+    if (!s || !s->s || !out) return psi::fail(PSI_ERR_INVALID, "null argument");
+    const psi::SolverTimes &t = s->s->times();
+    const int64_t vals[] = {t.evals, t.switches, t.sw_edges, t.sw_loads, t.sw_changed, t.unreached, t.jump_rounds};
+    for (int32_t i = 0; i < k && i < (int32_t)(sizeof vals / sizeof vals[0]); i++) out[i] = vals[i];
+    return PSI_OK;
+}
+
+int64_t psi_launch_count(void) { return psi::launch_count(); }
+
+int psi_solver_timer_begin(psi_solver *s)
+{
+    if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null solver");
+    PSI_GUARD_BEGIN
+    return s->s->timer_begin();
+    PSI_GUARD_END
+}
+
+int psi_solver_timer_end(psi_solver *s, double *ms)
+{
+    if (!s || !s->s || !ms) return psi::fail(PSI_ERR_INVALID, "null argument");
+    PSI_GUARD_BEGIN
+    return s->s->timer_end(ms);
+    PSI_GUARD_END
+}
+
+int psi_solver_stream(psi_solver *s, void **stream)
+{
+    if (!s || !s->s || !stream) return psi::fail(PSI_ERR_INVALID, "null argument");
+    *stream = (void *)s->s->stream();
+    return PSI_OK;
+}
+
+int psi_solver_unreached(psi_solver *s, int64_t *count)
+{
+    if (!s || !s->s || !count) return psi::fail(PSI_ERR_INVALID, "null argument");
+    *count = s->s->last_unreached();
     return PSI_OK;
 }
 

@@ -22,6 +22,17 @@ __host__ __device__ __forceinline__ int32_t st_infinite(int32_t st)
     return st == ST_POS_INF ? 1 : (st == ST_NEG_INF ? -1 : 0);
 }
 
+// Snapshot of a vertex the sink reached, written by an evaluation: its parent
+// in the sink tree (-1 = the sink), its priority, and a summary of its root
+// path (the path from the vertex to the sink): the highest priority on it and
+// how many vertices of the path carry that priority.  rmax == RM_UNKNOWN until
+// the summary has been computed.  16-byte aligned so one load fetches it all
+// and the (rmax, rcnt) pair is written as one 8-byte store.
+struct __align__(16) PathNode {
+    int32_t parent, pri, rmax, rcnt;
+};
+constexpr int32_t RM_UNKNOWN = INT32_MIN;
+
 // Tour node ids (an Euler tour of the strategy forest, two nodes per vertex):
 // node 2v is v's "down" node (leaving v's subtree toward the sink), 2v+1 its
 // "up" node (entering it); 2n / 2n+1 are the sink's down / up nodes.  The list

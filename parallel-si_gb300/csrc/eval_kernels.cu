@@ -3,31 +3,41 @@
 // One evaluation turns the current strategy (one successor per vertex, -1 for
 // the sink) into a per-vertex status word (device_common.cuh):
 //
-//  1. Euler tour of the sink tree (tour_init, tour_link): every non-solved
-//     vertex splices its up/down node pair into its parent's up slot with one
-//     atomic exchange.  This is the reference's list construction
-//     (gpu_list_ranking.cu:52-92); child order is whatever the atomics give and
-//     no result depends on it.
+//  1. Euler tour of the sink tree (tour_init, tour_link, sink_chain).  Every
+//     non-solved vertex's up/down node pair is spliced into its parent's list
+//     of children -- the reference builds the same list with one atomic
+//     exchange per vertex (gpu_list_ranking.cu:52-92).  Here each parent links
+//     its own children by scanning its in-neighbours in a reverse CSR that is
+//     built once per game, so the step needs no atomics and the child order
+//     (in-neighbour order) is deterministic; the sink's children, which can be
+//     millions, are compacted with one atomic per warp and chained.
 //  2. Helman-JaJa list ranking: `nsub` sublist heads at a fixed node stride
-//     (pick_heads, gpu_list_ranking.cu:96-110), one thread per sublist walks to
+//     (pick_heads, gpu_list_ranking.cu:96-110); one thread per sublist walks to
 //     the next head accumulating +1/-1 depth steps (walk_sublists,
-//     gpu_list_ranking.cu:114-193), then Wyllie pointer jumping over the reduced
-//     list of sublists (wyllie_round) replaces the reference's serial host walk
-//     (gpu_list_ranking.cu:197-240) and its device/host round trip.
+//     gpu_list_ranking.cu:114-193).  The reduced list of sublists is ranked on
+//     the device -- the reference copies it to the host and walks it serially
+//     (gpu_list_ranking.cu:197-240): a second Helman-JaJa level groups the
+//     sublists into segments (red_walk), one block ranks the segments by Wyllie
+//     pointer jumping (red_block), and red_finish gives every sublist its
+//     suffix sum and whether the list start reaches it.
 //  3. Broadcast (broadcast_depth, gpu_list_ranking.cu:244-277): a vertex the
 //     sink reaches gets its path length; its parent and priority are snapshot
-//     for the comparison walks of the following switch step.
-//  4. Vertices the sink does not reach end in a cycle or in a solved vertex.
-//     Pointer jumping with a running maximum (jump_*) gives each one the parity
-//     of its cycle's top priority, or the frozen value of the solved vertex, in
-//     every evaluation -- as the reference CPU solver does
-//     (cpu_parity.cpp:35-52, 80-104); the reference GPU list ranker marks all
-//     of them +inf (gpu_list_ranking.cu:254-276).
+//     for the comparison walks of the following switch step.  Vertices the
+//     sink does not reach are collected.
+//  4. Those vertices end in a cycle or in a solved vertex.  Pointer jumping
+//     with a running maximum (cycles, one cooperative launch) gives each the
+//     parity of its cycle's top priority, or the frozen value of the solved
+//     vertex, in every evaluation -- as the reference CPU solver does
+//     (cpu_parity.cpp:35-52, 80-104); the reference GPU list ranker marks all of
+//     them +inf (gpu_list_ranking.cu:254-276).
+#include <atomic>
 #include <climits>
-#include <cub/block/block_reduce.cuh>
+#include <cooperative_groups.h>
 
 #include "device_common.cuh"
 #include "kernels.h"
+
+namespace cg = cooperative_groups;
 
 namespace psi {
 
@@ -37,6 +47,28 @@ inline unsigned grid_for(int64_t items, int block = kBlock)
 {
     int64_t g = ceil_div(items, block);
     return (unsigned)(g < 1 ? 1 : g);
+}
+
+__device__ __forceinline__ int ceil_log2_dev(int64_t x)
+{
+    int r = 0;
+    while (((int64_t)1 << r) < x) r++;
+    return r;
+}
+
+// warp-aggregated append of `flag` lanes' values to list[*count ...]
+__device__ __forceinline__ void warp_append(bool flag, int32_t value, int32_t *__restrict__ list,
+                                            int32_t *__restrict__ count)
+{
+    unsigned mask = __ballot_sync(0xffffffffu, flag);
+    if (mask) {
+        int lane = threadIdx.x & 31;
+        int leader = __ffs(mask) - 1;
+        int32_t base = 0;
+        if (lane == leader) base = atomicAdd(count, __popc(mask));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (flag) list[base + __popc(mask & ((1u << lane) - 1))] = value;
+    }
 }
 
 __global__ void k_init_strat(int32_t n, const int8_t *__restrict__ owner, const int32_t *__restrict__ off,
@@ -57,8 +89,9 @@ __global__ void k_reset_odd(int32_t n, const int8_t *__restrict__ owner, const i
     if (owner[v] == 1) strat[v] = tgt[off[v]];
 }
 
-// Up node of v points at its own down node; a vertex that is not linked (solved)
-// keeps a two-node cycle.  The sink's down node ends the list.
+// Up node of v points at its own down node; the down node of a vertex that no
+// parent links (solved, or child of a solved vertex) points back at its up
+// node.  The sink's down node ends the list.
 __global__ void k_tour_init(int32_t n, int32_t *__restrict__ succ, int2 *__restrict__ vloc)
 {
     int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -68,27 +101,56 @@ __global__ void k_tour_init(int32_t n, int32_t *__restrict__ succ, int2 *__restr
     if (i < n) vloc[i] = make_int2(-1, 0);
 }
 
+// Thread p: (a) if p is a live child of the sink, append it to the sink list;
+// (b) if p is live, link its live children, found among its distinct
+// in-neighbours rev_src[rev_off[p] .. rev_off[p+1]), as
+// up(p) -> up(c0) ... down(c0) -> up(c1) ... down(c_last) -> down(p).
 __global__ void k_tour_link(int32_t n, const int32_t *__restrict__ strat, const uint8_t *__restrict__ solved,
-                            int32_t *__restrict__ succ)
+                            const int32_t *__restrict__ rev_off, const int32_t *__restrict__ rev_src,
+                            int32_t *__restrict__ succ, int32_t *__restrict__ sinklist,
+                            int32_t *__restrict__ sinkcount)
 {
-    int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= n || solved[v]) return;
-    int32_t p = strat[v];
-    int64_t slot = (p < 0) ? 2 * (int64_t)n + 1 : 2 * (int64_t)p + 1;
-    int32_t old = atomicExch(&succ[slot], 2 * v + 1);
-    succ[2 * (int64_t)v] = old;
+    int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = p < n && !solved[p];
+    bool to_sink = live && strat[p] < 0;
+    warp_append(to_sink, p, sinklist, sinkcount);
+    if (!live) return;
+    int32_t prev = -1;
+    int32_t e1 = rev_off[p + 1];
+    for (int32_t e = rev_off[p]; e < e1; e++) {
+        int32_t u = rev_src[e];
+        if (strat[u] != p || solved[u]) continue;
+        if (prev < 0) succ[2 * (int64_t)p + 1] = 2 * u + 1;
+        else succ[2 * (int64_t)prev] = 2 * u + 1;
+        prev = u;
+    }
+    if (prev >= 0) succ[2 * (int64_t)prev] = 2 * p;
+}
+
+// sink up -> up(c0) ... down(c0) -> up(c1) ... down(c_last) -> sink down
+__global__ void k_sink_chain(int32_t n, const int32_t *__restrict__ sinklist,
+                             const int32_t *__restrict__ sinkcount, int32_t *__restrict__ succ)
+{
+    int32_t k = *sinkcount;
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k; i += gridDim.x * blockDim.x) {
+        int32_t v = sinklist[i];
+        succ[2 * (int64_t)v] = (i + 1 < k) ? 2 * sinklist[i + 1] + 1 : 2 * n;
+        if (i == 0) succ[2 * (int64_t)n + 1] = 2 * v + 1;
+    }
 }
 
 // Head j sits at node j*stride; the last head is the sink's up node (the list
-// start), so the reduced list starts at sublist nsub-1.
+// start), so the reduced list starts at sublist nsub-1.  Also resets the
+// segment map of the reduced-list ranking.
 __global__ void k_pick_heads(int64_t L, int32_t nsub, int32_t stride, int32_t *__restrict__ succ,
-                             int32_t *__restrict__ hsucc)
+                             int32_t *__restrict__ hsucc, int2 *__restrict__ seg_of)
 {
     int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nsub) return;
     int64_t node = (j == nsub - 1) ? L - 1 : (int64_t)j * stride;
     hsucc[j] = succ[node];
     succ[node] = head_mark(j);
+    seg_of[j] = make_int2(-1, 0);
 }
 
 // One thread per sublist: walk from the head's successor up to and including
@@ -125,176 +187,344 @@ __global__ void k_walk_sublists(int32_t nsub, int32_t n, int64_t L, const int32_
     red[j] = make_int2(x == TOUR_END ? TOUR_END : head_of_mark(x), acc);
 }
 
-// Suffix sums over the reduced list: out[j] = (next after doubling, sum).  A
-// sublist reached from the list start ends with next == TOUR_END; sublists on
-// cycles never do.
-__global__ void k_wyllie_round(int32_t nsub, const int2 *__restrict__ in, int2 *__restrict__ out)
+// ---- ranking of the reduced list (items = sublists, weight = sublist total)
+// Segment heads: the items whose index is a multiple of seg_stride, plus the
+// list start nsub-1; segment k's head is k*seg_stride (k < nseg-1) or nsub-1.
+__device__ __forceinline__ bool seg_head(int32_t j, int32_t nsub, int32_t seg_stride)
+{
+    return j == nsub - 1 || (j % seg_stride) == 0;
+}
+
+__device__ __forceinline__ int32_t seg_index(int32_t j, int32_t nsub, int32_t nseg, int32_t seg_stride)
+{
+    return j == nsub - 1 ? nseg - 1 : j / seg_stride;
+}
+
+// One thread per segment: walk from its head through the items up to the next
+// head, recording each item's segment and inclusive prefix within it.
+// segs[k] = (next segment or TOUR_END, segment total).
+__global__ void k_red_walk(int32_t nsub, int32_t nseg, int32_t seg_stride, const int2 *__restrict__ red,
+                           int2 *__restrict__ seg_of, int2 *__restrict__ segs, uint32_t *__restrict__ err)
+{
+    int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nseg) return;
+    int32_t x = (k == nseg - 1) ? nsub - 1 : k * seg_stride;
+    int32_t acc = 0;
+    int32_t steps = 0;
+    for (;;) {
+        int2 r = red[x];
+        acc += r.y;
+        seg_of[x] = make_int2(k, acc);
+        x = r.x;
+        if (x < 0 || seg_head(x, nsub, seg_stride)) break;
+        if (++steps > nsub) {
+            atomicOr(err, DERR_SUBLIST_CAP);
+            x = TOUR_END;
+            break;
+        }
+    }
+    segs[k] = make_int2(x < 0 ? TOUR_END : seg_index(x, nsub, nseg, seg_stride), acc);
+}
+
+// Single block: Wyllie suffix sums over the segment list (at most a few
+// thousand entries) in two global buffers; result in `a` (or `b`, see return
+// slot written to *which).  Reads bypass L1 (buffers are rewritten each round).
+__global__ void __launch_bounds__(1024) k_red_block(int32_t nseg, int2 *__restrict__ a, int2 *__restrict__ b,
+                                                    int2 *__restrict__ out)
+{
+    int rounds = ceil_log2_dev(nseg) + 1;
+    int2 *in = a, *o = b;
+    for (int r = 0; r < rounds; r++) {
+        for (int32_t k = threadIdx.x; k < nseg; k += blockDim.x) {
+            int2 x = __ldcg(&in[k]);
+            if (x.x >= 0) {
+                int2 y = __ldcg(&in[x.x]);
+                x = make_int2(y.x, x.y + y.y);
+            }
+            o[k] = x;
+        }
+        __syncthreads();
+        int2 *t = in;
+        in = o;
+        o = t;
+    }
+    for (int32_t k = threadIdx.x; k < nseg; k += blockDim.x) out[k] = __ldcg(&in[k]);
+}
+
+// fin[j] = (TOUR_END if the list start reaches sublist j, else 0; inclusive
+// suffix sum of the reduced list from j).
+__global__ void k_red_finish(int32_t nsub, const int2 *__restrict__ red, const int2 *__restrict__ seg_of,
+                             const int2 *__restrict__ segfin, int2 *__restrict__ fin)
 {
     int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nsub) return;
-    int2 r = in[j];
-    if (r.x >= 0) {
-        int2 q = in[r.x];
-        r = make_int2(q.x, r.y + q.y);
+    int2 so = seg_of[j];
+    if (so.x < 0) {
+        fin[j] = make_int2(0, 0);
+        return;
     }
-    out[j] = r;
+    int2 sf = segfin[so.x];
+    fin[j] = make_int2(sf.x == TOUR_END ? TOUR_END : 0, sf.y - so.y + red[j].y);
 }
 
 // Depth of a reached vertex = inclusive prefix of the tour at its up node =
 // -(suffix sum of its sublist) + local prefix (the whole tour sums to 0).
-__global__ void k_broadcast_depth(int32_t n, const int2 *__restrict__ vloc, const int2 *__restrict__ red,
+__global__ void k_broadcast_depth(int32_t n, const int2 *__restrict__ vloc, const int2 *__restrict__ fin,
                                   const int32_t *__restrict__ strat, const int32_t *__restrict__ pri,
                                   const uint8_t *__restrict__ solved, int32_t *__restrict__ st,
-                                  int2 *__restrict__ pp, int32_t *__restrict__ ulist,
+                                  PathNode *__restrict__ node, int32_t *__restrict__ ulist,
                                   int32_t *__restrict__ ucount)
 {
     int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     bool unreached = false;
     if (v < n && !solved[v]) {
         int2 loc = vloc[v];
-        int2 r = (loc.x >= 0) ? red[loc.x] : make_int2(0, 0);
+        int2 r = (loc.x >= 0) ? fin[loc.x] : make_int2(0, 0);
         if (loc.x >= 0 && r.x == TOUR_END) {
             st[v] = loc.y - r.y;
-            pp[v] = make_int2(strat[v], pri[v]);
+            node[v] = PathNode{strat[v], pri[v], RM_UNKNOWN, 0};
         } else {
             st[v] = ST_UNRESOLVED;
             unreached = true;
         }
     }
-    // warp-aggregated append of the unreached vertices
-    unsigned mask = __ballot_sync(0xffffffffu, unreached);
-    if (mask) {
-        int lane = threadIdx.x & 31;
-        int leader = __ffs(mask) - 1;
-        int32_t base = 0;
-        if (lane == leader) base = atomicAdd(ucount, __popc(mask));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (unreached) ulist[base + __popc(mask & ((1u << lane) - 1))] = v;
+    warp_append(unreached, v, ulist, ucount);
+}
+
+// (max, count of max) of the union of two priority multisets
+__device__ __forceinline__ void top1_merge(int32_t &m, int32_t &c, int32_t m2, int32_t c2)
+{
+    if (m2 > m) {
+        m = m2;
+        c = c2;
+    } else if (m2 == m) {
+        c += c2;
     }
 }
 
-__global__ void k_jump_init(int32_t nu, const int32_t *__restrict__ ulist, const int32_t *__restrict__ strat,
-                            const int32_t *__restrict__ pri, int2 *__restrict__ jmp, uint32_t *__restrict__ err)
-{
-    int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nu) return;
-    int32_t u = ulist[i];
-    int32_t t = strat[u];
-    if (t < 0) {            // cannot happen: a vertex pointing at the sink is reached
-        atomicOr(err, DERR_BAD_INPUT);
-        t = u;
-    }
-    jmp[u] = make_int2(t, pri[u]);
-}
-
-// jmp[u] = (vertex 2^k steps ahead, maximum priority over those 2^k vertices
-// starting at u).  Solved vertices absorb.
-__global__ void k_jump_round(int32_t nu, const int32_t *__restrict__ ulist, const uint8_t *__restrict__ solved,
-                             const int2 *__restrict__ in, int2 *__restrict__ out)
-{
-    int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nu) return;
-    int32_t u = ulist[i];
-    int2 a = in[u];
-    if (!solved[a.x]) {
-        int2 b = in[a.x];
-        a = make_int2(b.x, max(a.y, b.y));
-    }
-    out[u] = a;
-}
-
-// After 2^R >= |unreached| steps every walk sits on its final cycle (or on a
-// solved vertex); the window maximum from a cycle vertex covers the cycle.
-__global__ void k_jump_finish(int32_t nu, const int32_t *__restrict__ ulist, const uint8_t *__restrict__ solved,
-                              const int2 *__restrict__ jmp, int32_t *__restrict__ st)
-{
-    int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nu) return;
-    int32_t u = ulist[i];
-    int32_t t = jmp[u].x;
-    int32_t val;
-    if (solved[t]) val = st[t];
-    else val = (jmp[t].y % 2 == 0) ? ST_POS_INF : ST_NEG_INF;
-    st[u] = val;
-}
-
-__global__ void k_mark_solved(int32_t n, int32_t player, const int32_t *__restrict__ st,
-                              uint8_t *__restrict__ solved)
+// Root-path summaries of the reached vertices.  Each thread walks from its
+// vertex towards the sink until it meets an ancestor whose summary is already
+// known (or the sink) and stores the summary of its own vertex only; with
+// threads in arbitrary order a walk is short on average (an ancestor has
+// usually been done already).  A concurrent reader sees either RM_UNKNOWN or
+// the final pair, which is written as one 8-byte store.
+__global__ void k_rootinfo(int32_t n, const int32_t *__restrict__ st, PathNode *__restrict__ node,
+                           uint32_t *__restrict__ err)
 {
     int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= n) return;
+    if (v >= n || st[v] < 1) return;
+    PathNode q = node[v];
+    int32_t m = q.pri, c = 1, y = q.parent;
+    int32_t steps = 0;
+    while (y >= 0) {
+        int4 r = *reinterpret_cast<const int4 *>(&node[y]);
+        if (r.z != RM_UNKNOWN) {
+            top1_merge(m, c, r.z, r.w);
+            break;
+        }
+        top1_merge(m, c, r.y, 1);
+        y = r.x;
+        if (++steps > n) {
+            atomicOr(err, DERR_WALK_CAP);
+            break;
+        }
+    }
+    *reinterpret_cast<int2 *>(&node[v].rmax) = make_int2(m, c);
+}
+
+// ---- cycle parity of the unreached vertices
+// jmp[u] = (vertex 2^k steps ahead, maximum priority over those 2^k vertices
+// starting at u); solved vertices absorb.  After 2^R >= |unreached| steps
+// every walk sits on its final cycle (or on a solved vertex), and the window
+// maximum from a cycle vertex covers the whole cycle.
+constexpr int kSmallCycles = 4096;   // up to this many: one block, no grid barrier
+
+template <bool GRID>
+__device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const int32_t *__restrict__ strat,
+                            const int32_t *__restrict__ pri, const uint8_t *__restrict__ solved,
+                            int32_t *__restrict__ st, int2 *__restrict__ ja, int2 *__restrict__ jb,
+                            uint32_t *__restrict__ err)
+{
+    const int64_t tid = GRID ? (int64_t)blockIdx.x * blockDim.x + threadIdx.x : threadIdx.x;
+    const int64_t nth = GRID ? (int64_t)gridDim.x * blockDim.x : blockDim.x;
+    auto barrier = [] {
+        if (GRID) cg::this_grid().sync();
+        else __syncthreads();
+    };
+    for (int64_t i = tid; i < nu; i += nth) {
+        int32_t u = ulist[i];
+        int32_t t = strat[u];
+        if (t < 0) {            // cannot happen: a vertex pointing at the sink is reached
+            atomicOr(err, DERR_BAD_INPUT);
+            t = u;
+        }
+        ja[u] = make_int2(t, pri[u]);
+    }
+    barrier();
+    int2 *in = ja, *out = jb;
+    int rounds = ceil_log2_dev(nu) + 1;
+    for (int r = 0; r < rounds; r++) {
+        for (int64_t i = tid; i < nu; i += nth) {
+            int32_t u = ulist[i];
+            int2 a = __ldcg(&in[u]);
+            if (!solved[a.x]) {
+                int2 b = __ldcg(&in[a.x]);
+                a = make_int2(b.x, max(a.y, b.y));
+            }
+            out[u] = a;
+        }
+        barrier();
+        int2 *t = in;
+        in = out;
+        out = t;
+    }
+    for (int64_t i = tid; i < nu; i += nth) {
+        int32_t u = ulist[i];
+        int32_t t = __ldcg(&in[u]).x;
+        st[u] = solved[t] ? st[t] : ((__ldcg(&in[t]).y % 2 == 0) ? ST_POS_INF : ST_NEG_INF);
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_cycles(const int32_t *__restrict__ ucount,
+                                                   const int32_t *__restrict__ ulist,
+                                                   const int32_t *__restrict__ strat,
+                                                   const int32_t *__restrict__ pri,
+                                                   const uint8_t *__restrict__ solved, int32_t *__restrict__ st,
+                                                   int2 *__restrict__ ja, int2 *__restrict__ jb,
+                                                   uint32_t *__restrict__ err)
+{
+    int32_t nu = *ucount;
+    if (nu == 0) return;
+    if (nu <= kSmallCycles) {
+        if (blockIdx.x == 0) cycles_body<false>(nu, ulist, strat, pri, solved, st, ja, jb, err);
+        return;
+    }
+    cycles_body<true>(nu, ulist, strat, pri, solved, st, ja, jb, err);
+}
+
+// mark_solved restricted to the last evaluation's unreached vertices: every
+// other non-solved vertex is finite.
+__global__ void k_mark_solved(const int32_t *__restrict__ ucount, const int32_t *__restrict__ ulist,
+                              int32_t player, const int32_t *__restrict__ st, uint8_t *__restrict__ solved)
+{
+    int32_t nu = *ucount;
     int32_t target = (player == 0) ? ST_POS_INF : ST_NEG_INF;
-    if (st[v] == target) solved[v] = 1;
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nu; i += gridDim.x * blockDim.x) {
+        int32_t u = ulist[i];
+        if (st[u] == target) solved[u] = 1;
+    }
+}
+
+int device_blocks(const void *kernel, int block)
+{
+    static int cached_dev = -1, cached_sms = 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != cached_dev) {
+        cudaDeviceGetAttribute(&cached_sms, cudaDevAttrMultiProcessorCount, dev);
+        cached_dev = dev;
+    }
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    return (cached_sms > 0 ? cached_sms : 1) * (per_sm > 0 ? per_sm : 1);
 }
 
 }  // namespace
 
+static std::atomic<long long> g_launches{0};
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
 void launch_init_strat(cudaStream_t s, int32_t n, const int8_t *owner, const int32_t *off,
                        const int32_t *tgt, int32_t *strat, int32_t *st)
 {
+    count_launch();
     k_init_strat<<<grid_for(n), kBlock, 0, s>>>(n, owner, off, tgt, strat, st);
 }
 
 void launch_reset_odd(cudaStream_t s, int32_t n, const int8_t *owner, const int32_t *off,
                       const int32_t *tgt, int32_t *strat)
 {
+    count_launch();
     k_reset_odd<<<grid_for(n), kBlock, 0, s>>>(n, owner, off, tgt, strat);
 }
 
-void launch_tour_init(cudaStream_t s, int32_t n, int32_t *succ, int2 *vloc)
+void launch_tour_build(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
+                       const int32_t *rev_off, const int32_t *rev_src, int32_t *succ, int2 *vloc,
+                       int32_t *sinklist, int32_t *sinkcount)
 {
+    count_launch();
     k_tour_init<<<grid_for((int64_t)n + 1), kBlock, 0, s>>>(n, succ, vloc);
+    count_launch();
+    k_tour_link<<<grid_for(n), kBlock, 0, s>>>(n, strat, solved, rev_off, rev_src, succ, sinklist, sinkcount);
+    count_launch();
+    unsigned g = grid_for(n);
+    k_sink_chain<<<g < 1216u ? g : 1216u, kBlock, 0, s>>>(n, sinklist, sinkcount, succ);
 }
 
-void launch_tour_link(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved, int32_t *succ)
+void launch_pick_heads(cudaStream_t s, int64_t L, int32_t nsub, int32_t stride, int32_t *succ, int32_t *hsucc,
+                       int2 *seg_of)
 {
-    k_tour_link<<<grid_for(n), kBlock, 0, s>>>(n, strat, solved, succ);
-}
-
-void launch_pick_heads(cudaStream_t s, int64_t L, int32_t nsub, int32_t stride, int32_t *succ, int32_t *hsucc)
-{
-    k_pick_heads<<<grid_for(nsub), kBlock, 0, s>>>(L, nsub, stride, succ, hsucc);
+    count_launch();
+    k_pick_heads<<<grid_for(nsub), kBlock, 0, s>>>(L, nsub, stride, succ, hsucc, seg_of);
 }
 
 void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, const int32_t *succ,
                           const int32_t *hsucc, int2 *vloc, int2 *red, uint32_t *err)
 {
+    count_launch();
     k_walk_sublists<<<grid_for(nsub, 128), 128, 0, s>>>(nsub, n, L, succ, hsucc, vloc, red, err);
 }
 
-void launch_wyllie_round(cudaStream_t s, int32_t nsub, const int2 *in, int2 *out)
+void launch_rank_reduced(cudaStream_t s, int32_t nsub, int32_t nseg, int32_t seg_stride, const int2 *red,
+                         int2 *seg_of, int2 *segA, int2 *segB, int2 *segfin, int2 *fin, uint32_t *err)
 {
-    k_wyllie_round<<<grid_for(nsub), kBlock, 0, s>>>(nsub, in, out);
+    count_launch();
+    k_red_walk<<<grid_for(nseg, 128), 128, 0, s>>>(nsub, nseg, seg_stride, red, seg_of, segA, err);
+    count_launch();
+    k_red_block<<<1, 1024, 0, s>>>(nseg, segA, segB, segfin);
+    count_launch();
+    k_red_finish<<<grid_for(nsub), kBlock, 0, s>>>(nsub, red, seg_of, segfin, fin);
 }
 
-void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const int2 *red,
+void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const int2 *fin,
                             const int32_t *strat, const int32_t *pri, const uint8_t *solved,
-                            int32_t *st, int2 *pp, int32_t *ulist, int32_t *ucount)
+                            int32_t *st, PathNode *node, int32_t *ulist, int32_t *ucount)
 {
-    k_broadcast_depth<<<grid_for(n), kBlock, 0, s>>>(n, vloc, red, strat, pri, solved, st, pp, ulist, ucount);
+    count_launch();
+    k_broadcast_depth<<<grid_for(n), kBlock, 0, s>>>(n, vloc, fin, strat, pri, solved, st, node, ulist, ucount);
 }
 
-void launch_jump_init(cudaStream_t s, int32_t nu, const int32_t *ulist, const int32_t *strat,
-                      const int32_t *pri, int2 *jmp, uint32_t *err)
+void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, uint32_t *err)
 {
-    if (nu > 0) k_jump_init<<<grid_for(nu), kBlock, 0, s>>>(nu, ulist, strat, pri, jmp, err);
+    count_launch();
+    k_rootinfo<<<grid_for(n), kBlock, 0, s>>>(n, st, node, err);
 }
 
-void launch_jump_round(cudaStream_t s, int32_t nu, const int32_t *ulist, const uint8_t *solved,
-                       const int2 *in, int2 *out)
+int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, const int32_t *strat,
+                  const int32_t *pri, const uint8_t *solved, int32_t *st, int2 *ja, int2 *jb, uint32_t *err)
 {
-    if (nu > 0) k_jump_round<<<grid_for(nu), kBlock, 0, s>>>(nu, ulist, solved, in, out);
+    static int blocks = 0, blocks_dev = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != blocks_dev) {
+        blocks = device_blocks((const void *)k_cycles, kBlock);
+        blocks_dev = dev;
+    }
+    void *args[] = {(void *)&ucount, (void *)&ulist, (void *)&strat, (void *)&pri, (void *)&solved,
+                    (void *)&st, (void *)&ja, (void *)&jb, (void *)&err};
+    count_launch();
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_cycles, dim3(blocks), dim3(kBlock), args, 0, s);
+    return e == cudaSuccess ? 0 : (int)e;
 }
 
-void launch_jump_finish(cudaStream_t s, int32_t nu, const int32_t *ulist, const uint8_t *solved,
-                        const int2 *jmp, int32_t *st)
+void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, int32_t player,
+                        const int32_t *st, uint8_t *solved)
 {
-    if (nu > 0) k_jump_finish<<<grid_for(nu), kBlock, 0, s>>>(nu, ulist, solved, jmp, st);
-}
-
-void launch_mark_solved(cudaStream_t s, int32_t n, int32_t player, const int32_t *st, uint8_t *solved)
-{
-    k_mark_solved<<<grid_for(n), kBlock, 0, s>>>(n, player, st, solved);
+    count_launch();
+    k_mark_solved<<<608, kBlock, 0, s>>>(ucount, ulist, player, st, solved);
 }
 
 }  // namespace psi

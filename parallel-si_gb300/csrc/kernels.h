@@ -8,41 +8,62 @@
 
 namespace psi {
 
+struct PathNode;   // device_common.cuh
+
+// Process-wide count of kernel launches issued by this library.
+void count_launch();
+long long launch_count();
+
+// ---- one-time game set-up: distinct in-neighbours of every vertex in
+// increasing order (rev_off: n+1 entries, rev_src: at most m).  Synchronous on
+// the stream; returns a cudaError_t value; *rev_m receives the entry count.
+int build_reverse_csr(cudaStream_t s, int32_t n, int64_t m, const int32_t *off, const int32_t *tgt,
+                      int32_t *rev_off, int32_t *rev_src, int64_t *rev_m);
+
 // ---- strategy set-up (gpu_parity.cu:38-56, cpu_parity.cpp:276-286, 300-307)
 void launch_init_strat(cudaStream_t s, int32_t n, const int8_t *owner, const int32_t *off,
                        const int32_t *tgt, int32_t *strat, int32_t *st);
 void launch_reset_odd(cudaStream_t s, int32_t n, const int8_t *owner, const int32_t *off,
                       const int32_t *tgt, int32_t *strat);
 
-// ---- evaluation: Euler tour, Helman-JaJa sublists, Wyllie on the reduced list
-void launch_tour_init(cudaStream_t s, int32_t n, int32_t *succ, int2 *vloc);
-void launch_tour_link(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
-                      int32_t *succ);
+// ---- evaluation (gpu_list_ranking.cu:52-277)
+// Euler tour of the sink tree.  rev_off/rev_src: distinct in-neighbours of each
+// vertex.  *sinkcount must be 0 on entry; sinklist holds n entries.
+void launch_tour_build(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
+                       const int32_t *rev_off, const int32_t *rev_src, int32_t *succ, int2 *vloc,
+                       int32_t *sinklist, int32_t *sinkcount);
 void launch_pick_heads(cudaStream_t s, int64_t L, int32_t nsub, int32_t stride, int32_t *succ,
-                       int32_t *hsucc);
+                       int32_t *hsucc, int2 *seg_of);
 void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, const int32_t *succ,
                           const int32_t *hsucc, int2 *vloc, int2 *red, uint32_t *err);
-void launch_wyllie_round(cudaStream_t s, int32_t nsub, const int2 *in, int2 *out);
-void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const int2 *red,
+// Ranks the reduced list red[0..nsub) (next, weight) from item nsub-1:
+// fin[j] = (TOUR_END if reached else 0, inclusive suffix sum).  nseg segments
+// of seg_stride items; segA/segB/segfin hold nseg entries.
+void launch_rank_reduced(cudaStream_t s, int32_t nsub, int32_t nseg, int32_t seg_stride, const int2 *red,
+                         int2 *seg_of, int2 *segA, int2 *segB, int2 *segfin, int2 *fin, uint32_t *err);
+void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const int2 *fin,
                             const int32_t *strat, const int32_t *pri, const uint8_t *solved,
-                            int32_t *st, int2 *pp, int32_t *ulist, int32_t *ucount);
-// ---- cycle parity of the vertices the sink does not reach (pointer jumping)
-void launch_jump_init(cudaStream_t s, int32_t nu, const int32_t *ulist, const int32_t *strat,
-                      const int32_t *pri, int2 *jmp, uint32_t *err);
-void launch_jump_round(cudaStream_t s, int32_t nu, const int32_t *ulist, const uint8_t *solved,
-                       const int2 *in, int2 *out);
-void launch_jump_finish(cudaStream_t s, int32_t nu, const int32_t *ulist, const uint8_t *solved,
-                        const int2 *jmp, int32_t *st);
-void launch_mark_solved(cudaStream_t s, int32_t n, int32_t player, const int32_t *st,
-                        uint8_t *solved);
+                            int32_t *st, PathNode *node, int32_t *ulist, int32_t *ucount);
+// Root-path summaries (rmax, rcnt) of every reached vertex.
+void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, uint32_t *err);
+// Cycle parity of the *ucount vertices in ulist (cooperative launch); returns
+// a cudaError_t value.
+int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, const int32_t *strat,
+                  const int32_t *pri, const uint8_t *solved, int32_t *st, int2 *ja, int2 *jb, uint32_t *err);
+// mark_solved over the last evaluation's unreached vertices (cpu_parity.cpp:265-274)
+void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, int32_t player,
+                        const int32_t *st, uint8_t *solved);
 
 // ---- all-switches (gpu_parity.cu:191-317, cpu_parity.cpp:154-263)
-void launch_switch(cudaStream_t s, int32_t n, int32_t player, const int8_t *owner,
+// Switches the np vertices listed in plist (all owned by `player`).
+// stats[0..3] += compared edges, walk loads, changed vertices, strict
+// improvements.
+void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player,
                    const int32_t *off, const int32_t *tgt, int32_t *strat, const int32_t *st,
-                   const int2 *pp, unsigned long long *count, uint32_t *err);
+                   const PathNode *node, unsigned long long *stats, uint32_t *err);
 // ---- dense valuation rows for export (the reference's ArrayVal layout)
 void launch_materialize(cudaStream_t s, int32_t v0, int32_t count, int32_t d, const int32_t *st,
-                        const int2 *pp, int32_t *rows, uint32_t *err);
+                        const PathNode *node, int32_t *rows, uint32_t *err);
 
 }  // namespace psi
 

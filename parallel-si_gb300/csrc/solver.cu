@@ -62,10 +62,17 @@ int Solver::alloc(const HostGame &g, const psi_options &)
     L_ = 2 * (int64_t)n_ + 2;
     // heads at node j*stride for j < nsub-1, plus the list start (node L-1)
     nsub_ = (int32_t)(ceil_div(L_ - 1, stride_) + 1);
+    // second level: segments of seg_stride sublists, few enough for one block
+    seg_stride_ = (int32_t)std::max<int64_t>(32, ceil_div(nsub_, 8192));
+    nseg_ = (int32_t)(ceil_div(nsub_ - 1, seg_stride_) + 1);
     game_ = &g;
     PSI_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
-    PSI_CUDA_TRY(cudaEventCreate(&ev0_));
-    PSI_CUDA_TRY(cudaEventCreate(&ev1_));
+    for (auto &p : ph_) {
+        PSI_CUDA_TRY(cudaEventCreate(&p.a));
+        PSI_CUDA_TRY(cudaEventCreate(&p.b));
+    }
+    PSI_CUDA_TRY(cudaEventCreate(&region_a_));
+    PSI_CUDA_TRY(cudaEventCreate(&region_b_));
 
     auto dalloc = [&](void **p, size_t bytes) -> int {
         cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
@@ -82,23 +89,43 @@ int Solver::alloc(const HostGame &g, const psi_options &)
     PSI_DALLOC(pri_, 4 * (size_t)n_);
     PSI_DALLOC(off_, 4 * ((size_t)n_ + 1));
     PSI_DALLOC(tgt_, 4 * (size_t)m_);
+    PSI_DALLOC(plist_, 4 * (size_t)n_);
     PSI_DALLOC(strat_, 4 * (size_t)n_);
     PSI_DALLOC(st_, 4 * (size_t)n_);
     PSI_DALLOC(solved_, n_);
-    PSI_DALLOC(pp_, 8 * (size_t)n_);
+    PSI_DALLOC(node_, sizeof(PathNode) * (size_t)n_);
     PSI_DALLOC(succ_, 4 * (size_t)L_);
     PSI_DALLOC(hsucc_, 4 * (size_t)nsub_);
     PSI_DALLOC(ulist_, 4 * (size_t)n_);
     PSI_DALLOC(vloc_, 8 * (size_t)n_);
     PSI_DALLOC(redA_, 8 * (size_t)nsub_);
     PSI_DALLOC(redB_, 8 * (size_t)nsub_);
+    PSI_DALLOC(seg_of_, 8 * (size_t)nsub_);
+    PSI_DALLOC(segA_, 8 * (size_t)nseg_);
+    PSI_DALLOC(segB_, 8 * (size_t)nseg_);
+    PSI_DALLOC(segfin_, 8 * (size_t)nseg_);
     PSI_DALLOC(jA_, 8 * (size_t)n_);
     PSI_DALLOC(jB_, 8 * (size_t)n_);
     PSI_DALLOC(dw_, sizeof(Words));
 #undef PSI_DALLOC
     PSI_CUDA_TRY(cudaMallocHost((void **)&hw_, sizeof(Words)));
 
+    {
+        int r1 = dalloc((void **)&rev_off_, 4 * ((size_t)n_ + 1));
+        if (r1) return r1;
+        int r2 = dalloc((void **)&rev_src_, 4 * std::max<size_t>((size_t)m_, 1));
+        if (r2) return r2;
+    }
+
     std::vector<int8_t> own8(g.owner.begin(), g.owner.end());
+    std::vector<int32_t> plist;
+    plist.reserve(n_);
+    for (int32_t v = 0; v < n_; v++)
+        if (g.owner[v] == 0) plist.push_back(v);
+    np0_ = (int32_t)plist.size();
+    for (int32_t v = 0; v < n_; v++)
+        if (g.owner[v] == 1) plist.push_back(v);
+    PSI_CUDA_TRY(cudaMemcpyAsync(plist_, plist.data(), 4 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
     PSI_CUDA_TRY(cudaMemcpyAsync(owner_, own8.data(), n_, cudaMemcpyHostToDevice, stream_));
     PSI_CUDA_TRY(cudaMemcpyAsync(pri_, g.priority.data(), 4 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
     PSI_CUDA_TRY(cudaMemcpyAsync(off_, g.offsets.data(), 4 * ((size_t)n_ + 1), cudaMemcpyHostToDevice, stream_));
@@ -106,6 +133,10 @@ int Solver::alloc(const HostGame &g, const psi_options &)
     PSI_CUDA_TRY(cudaMemsetAsync(solved_, 0, n_, stream_));
     PSI_CUDA_TRY(cudaMemsetAsync(st_, 0, 4 * (size_t)n_, stream_));
     PSI_CUDA_TRY(cudaMemsetAsync(dw_, 0, sizeof(Words), stream_));
+    // reverse CSR on the device (distinct in-neighbours, increasing order)
+    int64_t rev_m = 0;
+    int ce = build_reverse_csr(stream_, n_, m_, off_, tgt_, rev_off_, rev_src_, &rev_m);
+    if (ce) return fail(PSI_ERR_CUDA, std::string("reverse CSR: ") + cudaGetErrorString((cudaError_t)ce));
     PSI_CUDA_TRY(cudaStreamSynchronize(stream_));
     game_ = nullptr;
     return PSI_OK;
@@ -117,9 +148,61 @@ Solver::~Solver()
     if (stream_) cudaStreamSynchronize(stream_);
     for (void *p : allocs_) cudaFree(p);
     if (hw_) cudaFreeHost(hw_);
-    if (ev0_) cudaEventDestroy(ev0_);
-    if (ev1_) cudaEventDestroy(ev1_);
+    for (auto &p : ph_) {
+        if (p.a) cudaEventDestroy(p.a);
+        if (p.b) cudaEventDestroy(p.b);
+    }
+    if (region_a_) cudaEventDestroy(region_a_);
+    if (region_b_) cudaEventDestroy(region_b_);
     if (stream_) cudaStreamDestroy(stream_);
+}
+
+int Solver::timer_begin()
+{
+    int rc = set_device();
+    if (rc) return rc;
+    PSI_CUDA_TRY(cudaStreamSynchronize(stream_));
+    PSI_CUDA_TRY(cudaEventRecord(region_a_, stream_));
+    return PSI_OK;
+}
+
+int Solver::timer_end(double *ms)
+{
+    int rc = set_device();
+    if (rc) return rc;
+    PSI_CUDA_TRY(cudaEventRecord(region_b_, stream_));
+    PSI_CUDA_TRY(cudaEventSynchronize(region_b_));
+    float f = 0;
+    PSI_CUDA_TRY(cudaEventElapsedTime(&f, region_a_, region_b_));
+    *ms = f;
+    return PSI_OK;
+}
+
+void Solver::phase_begin(Phase p)
+{
+    if (timing_) cudaEventRecord(ph_[p].a, stream_);
+}
+
+void Solver::phase_end(Phase p)
+{
+    if (!timing_) return;
+    cudaEventRecord(ph_[p].b, stream_);
+    ph_[p].pending = true;
+}
+
+// Called after a stream synchronisation: adds the elapsed time of every phase
+// recorded since the last collection.
+int Solver::collect_phases()
+{
+    for (int i = 0; i < PH_COUNT; i++) {
+        if (!ph_[i].pending) continue;
+        float ms = 0;
+        PSI_CUDA_TRY(cudaEventElapsedTime(&ms, ph_[i].a, ph_[i].b));
+        times_.ms[i] += ms;
+        times_.calls[i]++;
+        ph_[i].pending = false;
+    }
+    return PSI_OK;
 }
 
 int Solver::sync_and_check(const char *what)
@@ -128,6 +211,8 @@ int Solver::sync_and_check(const char *what)
     PSI_CUDA_TRY(cudaMemcpyAsync(hw_, dw_, sizeof(Words), cudaMemcpyDeviceToHost, stream_));
     cudaError_t e = cudaStreamSynchronize(stream_);
     if (e != cudaSuccess) return fail(PSI_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    int rc = collect_phases();
+    if (rc) return rc;
     if (hw_->err) {
         uint32_t bits = hw_->err;
         cudaMemsetAsync(dw_, 0, sizeof(Words), stream_);
@@ -164,45 +249,39 @@ int Solver::compute_valuation()
     if (!strat_ready_) return fail(PSI_ERR_STATE, "compute_valuation before init_strat");
     int rc = set_device();
     if (rc) return rc;
-    if (timing_) PSI_CUDA_TRY(cudaEventRecord(ev0_, stream_));
+    phase_begin(PH_EVAL);
     // 1. Euler tour of the sink tree
-    launch_tour_init(stream_, n_, succ_, vloc_);
-    launch_tour_link(stream_, n_, strat_, solved_, succ_);
-    // 2. Helman-JaJa sublists + Wyllie over the reduced list
-    launch_pick_heads(stream_, L_, nsub_, stride_, succ_, hsucc_);
+    phase_begin(PH_TOUR);
+    PSI_CUDA_TRY(cudaMemsetAsync(&dw_->ucount, 0, 2 * sizeof(int32_t), stream_));   // ucount, sinkcount
+    launch_tour_build(stream_, n_, strat_, solved_, rev_off_, rev_src_, succ_, vloc_, ulist_, &dw_->sinkcount);
+    launch_pick_heads(stream_, L_, nsub_, stride_, succ_, hsucc_, seg_of_);
+    phase_end(PH_TOUR);
+    // 2. Helman-JaJa sublists, then the reduced list ranked on the device
+    phase_begin(PH_SUBLIST);
     launch_walk_sublists(stream_, nsub_, n_, L_, succ_, hsucc_, vloc_, redA_, &dw_->err);
-    int rounds = ceil_log2(nsub_) + 1;
-    int2 *in = redA_, *out = redB_;
-    for (int r = 0; r < rounds; r++) {
-        launch_wyllie_round(stream_, nsub_, in, out);
-        std::swap(in, out);
-    }
+    phase_end(PH_SUBLIST);
+    phase_begin(PH_REDUCED);
+    launch_rank_reduced(stream_, nsub_, nseg_, seg_stride_, redA_, seg_of_, segA_, segB_, segfin_, redB_,
+                        &dw_->err);
+    phase_end(PH_REDUCED);
     // 3. broadcast depths; collect the vertices the sink does not reach
-    PSI_CUDA_TRY(cudaMemsetAsync(&dw_->ucount, 0, sizeof(int32_t), stream_));
-    launch_broadcast_depth(stream_, n_, vloc_, in, strat_, pri_, solved_, st_, pp_, ulist_, &dw_->ucount);
-    rc = sync_and_check("compute_valuation (ranking)");
+    //    (ulist held the sink's children until here)
+    phase_begin(PH_BROADCAST);
+    launch_broadcast_depth(stream_, n_, vloc_, redB_, strat_, pri_, solved_, st_, node_, ulist_, &dw_->ucount);
+    launch_rootinfo(stream_, n_, st_, node_, &dw_->err);
+    phase_end(PH_BROADCAST);
+    // 4. cycle parity by pointer jumping over the unreached vertices
+    phase_begin(PH_CYCLES);
+    int ce = launch_cycles(stream_, &dw_->ucount, ulist_, strat_, pri_, solved_, st_, jA_, jB_, &dw_->err);
+    if (ce) return fail(PSI_ERR_CUDA, std::string("cycle kernel launch: ") + cudaGetErrorString((cudaError_t)ce));
+    phase_end(PH_CYCLES);
+    phase_end(PH_EVAL);
+    rc = sync_and_check("compute_valuation");
     if (rc) return rc;
     int32_t nu = hw_->ucount;
     last_unreached_ = nu;
-    // 4. cycle parity by pointer jumping over the unreached vertices
-    if (nu > 0) {
-        launch_jump_init(stream_, nu, ulist_, strat_, pri_, jA_, &dw_->err);
-        int jr = ceil_log2(nu) + 1;
-        int2 *ja = jA_, *jb = jB_;
-        for (int r = 0; r < jr; r++) {
-            launch_jump_round(stream_, nu, ulist_, solved_, ja, jb);
-            std::swap(ja, jb);
-        }
-        launch_jump_finish(stream_, nu, ulist_, solved_, ja, st_);
-    }
-    if (timing_) PSI_CUDA_TRY(cudaEventRecord(ev1_, stream_));
-    rc = sync_and_check("compute_valuation");
-    if (rc) return rc;
-    if (timing_) {
-        float ms = 0;
-        PSI_CUDA_TRY(cudaEventElapsedTime(&ms, ev0_, ev1_));
-        times_.eval_ms += ms;
-    }
+    times_.unreached += nu;
+    if (nu > 0) times_.jump_rounds += ceil_log2(nu) + 1;
     times_.evals++;
     val_ready_ = true;
     return PSI_OK;
@@ -214,7 +293,7 @@ int Solver::mark_solved(int32_t player)
     if (!val_ready_) return fail(PSI_ERR_STATE, "mark_solved before compute_valuation");
     int rc = set_device();
     if (rc) return rc;
-    launch_mark_solved(stream_, n_, player, st_, solved_);
+    launch_mark_solved(stream_, &dw_->ucount, ulist_, player, st_, solved_);
     PSI_CUDA_TRY(cudaGetLastError());
     return PSI_OK;   // ordered on the stream before the next call
 }
@@ -225,19 +304,19 @@ int Solver::switch_strategy(int32_t player, int64_t *switched)
     if (!val_ready_) return fail(PSI_ERR_STATE, "switch_strategy before compute_valuation");
     int rc = set_device();
     if (rc) return rc;
-    PSI_CUDA_TRY(cudaMemsetAsync(&dw_->count, 0, sizeof(unsigned long long), stream_));
-    if (timing_) PSI_CUDA_TRY(cudaEventRecord(ev0_, stream_));
-    launch_switch(stream_, n_, player, owner_, off_, tgt_, strat_, st_, pp_, &dw_->count, &dw_->err);
-    if (timing_) PSI_CUDA_TRY(cudaEventRecord(ev1_, stream_));
+    PSI_CUDA_TRY(cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_));
+    phase_begin(PH_SWITCH);
+    const int32_t np = (player == 0) ? np0_ : n_ - np0_;
+    const int32_t *pl = plist_ + (player == 0 ? 0 : np0_);
+    launch_switch(stream_, np, pl, player, off_, tgt_, strat_, st_, node_, dw_->sw, &dw_->err);
+    phase_end(PH_SWITCH);
     rc = sync_and_check("switch_strategy");
     if (rc) return rc;
-    if (timing_) {
-        float ms = 0;
-        PSI_CUDA_TRY(cudaEventElapsedTime(&ms, ev0_, ev1_));
-        times_.switch_ms += ms;
-    }
     times_.switches++;
-    if (switched) *switched = (int64_t)hw_->count;
+    times_.sw_edges += (int64_t)hw_->sw[0];
+    times_.sw_loads += (int64_t)hw_->sw[1];
+    times_.sw_changed += (int64_t)hw_->sw[2];
+    if (switched) *switched = (int64_t)hw_->sw[3];
     return PSI_OK;
 }
 
@@ -330,7 +409,7 @@ int Solver::get_valuation(int32_t v0, int32_t count, int32_t *out)
     int32_t *rows = nullptr;
     cudaError_t e = cudaMallocAsync((void **)&rows, (size_t)bytes, stream_);
     if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, "valuation export buffer");
-    launch_materialize(stream_, v0, count, (int32_t)d, st_, pp_, rows, &dw_->err);
+    launch_materialize(stream_, v0, count, (int32_t)d, st_, node_, rows, &dw_->err);
     PSI_CUDA_TRY(cudaMemcpyAsync(out, rows, (size_t)bytes, cudaMemcpyDeviceToHost, stream_));
     PSI_CUDA_TRY(cudaFreeAsync(rows, stream_));
     return sync_and_check("get_valuation");

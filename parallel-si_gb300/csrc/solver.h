@@ -12,9 +12,20 @@
 
 namespace psi {
 
+struct PathNode;   // device_common.cuh
+
+// Device time per phase, summed over calls (CUDA events on the solver stream).
+enum Phase { PH_EVAL = 0, PH_SWITCH, PH_TOUR, PH_SUBLIST, PH_REDUCED, PH_BROADCAST, PH_CYCLES, PH_COUNT };
+
 struct SolverTimes {
-    double eval_ms = 0, switch_ms = 0;   // device time, summed over calls (CUDA events)
+    double ms[PH_COUNT] = {0};
+    int64_t calls[PH_COUNT] = {0};
     int64_t evals = 0, switches = 0;
+    // work counters: switch steps (compared edges, walk loads of the
+    // parent/priority snapshot, changed vertices) and evaluations (vertices
+    // the sink did not reach, pointer-jumping rounds over them)
+    int64_t sw_edges = 0, sw_loads = 0, sw_changed = 0;
+    int64_t unreached = 0, jump_rounds = 0;
 };
 
 class Solver {
@@ -47,6 +58,9 @@ public:
     const SolverTimes &times() const { return times_; }
     void reset_times() { times_ = SolverTimes(); }
     int last_unreached() const { return last_unreached_; }
+    // Region timer: CUDA events on the solver stream, synchronised at the end.
+    int timer_begin();
+    int timer_end(double *ms);
 
 private:
     Solver() = default;
@@ -56,8 +70,16 @@ private:
 
     int device_ = 0;
     cudaStream_t stream_ = nullptr;
-    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    struct PhaseEvents {
+        cudaEvent_t a = nullptr, b = nullptr;
+        bool pending = false;
+    };
+    PhaseEvents ph_[PH_COUNT];
+    cudaEvent_t region_a_ = nullptr, region_b_ = nullptr;
     bool timing_ = true;
+    void phase_begin(Phase p);
+    void phase_end(Phase p);
+    int collect_phases();
     SolverTimes times_;
     const HostGame *game_ = nullptr;
 
@@ -66,21 +88,27 @@ private:
     bool strat_ready_ = false, val_ready_ = false;
     int last_unreached_ = 0;
 
-    // game (device)
+    // game (device); plist_ lists Even's vertices then Odd's (np0_ of them are Even's)
     int8_t *owner_ = nullptr;
-    int32_t *pri_ = nullptr, *off_ = nullptr, *tgt_ = nullptr;
+    int32_t *pri_ = nullptr, *off_ = nullptr, *tgt_ = nullptr, *plist_ = nullptr;
+    int32_t np0_ = 0;
     // state
     int32_t *strat_ = nullptr, *st_ = nullptr;
     uint8_t *solved_ = nullptr;
-    int2 *pp_ = nullptr;
+    PathNode *node_ = nullptr;   // parent, priority and root-path summary (evaluation snapshot)
     // evaluation scratch
     int32_t *succ_ = nullptr, *hsucc_ = nullptr, *ulist_ = nullptr;
+    int32_t *rev_off_ = nullptr, *rev_src_ = nullptr;   // distinct in-neighbours (static)
     int2 *vloc_ = nullptr, *redA_ = nullptr, *redB_ = nullptr, *jA_ = nullptr, *jB_ = nullptr;
+    int2 *seg_of_ = nullptr, *segA_ = nullptr, *segB_ = nullptr, *segfin_ = nullptr;
+    int32_t nseg_ = 0, seg_stride_ = 32;
     // small device words + pinned host mirrors
     struct Words {
-        unsigned long long count;
+        unsigned long long sw[4];   // switch counters (launch_switch)
         uint32_t err;
-        int32_t ucount;
+        int32_t ucount;             // vertices the sink did not reach
+        int32_t sinkcount;          // children of the sink (tour build)
+        int32_t pad;
     };
     Words *dw_ = nullptr, *hw_ = nullptr;
     std::vector<void *> allocs_;

@@ -6,15 +6,18 @@
 // count at the highest priority where the counts differ if that priority is
 // even, the smaller count if it is odd.
 //
-// The counts on the common part of two paths (from their lowest common
-// ancestor in the sink tree down to the sink) cancel, so a comparison only
-// needs the two path segments above the LCA.  The kernel walks them with the
-// parent/priority snapshot and depths of the last evaluation, keeping the two
-// highest distinct priorities and their counts per side; that settles the
-// comparison unless both sides agree on both, in which case it walks again
-// below the second priority.  Every pass removes at least two distinct
-// priorities, so the number of passes is bounded by the path lengths and the
-// result is exact.
+// A comparison of two finite valuations u, w is settled in three tiers, each
+// exact:
+//  1. u == w: equal.
+//  2. Root-path summaries (highest priority M on the path, its count c), made
+//     by the evaluation: if (M_u, c_u) != (M_w, c_w), the highest priority
+//     whose counts differ is max(M_u, M_w) -- every higher priority is absent
+//     from both paths -- and its two counts are known.
+//  3. Otherwise walk both paths up to their lowest common ancestor (the counts
+//     on the common part cancel), keeping the two highest distinct priorities
+//     and their counts per side; if both sides agree on both, walk again below
+//     the second one.  Every pass removes at least two distinct priorities, so
+//     the passes are bounded by the path lengths.
 //
 // The switch rule is the reference's (cpu_parity.cpp:239-263,
 // gpu_parity.cu:264-300): scan the successors in CSR order, move to a
@@ -63,44 +66,36 @@ __device__ __forceinline__ int decide(int32_t p, int32_t ca, int32_t cb)
     return ca < cb ? 1 : -1;
 }
 
-// Exact comparison of two finite valuations (u, w: vertices or -1 = sink; du,
-// dw: their depths, 0 for the sink).
-__device__ int walk_compare(const int2 *__restrict__ pp, int32_t u, int32_t du, int32_t w, int32_t dw,
-                            uint32_t *__restrict__ err)
+// Tier 3: walks to the lowest common ancestor of u and w (depths du, dw; w may
+// be the sink, -1 with depth 0).
+__device__ int walk_compare(const PathNode *__restrict__ node, int32_t u, int32_t du, int32_t w, int32_t dw,
+                            int32_t &loads, uint32_t *__restrict__ err)
 {
     int32_t thr = INT_MAX;
     const int32_t max_pass = (du + dw) / 2 + 2;
     for (int32_t pass = 0; pass < max_pass; pass++) {
         Top2 A = {-1, 0, -1, 0}, B = {-1, 0, -1, 0};
         int32_t a = u, b = w, da = du, db = dw;
-        while (da > db) {
-            if (a < 0) break;
-            int2 q = pp[a];
-            if (q.y < thr) top2_add(A, q.y);
-            a = q.x;
-            da--;
-        }
-        while (db > da) {
-            if (b < 0) break;
-            int2 q = pp[b];
-            if (q.y < thr) top2_add(B, q.y);
-            b = q.x;
-            db--;
-        }
-        while (a != b && da > 0) {
-            if (a < 0 || b < 0) break;
-            int2 qa = pp[a];
-            int2 qb = pp[b];
-            if (qa.y < thr) top2_add(A, qa.y);
-            if (qb.y < thr) top2_add(B, qb.y);
-            a = qa.x;
-            b = qb.x;
-            da--;
-            db--;
-        }
-        if (a != b || da != db) {
-            atomicOr(err, DERR_WALK_CAP);
-            return 0;
+        while (a != b || da != db) {
+            bool adv_a = da >= db, adv_b = db >= da;
+            if ((adv_a && (a < 0 || da <= 0)) || (adv_b && (b < 0 || db <= 0))) {   // inconsistent: cannot happen
+                atomicOr(err, DERR_WALK_CAP);
+                return 0;
+            }
+            if (adv_a) {
+                int2 q = *reinterpret_cast<const int2 *>(&node[a]);
+                loads++;
+                if (q.y < thr) top2_add(A, q.y);
+                a = q.x;
+                da--;
+            }
+            if (adv_b) {
+                int2 q = *reinterpret_cast<const int2 *>(&node[b]);
+                loads++;
+                if (q.y < thr) top2_add(B, q.y);
+                b = q.x;
+                db--;
+            }
         }
         int32_t M1 = max(A.m1, B.m1);
         if (M1 < 0) return 0;
@@ -117,50 +112,85 @@ __device__ int walk_compare(const int2 *__restrict__ pp, int32_t u, int32_t du, 
     return 0;
 }
 
-// cpu_parity.cpp:194-236: +1 if u is better than w for Even, 0 if equal.
-__device__ __forceinline__ int compare_vals(const int32_t *__restrict__ st, const int2 *__restrict__ pp,
-                                            int32_t u, int32_t w, uint32_t *__restrict__ err)
+// Comparison of finite u and w, u != w; ru, rw their root-path summaries
+// ((-1, 0) for the sink).
+__device__ __forceinline__ int compare_finite(const PathNode *__restrict__ node, int32_t u, int32_t su, int2 ru,
+                                              int32_t w, int32_t sw, int2 rw, int32_t &loads,
+                                              uint32_t *__restrict__ err)
 {
-    int32_t su = (u >= 0) ? st[u] : 0;
-    int32_t sw = (w >= 0) ? st[w] : 0;
-    int iu = st_infinite(su), iw = st_infinite(sw);
-    if (iu && iw) return iu == iw ? 0 : (iu == 1 ? 1 : -1);
-    if (iu) return iu == 1 ? 1 : -1;
-    if (iw) return iw == 1 ? -1 : 1;
-    return walk_compare(pp, u, su, w, sw, err);
+    if (ru.x != rw.x) return ru.x > rw.x ? decide(ru.x, ru.y, 0) : decide(rw.x, 0, rw.y);
+    if (ru.y != rw.y) return decide(ru.x, ru.y, rw.y);
+    return walk_compare(node, u, su, w, sw, loads, err);
 }
 
-__global__ void k_switch(int32_t n, int32_t player, const int8_t *__restrict__ owner,
-                         const int32_t *__restrict__ off, const int32_t *__restrict__ tgt,
-                         int32_t *__restrict__ strat, const int32_t *__restrict__ st,
-                         const int2 *__restrict__ pp, unsigned long long *__restrict__ count,
-                         uint32_t *__restrict__ err)
+__device__ __forceinline__ int2 summary_of(const PathNode *__restrict__ node, int32_t x, int32_t sx)
 {
-    typedef cub::BlockReduce<int32_t, kBlock> Reduce;
-    __shared__ typename Reduce::TempStorage tmp;
-    int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    int32_t moves = 0;
-    if (v < n && owner[v] == player) {
+    return (x >= 0 && sx >= 1) ? *reinterpret_cast<const int2 *>(&node[x].rmax) : make_int2(-1, 0);
+}
+
+// One thread per vertex of plist (all owned by `player`).
+// stats[0] += compared edges, stats[1] += parent/priority loads of tier-3
+// walks, stats[2] += vertices whose strategy changed, stats[3] += strict
+// improvements.
+__global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__restrict__ plist, int32_t player,
+                                                   const int32_t *__restrict__ off, const int32_t *__restrict__ tgt,
+                                                   int32_t *__restrict__ strat, const int32_t *__restrict__ st,
+                                                   const PathNode *__restrict__ node,
+                                                   unsigned long long *__restrict__ stats,
+                                                   uint32_t *__restrict__ err)
+{
+    int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    int32_t n_edges = 0, n_loads = 0, moves = 0;
+    if (i < np) {
+        int32_t v = plist[i];
         int32_t cur = strat[v];
-        int32_t e1 = off[v + 1];
-        for (int32_t e = off[v]; e < e1; e++) {
+        int32_t scur = (cur >= 0) ? st[cur] : 0;
+        int2 rcur = summary_of(node, cur, scur);
+        int32_t e0 = off[v], e1 = off[v + 1];
+        n_edges = e1 - e0;
+        for (int32_t e = e0; e < e1; e++) {
             int32_t u = tgt[e];
-            int c = compare_vals(st, pp, u, cur, err);
+            int32_t su = st[u];
+            int iu = st_infinite(su), ic = st_infinite(scur);
+            int c;
+            bool have_ru = false;
+            int2 ru = make_int2(-1, 0);
+            if (iu | ic) {
+                c = (iu && ic) ? (iu == ic ? 0 : (iu == 1 ? 1 : -1)) : (iu ? iu : -ic);
+            } else if (u == cur) {
+                c = 0;
+            } else {
+                ru = summary_of(node, u, su);
+                have_ru = true;
+                c = compare_finite(node, u, su, ru, cur, scur, rcur, n_loads, err);
+            }
             if ((player == 0 && c > 0) || (player == 1 && c < 0)) {
                 cur = u;
+                scur = su;
+                rcur = have_ru ? ru : summary_of(node, u, su);
                 moves++;
             }
         }
         if (moves) strat[v] = cur;
     }
-    int32_t total = Reduce(tmp).Sum(moves);
-    if (threadIdx.x == 0 && total) atomicAdd(count, (unsigned long long)total);
+    typedef cub::BlockReduce<int4, kBlock> Reduce;
+    __shared__ typename Reduce::TempStorage tmp;
+    int4 mine = make_int4(n_edges, n_loads, moves ? 1 : 0, moves);
+    int4 tot = Reduce(tmp).Reduce(mine, [](const int4 &x, const int4 &y) {
+        return make_int4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
+    });
+    if (threadIdx.x == 0) {
+        if (tot.x) atomicAdd(&stats[0], (unsigned long long)tot.x);
+        if (tot.y) atomicAdd(&stats[1], (unsigned long long)tot.y);
+        if (tot.z) atomicAdd(&stats[2], (unsigned long long)tot.z);
+        if (tot.w) atomicAdd(&stats[3], (unsigned long long)tot.w);
+    }
 }
 
 // Dense row of v: counts of the priorities on its strategy path (the reference
 // layout, vals[v][p]); rows of infinite vertices are left zero.
 __global__ void k_materialize(int32_t v0, int32_t count, int32_t d, const int32_t *__restrict__ st,
-                              const int2 *__restrict__ pp, int32_t *__restrict__ rows,
+                              const PathNode *__restrict__ node, int32_t *__restrict__ rows,
                               uint32_t *__restrict__ err)
 {
     int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -175,7 +205,7 @@ __global__ void k_materialize(int32_t v0, int32_t count, int32_t d, const int32_
             atomicOr(err, DERR_WALK_CAP);
             return;
         }
-        int2 q = pp[x];
+        int2 q = *reinterpret_cast<const int2 *>(&node[x]);
         row[q.y] += 1;
         x = q.x;
     }
@@ -183,17 +213,22 @@ __global__ void k_materialize(int32_t v0, int32_t count, int32_t d, const int32_
 
 }  // namespace
 
-void launch_switch(cudaStream_t s, int32_t n, int32_t player, const int8_t *owner, const int32_t *off,
-                   const int32_t *tgt, int32_t *strat, const int32_t *st, const int2 *pp,
-                   unsigned long long *count, uint32_t *err)
+void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player, const int32_t *off,
+                   const int32_t *tgt, int32_t *strat, const int32_t *st, const PathNode *node,
+                   unsigned long long *stats, uint32_t *err)
 {
-    k_switch<<<grid_for(n), kBlock, 0, s>>>(n, player, owner, off, tgt, strat, st, pp, count, err);
+    if (np <= 0) return;
+    count_launch();
+    k_switch<<<grid_for(np), kBlock, 0, s>>>(np, plist, player, off, tgt, strat, st, node, stats, err);
 }
 
 void launch_materialize(cudaStream_t s, int32_t v0, int32_t count, int32_t d, const int32_t *st,
-                        const int2 *pp, int32_t *rows, uint32_t *err)
+                        const PathNode *node, int32_t *rows, uint32_t *err)
 {
-    if (count > 0) k_materialize<<<grid_for(count, 128), 128, 0, s>>>(v0, count, d, st, pp, rows, err);
+    if (count > 0) {
+        count_launch();
+        k_materialize<<<grid_for(count, 128), 128, 0, s>>>(v0, count, d, st, node, rows, err);
+    }
 }
 
 }  // namespace psi

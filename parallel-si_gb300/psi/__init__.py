@@ -14,7 +14,12 @@ from typing import List, Optional
 
 import numpy as np
 
-from ._lib import (PSI_VAL_PATH, Options, PsiError, check, last_error, lib, ptr)
+from ._lib import (COUNTERS, PHASES, PSI_VAL_PATH, Options, PsiError, check, last_error, lib, ptr)
+
+
+def launch_count() -> int:
+    """Kernel launches issued by the native library in this process."""
+    return int(lib.psi_launch_count())
 
 __all__ = ["Game", "GPUList", "PsiError", "Options", "solve_si", "default_options", "version"]
 
@@ -208,6 +213,39 @@ class GPUList:
 
     def reset_times(self) -> None:
         check(lib.psi_solver_reset_times(self._h))
+
+    def phase_times(self):
+        """{phase: (ms, calls)} of the device phases since the last reset."""
+        k = len(PHASES)
+        ms = (C.c_double * k)()
+        calls = (C.c_int64 * k)()
+        check(lib.psi_solver_phase_times(self._h, ms, calls, k))
+        return {p: (ms[i], calls[i]) for i, p in enumerate(PHASES)}
+
+    def counters(self):
+        """Work counters since the last reset (psi_solver_counters)."""
+        out = (C.c_int64 * len(COUNTERS))()
+        check(lib.psi_solver_counters(self._h, out, len(COUNTERS)))
+        return {k: out[i] for i, k in enumerate(COUNTERS)}
+
+    def timer_begin(self) -> None:
+        check(lib.psi_solver_timer_begin(self._h))
+
+    def timer_end(self) -> float:
+        ms = C.c_double()
+        check(lib.psi_solver_timer_end(self._h, C.byref(ms)))
+        return ms.value
+
+    def stream_handle(self) -> int:
+        """The solver's cudaStream_t as an integer."""
+        h = C.c_void_p()
+        check(lib.psi_solver_stream(self._h, C.byref(h)))
+        return h.value or 0
+
+    def unreached(self) -> int:
+        k = C.c_int64()
+        check(lib.psi_solver_unreached(self._h, C.byref(k)))
+        return k.value
 
     def close(self) -> None:
         if self._h:

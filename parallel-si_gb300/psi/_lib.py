@@ -88,7 +88,18 @@ _SIGS = {
     "psi_solve": ([_vp, C.c_int32, _i32p, _i32p, C.c_int64], C.c_int),
     "psi_solver_times": ([_vp, C.POINTER(C.c_double), C.POINTER(C.c_double), _i64p, _i64p], C.c_int),
     "psi_solver_reset_times": ([_vp], C.c_int),
+    "psi_solver_phase_times": ([_vp, C.POINTER(C.c_double), _i64p, C.c_int32], C.c_int),
+    "psi_solver_stream": ([_vp, _pp], C.c_int),
+    "psi_solver_unreached": ([_vp, _i64p], C.c_int),
+    "psi_solver_counters": ([_vp, _i64p, C.c_int32], C.c_int),
+    "psi_launch_count": ([], C.c_int64),
+    "psi_solver_timer_begin": ([_vp], C.c_int),
+    "psi_solver_timer_end": ([_vp, C.POINTER(C.c_double)], C.c_int),
 }
+
+COUNTERS = ("evals", "switches", "sw_edges", "sw_loads", "sw_changed", "unreached", "jump_rounds")
+
+PHASES = ("eval", "switch", "tour", "sublist", "reduced", "broadcast", "cycles")
 
 for _name, (_args, _res) in _SIGS.items():
     _f = getattr(lib, _name)
