@@ -1,0 +1,219 @@
+// psi_si.hpp -- C++ mirror of the reference solver interface over the C ABI.
+//
+// Header-only.  It gives C++ callers the shape of the reference's classes so
+// a driver written against them keeps its structure:
+//   psi::Game           ~ Game (game.h:9-34): parse_pgsolver, get_n_vertices,
+//                          get_max_pri, get_player, get_priority, get_edges
+//   psi::StrategyImprovement ~ StrategyImprovement (si.h:6-16)
+//   psi::GPUList        ~ GPUList(Game&, GPUGame&) (gpu_list_ranking.h:11-41):
+//                          the GPU solver; constructing it uploads the game
+//   psi::solve_si       ~ solve_si (main.cpp:20-55, gpumain.cpp:18-53)
+// Failures become psi::Error exceptions carrying the C ABI status and message
+// (the reference exits on CUDA errors, gpu_util.cpp:10-17, and throws
+// const char* on parse errors, game.cpp:68-105).
+#ifndef PSI_SI_HPP
+#define PSI_SI_HPP
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "psi.h"
+
+namespace psi {
+
+class Error : public std::runtime_error {
+public:
+    Error(int code, const std::string &msg) : std::runtime_error(msg), code_(code) {}
+    int code() const { return code_; }
+
+private:
+    int code_;
+};
+
+inline void check(int rc)
+{
+    if (rc != PSI_OK) throw Error(rc, psi_last_error());
+}
+
+class Game {
+public:
+    Game() = default;
+    explicit Game(psi_game *h) : h_(h) { load_info(); }
+    Game(const Game &) = delete;
+    Game &operator=(const Game &) = delete;
+    Game(Game &&o) noexcept { *this = std::move(o); }
+    Game &operator=(Game &&o) noexcept
+    {
+        std::swap(h_, o.h_);
+        n_ = o.n_;
+        m_ = o.m_;
+        max_pri_ = o.max_pri_;
+        csr_loaded_ = false;
+        return *this;
+    }
+    ~Game() { psi_game_free(h_); }
+
+    // Game::parse_pgsolver(std::string filename) (game.cpp:38-50)
+    void parse_pgsolver(const std::string &filename)
+    {
+        psi_game *h = nullptr;
+        check(psi_game_load_gm(filename.c_str(), &h));
+        replace(h);
+    }
+    // Game::parse_pgsolver(std::istream&) on text already in memory
+    void parse_pgsolver_text(const std::string &text)
+    {
+        psi_game *h = nullptr;
+        check(psi_game_parse_gm(text.data(), (int64_t)text.size(), &h));
+        replace(h);
+    }
+    static Game from_csr(const std::vector<int32_t> &owner, const std::vector<int32_t> &priority,
+                         const std::vector<int32_t> &offsets, const std::vector<int32_t> &targets)
+    {
+        psi_game *h = nullptr;
+        check(psi_game_from_csr((int32_t)owner.size(), owner.data(), priority.data(), offsets.data(),
+                                targets.data(), &h));
+        return Game(h);
+    }
+
+    int get_n_vertices() const { return n_; }
+    int get_max_pri() const { return max_pri_; }
+    int64_t get_n_edges() const { return m_; }
+    int get_player(int v) { return csr().owner[v]; }
+    int get_priority(int v) { return csr().priority[v]; }
+    std::vector<int> get_edges(int v)
+    {
+        const Csr &c = csr();
+        return std::vector<int>(c.targets.begin() + c.offsets[v], c.targets.begin() + c.offsets[v + 1]);
+    }
+    psi_game *handle() const { return h_; }
+
+private:
+    struct Csr {
+        std::vector<int32_t> owner, priority, offsets, targets;
+    };
+    void replace(psi_game *h)
+    {
+        psi_game_free(h_);
+        h_ = h;
+        csr_loaded_ = false;
+        load_info();
+    }
+    void load_info() { check(psi_game_info(h_, &n_, &m_, &max_pri_)); }
+    const Csr &csr()
+    {
+        if (!csr_loaded_) {
+            csr_.owner.resize(n_);
+            csr_.priority.resize(n_);
+            csr_.offsets.resize((size_t)n_ + 1);
+            csr_.targets.resize((size_t)m_);
+            check(psi_game_copy_csr(h_, csr_.owner.data(), csr_.priority.data(), csr_.offsets.data(),
+                                    csr_.targets.data()));
+            csr_loaded_ = true;
+        }
+        return csr_;
+    }
+    psi_game *h_ = nullptr;
+    int32_t n_ = 0, max_pri_ = 0;
+    int64_t m_ = 0;
+    bool csr_loaded_ = false;
+    Csr csr_;
+};
+
+// si.h:6-16
+class StrategyImprovement {
+public:
+    virtual ~StrategyImprovement() = default;
+    virtual void init_strat() = 0;
+    virtual void compute_valuation() = 0;
+    virtual void compute_first_val() { compute_valuation(); }
+    virtual void mark_solved(int player) = 0;
+    virtual int switch_strategy(int player) = 0;
+    virtual void get_winning(std::vector<int> &out, int player) = 0;
+    virtual void reset_opponent_strategy() {}
+};
+
+class GPUList : public StrategyImprovement {
+public:
+    explicit GPUList(const Game &g, const psi_options *opt = nullptr) : n_(g.get_n_vertices())
+    {
+        check(psi_solver_create(g.handle(), opt, &s_));
+    }
+    GPUList(const GPUList &) = delete;
+    GPUList &operator=(const GPUList &) = delete;
+    ~GPUList() override { psi_solver_destroy(s_); }
+
+    void init_strat() override { check(psi_init_strat(s_)); }
+    void compute_valuation() override { check(psi_compute_valuation(s_)); }
+    void compute_first_val() override { check(psi_compute_first_val(s_)); }
+    void mark_solved(int player) override { check(psi_mark_solved(s_, player)); }
+    // Returns the number of strict improvements, saturated to int.
+    int switch_strategy(int player) override
+    {
+        int64_t k = 0;
+        check(psi_switch_strategy(s_, player, &k));
+        return k > INT32_MAX ? INT32_MAX : (int)k;
+    }
+    // Appends the winning set of `player` to out (gpu_parity.cu:340-354).
+    void get_winning(std::vector<int> &out, int player) override
+    {
+        std::vector<int32_t> w((size_t)n_);
+        int64_t count = 0;
+        check(psi_get_winning(s_, player, w.data(), (int64_t)w.size(), &count));
+        out.insert(out.end(), w.begin(), w.begin() + count);
+    }
+    void reset_opponent_strategy() override { check(psi_reset_opponent_strategy(s_)); }
+
+    std::vector<int32_t> get_strategy()
+    {
+        std::vector<int32_t> s((size_t)n_);
+        check(psi_get_strategy(s_, s.data()));
+        return s;
+    }
+    std::vector<int32_t> get_infinite()
+    {
+        std::vector<int32_t> s((size_t)n_);
+        check(psi_get_infinite(s_, s.data()));
+        return s;
+    }
+    // The whole solve on the device side of the boundary (psi_solve).
+    void solve(int *iter_count, int *br_count, bool reset = false)
+    {
+        int32_t it = 0, br = 0;
+        check(psi_solve(s_, reset ? 1 : 0, &it, &br, 0));
+        *iter_count = it;
+        *br_count = br;
+    }
+    psi_solver *handle() const { return s_; }
+
+private:
+    psi_solver *s_ = nullptr;
+    int32_t n_ = 0;
+};
+
+// The reference driver loop (main.cpp:20-55) over any StrategyImprovement.
+inline void solve_si(StrategyImprovement &si, int *br_count, int *iter_count, bool reset)
+{
+    si.init_strat();
+    bool first = true;
+    while (true) {
+        if (!first && reset) si.reset_opponent_strategy();
+        while (true) {
+            if (first) si.compute_first_val();
+            else si.compute_valuation();
+            (*br_count)++;
+            si.mark_solved(1);
+            if (si.switch_strategy(1) == 0) break;
+        }
+        first = false;
+        si.mark_solved(0);
+        (*iter_count)++;
+        if (si.switch_strategy(0) == 0) break;
+    }
+}
+
+}  // namespace psi
+
+#endif

@@ -1,0 +1,41 @@
+// drop_in_driver.cpp -- the reference's GPU driver flow (gpumain.cpp:102-146:
+// parse a .gm file, build the solver, run solve_si, print "time iters brs")
+// written against include/psi_si.hpp.  Built and run by tests/test_cpp_driver.py.
+//   drop_in_driver parse <game.gm>   -> "n m max_pri" (no GPU needed)
+//   drop_in_driver solve <game.gm>   -> "time iters brs" then the W0 size
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "psi_si.hpp"
+
+int main(int argc, char **argv)
+{
+    if (argc != 3) {
+        std::printf("usage: %s parse|solve game.gm\n", argv[0]);
+        return 1;
+    }
+    try {
+        psi::Game g;
+        g.parse_pgsolver(argv[2]);
+        if (std::strcmp(argv[1], "parse") == 0) {
+            std::printf("%d %lld %d\n", g.get_n_vertices(), (long long)g.get_n_edges(), g.get_max_pri());
+            return 0;
+        }
+        psi::GPUList si(g);
+        int iters = 0, brs = 0;
+        auto t0 = std::chrono::steady_clock::now();
+        psi::solve_si(si, &brs, &iters, false);
+        double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        std::printf("%f %d %d\n", dt, iters, brs);
+        std::vector<int> w0;
+        si.get_winning(w0, 0);
+        std::printf("%zu\n", w0.size());
+    } catch (const psi::Error &e) {
+        std::fprintf(stderr, "parsing error: %s\n", e.what());
+        return 2;
+    }
+    return 0;
+}
