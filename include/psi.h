@@ -160,6 +160,34 @@ int64_t psi_launch_count(void);
 int psi_solver_timer_begin(psi_solver *s);
 int psi_solver_timer_end(psi_solver *s, double *ms);
 
+/* ------------------------------------------------- evaluation without allocation
+ * No counterpart in the reference.  For callers that must not allocate device
+ * memory while they run -- e.g. a serving process that reserves its device
+ * memory at start-up and cannot risk an allocation failing or stalling the
+ * device under load, or a program whose device memory is owned by another
+ * allocator.  It evaluates one strategy profile exactly as
+ * psi_compute_valuation does on a fresh solver (no solved vertices), on
+ * device arrays the caller provides:
+ *   strategy[n]  successor of each vertex, -1 = the sink (Even's choice)
+ *   priority[n]  vertex priorities (>= 0)
+ *   status[n]    output: the length of the strategy path from the vertex to
+ *                the sink (>= 1) if its valuation is finite, -1 if it is
+ *                -inf, -2 if it is +inf
+ * on `stream` (a cudaStream_t; NULL = the legacy default stream) of the
+ * current device, and returns when the result is ready.
+ * It calls no cudaMalloc/cudaFree: its working memory is one fixed
+ * __device__ array of 13.5 MiB (14,131,456 bytes) that every process loading the library
+ * holds on each device it uses, until exit.  Hence the size limit: n may be at
+ * most PSI_NOALLOC_MAX_VERTICES, larger n returns PSI_ERR_TOO_LARGE.
+ * The first call on a device looks up that array's device address (once per
+ * device); make that first call before any stream capture.  All calls share
+ * the one array, which keeps the previous call's contents (the call clears
+ * what must start at zero): calls that overlap on the GPU -- from two host
+ * threads, or on two streams -- race and must not be issued. */
+#define PSI_NOALLOC_MAX_VERTICES 262144
+int psi_evaluate_strategy_noalloc(int32_t n, const int32_t *strategy, const int32_t *priority,
+                                  int32_t *status, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
