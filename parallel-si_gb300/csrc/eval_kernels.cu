@@ -140,17 +140,15 @@ __global__ void k_sink_chain(int32_t n, const int32_t *__restrict__ sinklist,
 }
 
 // Head j sits at node j*stride; the last head is the sink's up node (the list
-// start), so the reduced list starts at sublist nsub-1.  Also resets the
-// segment map of the reduced-list ranking.
+// start), so the reduced list starts at sublist nsub-1.
 __global__ void k_pick_heads(int64_t L, int32_t nsub, int32_t stride, int32_t *__restrict__ succ,
-                             int32_t *__restrict__ hsucc, int2 *__restrict__ seg_of)
+                             int32_t *__restrict__ hsucc)
 {
     int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nsub) return;
     int64_t node = (j == nsub - 1) ? L - 1 : (int64_t)j * stride;
     hsucc[j] = succ[node];
     succ[node] = head_mark(j);
-    seg_of[j] = make_int2(-1, 0);
 }
 
 // One thread per sublist: walk from the head's successor up to and including
@@ -188,83 +186,34 @@ __global__ void k_walk_sublists(int32_t nsub, int32_t n, int64_t L, const int32_
 }
 
 // ---- ranking of the reduced list (items = sublists, weight = sublist total)
-// Segment heads: the items whose index is a multiple of seg_stride, plus the
-// list start nsub-1; segment k's head is k*seg_stride (k < nseg-1) or nsub-1.
-__device__ __forceinline__ bool seg_head(int32_t j, int32_t nsub, int32_t seg_stride)
+// Wyllie pointer jumping in one cooperative launch: after round r each item
+// holds (the item 2^r positions ahead or TOUR_END, the sum of the weights over
+// those positions).  ceil(log2 nsub)+1 rounds reach the end of every list;
+// items on cycles (tours of components the sink does not reach) never do.
+// Round 0 reads red and writes a, then the rounds alternate a -> b -> a ...
+// Reads bypass L1 (each buffer is rewritten by other blocks between reads).
+__global__ void __launch_bounds__(kBlock) k_rank_reduced(int32_t nsub, const int2 *__restrict__ red,
+                                                         int2 *__restrict__ a, int2 *__restrict__ b)
 {
-    return j == nsub - 1 || (j % seg_stride) == 0;
-}
-
-__device__ __forceinline__ int32_t seg_index(int32_t j, int32_t nsub, int32_t nseg, int32_t seg_stride)
-{
-    return j == nsub - 1 ? nseg - 1 : j / seg_stride;
-}
-
-// One thread per segment: walk from its head through the items up to the next
-// head, recording each item's segment and inclusive prefix within it.
-// segs[k] = (next segment or TOUR_END, segment total).
-__global__ void k_red_walk(int32_t nsub, int32_t nseg, int32_t seg_stride, const int2 *__restrict__ red,
-                           int2 *__restrict__ seg_of, int2 *__restrict__ segs, uint32_t *__restrict__ err)
-{
-    int32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nseg) return;
-    int32_t x = (k == nseg - 1) ? nsub - 1 : k * seg_stride;
-    int32_t acc = 0;
-    int32_t steps = 0;
-    for (;;) {
-        int2 r = red[x];
-        acc += r.y;
-        seg_of[x] = make_int2(k, acc);
-        x = r.x;
-        if (x < 0 || seg_head(x, nsub, seg_stride)) break;
-        if (++steps > nsub) {
-            atomicOr(err, DERR_SUBLIST_CAP);
-            x = TOUR_END;
-            break;
-        }
-    }
-    segs[k] = make_int2(x < 0 ? TOUR_END : seg_index(x, nsub, nseg, seg_stride), acc);
-}
-
-// Single block: Wyllie suffix sums over the segment list (at most a few
-// thousand entries) in two global buffers; result in `a` (or `b`, see return
-// slot written to *which).  Reads bypass L1 (buffers are rewritten each round).
-__global__ void __launch_bounds__(1024) k_red_block(int32_t nseg, int2 *__restrict__ a, int2 *__restrict__ b,
-                                                    int2 *__restrict__ out)
-{
-    int rounds = ceil_log2_dev(nseg) + 1;
-    int2 *in = a, *o = b;
+    cg::grid_group g = cg::this_grid();
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    const int rounds = ceil_log2_dev(nsub) + 1;
+    const int2 *in = red;
+    int2 *out = a;
     for (int r = 0; r < rounds; r++) {
-        for (int32_t k = threadIdx.x; k < nseg; k += blockDim.x) {
-            int2 x = __ldcg(&in[k]);
+        for (int64_t j = tid; j < nsub; j += nth) {
+            int2 x = __ldcg(&in[j]);
             if (x.x >= 0) {
                 int2 y = __ldcg(&in[x.x]);
                 x = make_int2(y.x, x.y + y.y);
             }
-            o[k] = x;
+            out[j] = x;
         }
-        __syncthreads();
-        int2 *t = in;
-        in = o;
-        o = t;
+        g.sync();
+        in = out;
+        out = (out == a) ? b : a;
     }
-    for (int32_t k = threadIdx.x; k < nseg; k += blockDim.x) out[k] = __ldcg(&in[k]);
-}
-
-// fin[j] = (TOUR_END if the list start reaches sublist j, else 0; inclusive
-// suffix sum of the reduced list from j).
-__global__ void k_red_finish(int32_t nsub, const int2 *__restrict__ red, const int2 *__restrict__ seg_of,
-                             const int2 *__restrict__ segfin, int2 *__restrict__ fin)
-{
-    int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nsub) return;
-    int2 so = seg_of[j];
-    if (so.x < 0) {
-        fin[j] = make_int2(0, 0);
-        return;
-    }
-    int2 sf = segfin[so.x];
-    fin[j] = make_int2(sf.x == TOUR_END ? TOUR_END : 0, sf.y - so.y + red[j].y);
 }
 
 // Depth of a reached vertex = inclusive prefix of the tour at its up node =
@@ -333,16 +282,23 @@ __global__ void k_rootinfo(int32_t n, const int32_t *__restrict__ st, PathNode *
 }
 
 // ---- cycle parity of the unreached vertices
-// jmp[u] = (vertex 2^k steps ahead, maximum priority over those 2^k vertices
-// starting at u); solved vertices absorb.  After 2^R >= |unreached| steps
-// every walk sits on its final cycle (or on a solved vertex), and the window
-// maximum from a cycle vertex covers the whole cycle.
+// jmp[u] = (vertex 2^r steps ahead, maximum priority over those 2^r vertices
+// starting at u); solved vertices absorb.  After ceil(log2 |U|)+1 rounds every
+// window is longer than any path into a cycle plus the cycle, so each walk sits
+// on its final cycle (or on a solved vertex) and the window maximum from a
+// cycle vertex is the cycle's top priority.  A vertex whose window has reached
+// a solved vertex is settled: it leaves the active list (later rounds only
+// touch active vertices, and stop early when none is left) and its final entry
+// is stored in both buffers, so any later reader sees it.  A reader racing with
+// that store sees either the previous entry or the final one; both lead to the
+// same solved vertex.
 constexpr int kSmallCycles = 4096;   // up to this many: one block, no grid barrier
 
 template <bool GRID>
 __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const int32_t *__restrict__ strat,
                             const int32_t *__restrict__ pri, const uint8_t *__restrict__ solved,
                             int32_t *__restrict__ st, int2 *__restrict__ ja, int2 *__restrict__ jb,
+                            int32_t *__restrict__ la, int32_t *__restrict__ lb, int32_t *__restrict__ cnt,
                             uint32_t *__restrict__ err)
 {
     const int64_t tid = GRID ? (int64_t)blockIdx.x * blockDim.x + threadIdx.x : threadIdx.x;
@@ -358,22 +314,46 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
             atomicOr(err, DERR_BAD_INPUT);
             t = u;
         }
-        ja[u] = make_int2(t, pri[u]);
+        int2 e = make_int2(t, pri[u]);
+        ja[u] = e;
+        jb[u] = e;
+    }
+    if (tid == 0) {
+        cnt[0] = 0;
+        cnt[1] = 0;
+        cnt[2] = 0;
     }
     barrier();
+    const int32_t *act = ulist;
+    int32_t na = nu;
     int2 *in = ja, *out = jb;
-    int rounds = ceil_log2_dev(nu) + 1;
-    for (int r = 0; r < rounds; r++) {
-        for (int64_t i = tid; i < nu; i += nth) {
-            int32_t u = ulist[i];
-            int2 a = __ldcg(&in[u]);
-            if (!solved[a.x]) {
-                int2 b = __ldcg(&in[a.x]);
-                a = make_int2(b.x, max(a.y, b.y));
+    int32_t *next = la;
+    const int rounds = ceil_log2_dev(nu) + 1;
+    for (int r = 0; r < rounds && na > 0; r++) {
+        int32_t *c = &cnt[r % 3];
+        if (tid == 0) cnt[(r + 1) % 3] = 0;    // next round's counter (last read two rounds ago)
+        for (int64_t i0 = tid; i0 - (threadIdx.x & 31) < na; i0 += nth) {
+            bool keep = false;
+            int32_t u = -1;
+            if (i0 < na) {
+                u = act[i0];
+                int2 a = __ldcg(&in[u]);
+                if (solved[a.x]) {
+                    out[u] = a;                  // settled earlier: entry already final
+                } else {
+                    int2 b = __ldcg(&in[a.x]);
+                    int2 a2 = make_int2(b.x, max(a.y, b.y));
+                    out[u] = a2;
+                    if (solved[a2.x]) in[u] = a2;   // settled now: final in both buffers
+                    else keep = true;
+                }
             }
-            out[u] = a;
+            warp_append(keep, u, next, c);
         }
         barrier();
+        na = *(volatile int32_t *)c;
+        act = next;
+        next = (next == la) ? lb : la;
         int2 *t = in;
         in = out;
         out = t;
@@ -391,15 +371,16 @@ __global__ void __launch_bounds__(kBlock) k_cycles(const int32_t *__restrict__ u
                                                    const int32_t *__restrict__ pri,
                                                    const uint8_t *__restrict__ solved, int32_t *__restrict__ st,
                                                    int2 *__restrict__ ja, int2 *__restrict__ jb,
-                                                   uint32_t *__restrict__ err)
+                                                   int32_t *__restrict__ la, int32_t *__restrict__ lb,
+                                                   int32_t *__restrict__ cnt, uint32_t *__restrict__ err)
 {
     int32_t nu = *ucount;
     if (nu == 0) return;
     if (nu <= kSmallCycles) {
-        if (blockIdx.x == 0) cycles_body<false>(nu, ulist, strat, pri, solved, st, ja, jb, err);
+        if (blockIdx.x == 0) cycles_body<false>(nu, ulist, strat, pri, solved, st, ja, jb, la, lb, cnt, err);
         return;
     }
-    cycles_body<true>(nu, ulist, strat, pri, solved, st, ja, jb, err);
+    cycles_body<true>(nu, ulist, strat, pri, solved, st, ja, jb, la, lb, cnt, err);
 }
 
 // mark_solved restricted to the last evaluation's unreached vertices: every
@@ -464,11 +445,10 @@ void launch_tour_build(cudaStream_t s, int32_t n, const int32_t *strat, const ui
     k_sink_chain<<<g < 1216u ? g : 1216u, kBlock, 0, s>>>(n, sinklist, sinkcount, succ);
 }
 
-void launch_pick_heads(cudaStream_t s, int64_t L, int32_t nsub, int32_t stride, int32_t *succ, int32_t *hsucc,
-                       int2 *seg_of)
+void launch_pick_heads(cudaStream_t s, int64_t L, int32_t nsub, int32_t stride, int32_t *succ, int32_t *hsucc)
 {
     count_launch();
-    k_pick_heads<<<grid_for(nsub), kBlock, 0, s>>>(L, nsub, stride, succ, hsucc, seg_of);
+    k_pick_heads<<<grid_for(nsub), kBlock, 0, s>>>(L, nsub, stride, succ, hsucc);
 }
 
 void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, const int32_t *succ,
@@ -478,15 +458,25 @@ void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, co
     k_walk_sublists<<<grid_for(nsub, 128), 128, 0, s>>>(nsub, n, L, succ, hsucc, vloc, red, err);
 }
 
-void launch_rank_reduced(cudaStream_t s, int32_t nsub, int32_t nseg, int32_t seg_stride, const int2 *red,
-                         int2 *seg_of, int2 *segA, int2 *segB, int2 *segfin, int2 *fin, uint32_t *err)
+int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, int2 *b, const int2 **fin)
 {
+    static int blocks = 0, blocks_dev = -1;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != blocks_dev) {
+        blocks = device_blocks((const void *)k_rank_reduced, kBlock);
+        blocks_dev = dev;
+    }
+    int64_t need = ceil_div(nsub, kBlock);
+    int grid = (int)(need < blocks ? need : blocks);
+    int rounds = 0;
+    while (((int64_t)1 << rounds) < nsub) rounds++;
+    rounds += 1;
+    *fin = (rounds % 2 == 1) ? a : b;
+    void *args[] = {(void *)&nsub, (void *)&red, (void *)&a, (void *)&b};
     count_launch();
-    k_red_walk<<<grid_for(nseg, 128), 128, 0, s>>>(nsub, nseg, seg_stride, red, seg_of, segA, err);
-    count_launch();
-    k_red_block<<<1, 1024, 0, s>>>(nseg, segA, segB, segfin);
-    count_launch();
-    k_red_finish<<<grid_for(nsub), kBlock, 0, s>>>(nsub, red, seg_of, segfin, fin);
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_rank_reduced, dim3(grid), dim3(kBlock), args, 0, s);
+    return e == cudaSuccess ? 0 : (int)e;
 }
 
 void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const int2 *fin,
@@ -504,7 +494,8 @@ void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *nod
 }
 
 int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, const int32_t *strat,
-                  const int32_t *pri, const uint8_t *solved, int32_t *st, int2 *ja, int2 *jb, uint32_t *err)
+                  const int32_t *pri, const uint8_t *solved, int32_t *st, int2 *ja, int2 *jb, int32_t *la,
+                  int32_t *lb, int32_t *cnt, uint32_t *err)
 {
     static int blocks = 0, blocks_dev = -1;
     int dev = 0;
@@ -514,7 +505,8 @@ int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, c
         blocks_dev = dev;
     }
     void *args[] = {(void *)&ucount, (void *)&ulist, (void *)&strat, (void *)&pri, (void *)&solved,
-                    (void *)&st, (void *)&ja, (void *)&jb, (void *)&err};
+                    (void *)&st, (void *)&ja, (void *)&jb, (void *)&la, (void *)&lb, (void *)&cnt,
+                    (void *)&err};
     count_launch();
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_cycles, dim3(blocks), dim3(kBlock), args, 0, s);
     return e == cudaSuccess ? 0 : (int)e;

@@ -33,23 +33,25 @@ void launch_tour_build(cudaStream_t s, int32_t n, const int32_t *strat, const ui
                        const int32_t *rev_off, const int32_t *rev_src, int32_t *succ, int2 *vloc,
                        int32_t *sinklist, int32_t *sinkcount);
 void launch_pick_heads(cudaStream_t s, int64_t L, int32_t nsub, int32_t stride, int32_t *succ,
-                       int32_t *hsucc, int2 *seg_of);
+                       int32_t *hsucc);
 void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, const int32_t *succ,
                           const int32_t *hsucc, int2 *vloc, int2 *red, uint32_t *err);
-// Ranks the reduced list red[0..nsub) (next, weight) from item nsub-1:
-// fin[j] = (TOUR_END if reached else 0, inclusive suffix sum).  nseg segments
-// of seg_stride items; segA/segB/segfin hold nseg entries.
-void launch_rank_reduced(cudaStream_t s, int32_t nsub, int32_t nseg, int32_t seg_stride, const int2 *red,
-                         int2 *seg_of, int2 *segA, int2 *segB, int2 *segfin, int2 *fin, uint32_t *err);
+// Ranks the reduced list red[0..nsub) (next, weight) by Wyllie pointer jumping
+// (cooperative launch; a, b: nsub entries each).  *fin is set to the buffer
+// that will hold, per item, (TOUR_END if the list start reaches it, else >= 0;
+// inclusive suffix sum).  Returns a cudaError_t value.
+int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, int2 *b, const int2 **fin);
 void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const int2 *fin,
                             const int32_t *strat, const int32_t *pri, const uint8_t *solved,
                             int32_t *st, PathNode *node, int32_t *ulist, int32_t *ucount);
 // Root-path summaries (rmax, rcnt) of every reached vertex.
 void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, uint32_t *err);
-// Cycle parity of the *ucount vertices in ulist (cooperative launch); returns
-// a cudaError_t value.
+// Cycle parity of the *ucount vertices in ulist (cooperative launch).  ja, jb:
+// n entries; la, lb: n entries (active lists); cnt: 3 counters.  Returns a
+// cudaError_t value.
 int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, const int32_t *strat,
-                  const int32_t *pri, const uint8_t *solved, int32_t *st, int2 *ja, int2 *jb, uint32_t *err);
+                  const int32_t *pri, const uint8_t *solved, int32_t *st, int2 *ja, int2 *jb, int32_t *la,
+                  int32_t *lb, int32_t *cnt, uint32_t *err);
 // mark_solved over the last evaluation's unreached vertices (cpu_parity.cpp:265-274)
 void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, int32_t player,
                         const int32_t *st, uint8_t *solved);

@@ -31,16 +31,14 @@ constexpr int32_t kMaxN = PSI_NOALLOC_MAX_VERTICES;
 constexpr int32_t kStride = 64;                                   // sublist stride
 constexpr int64_t kMaxL = 2 * (int64_t)kMaxN + 2;                 // tour nodes
 constexpr int32_t kMaxSub = (int32_t)((kMaxL - 1 + kStride - 1) / kStride + 1);
-constexpr int32_t kSegStride = 32;                                // kMaxSub / 32 <= 8192
-constexpr int32_t kMaxSeg = (kMaxSub - 1 + kSegStride - 1) / kSegStride + 1;
 
 constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Layout of the scratch array (byte offsets).
 struct Layout {
-    static constexpr size_t words = 0;                                            // err, ucount, sinkcount
-    static constexpr size_t succ = align256(words + 16);
-    static constexpr size_t vloc = align256(succ + 4 * kMaxL);
+    static constexpr size_t words = 0;                                            // struct Words
+    static constexpr size_t succ = align256(words + 32);
+    static constexpr size_t vloc = align256(succ + 4 * kMaxL);                    // later: two active lists
     static constexpr size_t list = align256(vloc + 8 * (size_t)kMaxN);            // sink list, then unreached list
     static constexpr size_t node = align256(list + 4 * (size_t)kMaxN);
     static constexpr size_t solved = align256(node + sizeof(PathNode) * (size_t)kMaxN);
@@ -49,13 +47,9 @@ struct Layout {
     static constexpr size_t hsucc = align256(jb + 8 * (size_t)kMaxN);
     static constexpr size_t redA = align256(hsucc + 4 * (size_t)kMaxSub);
     static constexpr size_t redB = align256(redA + 8 * (size_t)kMaxSub);
-    static constexpr size_t seg_of = align256(redB + 8 * (size_t)kMaxSub);
-    static constexpr size_t segA = align256(seg_of + 8 * (size_t)kMaxSub);
-    static constexpr size_t segB = align256(segA + 8 * (size_t)kMaxSeg);
-    static constexpr size_t segfin = align256(segB + 8 * (size_t)kMaxSeg);
-    static constexpr size_t total = align256(segfin + 8 * (size_t)kMaxSeg);
+    static constexpr size_t redC = align256(redB + 8 * (size_t)kMaxSub);
+    static constexpr size_t total = align256(redC + 8 * (size_t)kMaxSub);
 };
-static_assert(kMaxSeg <= 8193, "segment count must stay within one block's ranking");
 
 // The working memory of psi_evaluate_strategy_noalloc (one copy per device).
 static __device__ __align__(256) unsigned char g_scratch[Layout::total];
@@ -69,8 +63,9 @@ struct Words {
     uint32_t err;
     int32_t ucount;
     int32_t sinkcount;
-    int32_t pad;
+    int32_t cnt[3];
 };
+static_assert(sizeof(Words) <= 32, "Words must fit its slot");
 
 inline unsigned grid_for(int64_t items, int block = kBlock)
 {
@@ -181,14 +176,10 @@ extern "C" int psi_evaluate_strategy_noalloc(int32_t n, const int32_t *strategy,
     int32_t *hsucc = reinterpret_cast<int32_t *>(base + Layout::hsucc);
     int2 *redA = reinterpret_cast<int2 *>(base + Layout::redA);
     int2 *redB = reinterpret_cast<int2 *>(base + Layout::redB);
-    int2 *seg_of = reinterpret_cast<int2 *>(base + Layout::seg_of);
-    int2 *segA = reinterpret_cast<int2 *>(base + Layout::segA);
-    int2 *segB = reinterpret_cast<int2 *>(base + Layout::segB);
-    int2 *segfin = reinterpret_cast<int2 *>(base + Layout::segfin);
+    int2 *redC = reinterpret_cast<int2 *>(base + Layout::redC);
 
     const int64_t L = 2 * (int64_t)n + 2;
     const int32_t nsub = (int32_t)(ceil_div(L - 1, kStride) + 1);
-    const int32_t nseg = (int32_t)(ceil_div(nsub - 1, kSegStride) + 1);
 
     // the scratch keeps the previous call's contents: reset what must start at zero
     e = cudaMemsetAsync(w, 0, sizeof(Words), s);
@@ -200,11 +191,14 @@ extern "C" int psi_evaluate_strategy_noalloc(int32_t n, const int32_t *strategy,
     count_launch();
     unsigned g = grid_for(n);
     k_na_sink_chain<<<g < 1216u ? g : 1216u, kBlock, 0, s>>>(n, list, &w->sinkcount, succ);
-    launch_pick_heads(s, L, nsub, kStride, succ, hsucc, seg_of);
+    launch_pick_heads(s, L, nsub, kStride, succ, hsucc);
     launch_walk_sublists(s, nsub, n, L, succ, hsucc, vloc, redA, &w->err);
-    launch_rank_reduced(s, nsub, nseg, kSegStride, redA, seg_of, segA, segB, segfin, redB, &w->err);
-    launch_broadcast_depth(s, n, vloc, redB, strategy, priority, solved, status, node, list, &w->ucount);
-    int ce = launch_cycles(s, &w->ucount, list, strategy, priority, solved, status, ja, jb, &w->err);
+    const int2 *fin = nullptr;
+    int re = launch_rank_reduced(s, nsub, redA, redB, redC, &fin);
+    if (re) return fail(PSI_ERR_CUDA, std::string("reduced-list kernel launch: ") + cudaGetErrorString((cudaError_t)re));
+    launch_broadcast_depth(s, n, vloc, fin, strategy, priority, solved, status, node, list, &w->ucount);
+    int32_t *la = reinterpret_cast<int32_t *>(vloc), *lb = la + n;
+    int ce = launch_cycles(s, &w->ucount, list, strategy, priority, solved, status, ja, jb, la, lb, w->cnt, &w->err);
     if (ce) return fail(PSI_ERR_CUDA, std::string("cycle kernel launch: ") + cudaGetErrorString((cudaError_t)ce));
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(PSI_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));

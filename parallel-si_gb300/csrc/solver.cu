@@ -62,9 +62,6 @@ int Solver::alloc(const HostGame &g, const psi_options &)
     L_ = 2 * (int64_t)n_ + 2;
     // heads at node j*stride for j < nsub-1, plus the list start (node L-1)
     nsub_ = (int32_t)(ceil_div(L_ - 1, stride_) + 1);
-    // second level: segments of seg_stride sublists, few enough for one block
-    seg_stride_ = (int32_t)std::max<int64_t>(32, ceil_div(nsub_, 8192));
-    nseg_ = (int32_t)(ceil_div(nsub_ - 1, seg_stride_) + 1);
     game_ = &g;
     PSI_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     for (auto &p : ph_) {
@@ -100,10 +97,7 @@ int Solver::alloc(const HostGame &g, const psi_options &)
     PSI_DALLOC(vloc_, 8 * (size_t)n_);
     PSI_DALLOC(redA_, 8 * (size_t)nsub_);
     PSI_DALLOC(redB_, 8 * (size_t)nsub_);
-    PSI_DALLOC(seg_of_, 8 * (size_t)nsub_);
-    PSI_DALLOC(segA_, 8 * (size_t)nseg_);
-    PSI_DALLOC(segB_, 8 * (size_t)nseg_);
-    PSI_DALLOC(segfin_, 8 * (size_t)nseg_);
+    PSI_DALLOC(redC_, 8 * (size_t)nsub_);
     PSI_DALLOC(jA_, 8 * (size_t)n_);
     PSI_DALLOC(jB_, 8 * (size_t)n_);
     PSI_DALLOC(dw_, sizeof(Words));
@@ -254,25 +248,29 @@ int Solver::compute_valuation()
     phase_begin(PH_TOUR);
     PSI_CUDA_TRY(cudaMemsetAsync(&dw_->ucount, 0, 2 * sizeof(int32_t), stream_));   // ucount, sinkcount
     launch_tour_build(stream_, n_, strat_, solved_, rev_off_, rev_src_, succ_, vloc_, ulist_, &dw_->sinkcount);
-    launch_pick_heads(stream_, L_, nsub_, stride_, succ_, hsucc_, seg_of_);
+    launch_pick_heads(stream_, L_, nsub_, stride_, succ_, hsucc_);
     phase_end(PH_TOUR);
     // 2. Helman-JaJa sublists, then the reduced list ranked on the device
     phase_begin(PH_SUBLIST);
     launch_walk_sublists(stream_, nsub_, n_, L_, succ_, hsucc_, vloc_, redA_, &dw_->err);
     phase_end(PH_SUBLIST);
     phase_begin(PH_REDUCED);
-    launch_rank_reduced(stream_, nsub_, nseg_, seg_stride_, redA_, seg_of_, segA_, segB_, segfin_, redB_,
-                        &dw_->err);
+    const int2 *fin = nullptr;
+    int re = launch_rank_reduced(stream_, nsub_, redA_, redB_, redC_, &fin);
+    if (re) return fail(PSI_ERR_CUDA, std::string("reduced-list kernel launch: ") + cudaGetErrorString((cudaError_t)re));
     phase_end(PH_REDUCED);
     // 3. broadcast depths; collect the vertices the sink does not reach
     //    (ulist held the sink's children until here)
     phase_begin(PH_BROADCAST);
-    launch_broadcast_depth(stream_, n_, vloc_, redB_, strat_, pri_, solved_, st_, node_, ulist_, &dw_->ucount);
+    launch_broadcast_depth(stream_, n_, vloc_, fin, strat_, pri_, solved_, st_, node_, ulist_, &dw_->ucount);
     launch_rootinfo(stream_, n_, st_, node_, &dw_->err);
     phase_end(PH_BROADCAST);
     // 4. cycle parity by pointer jumping over the unreached vertices
     phase_begin(PH_CYCLES);
-    int ce = launch_cycles(stream_, &dw_->ucount, ulist_, strat_, pri_, solved_, st_, jA_, jB_, &dw_->err);
+    // the tour's vloc array is free again: it holds the two active lists
+    int32_t *la = reinterpret_cast<int32_t *>(vloc_), *lb = la + n_;
+    int ce = launch_cycles(stream_, &dw_->ucount, ulist_, strat_, pri_, solved_, st_, jA_, jB_, la, lb, dw_->cnt,
+                           &dw_->err);
     if (ce) return fail(PSI_ERR_CUDA, std::string("cycle kernel launch: ") + cudaGetErrorString((cudaError_t)ce));
     phase_end(PH_CYCLES);
     phase_end(PH_EVAL);

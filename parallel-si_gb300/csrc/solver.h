@@ -100,15 +100,14 @@ private:
     int32_t *succ_ = nullptr, *hsucc_ = nullptr, *ulist_ = nullptr;
     int32_t *rev_off_ = nullptr, *rev_src_ = nullptr;   // distinct in-neighbours (static)
     int2 *vloc_ = nullptr, *redA_ = nullptr, *redB_ = nullptr, *jA_ = nullptr, *jB_ = nullptr;
-    int2 *seg_of_ = nullptr, *segA_ = nullptr, *segB_ = nullptr, *segfin_ = nullptr;
-    int32_t nseg_ = 0, seg_stride_ = 32;
+    int2 *redC_ = nullptr;
     // small device words + pinned host mirrors
     struct Words {
         unsigned long long sw[4];   // switch counters (launch_switch)
         uint32_t err;
         int32_t ucount;             // vertices the sink did not reach
         int32_t sinkcount;          // children of the sink (tour build)
-        int32_t pad;
+        int32_t cnt[3];             // active-list counters of the cycle kernel
     };
     Words *dw_ = nullptr, *hw_ = nullptr;
     std::vector<void *> allocs_;
