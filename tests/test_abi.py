@@ -1,0 +1,67 @@
+"""The C ABI library: loads without a GPU, exports every entry point declared
+in include/psi.h, and reports argument errors as status codes."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+import psi
+from psi._lib import (LIB_PATH, PSI_ERR_INVALID, PSI_ERR_NO_DEVICE, PSI_OK, lib)
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "psi.h")).read()
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(psi_\w+)\s*\(", text)))
+
+
+def test_header_declares_the_si_interface():
+    names = declared_functions()
+    for f in ("psi_init_strat", "psi_compute_valuation", "psi_compute_first_val", "psi_mark_solved",
+              "psi_switch_strategy", "psi_get_winning", "psi_reset_opponent_strategy", "psi_solve",
+              "psi_game_load_gm", "psi_solver_create", "psi_solver_destroy"):
+        assert f in names
+
+
+def test_library_exports_every_declared_function():
+    missing = [f for f in declared_functions() if not hasattr(lib, f)]
+    assert not missing, f"declared in include/psi.h but not exported by {LIB_PATH}: {missing}"
+
+
+def test_version_and_defaults():
+    assert "sm_103a" in psi.version()
+    o = psi.default_options()
+    assert (o.device, o.valuation_mode, o.sublist_len, o.timing) == (0, 0, 64, 1)
+
+
+def test_null_arguments_are_status_codes():
+    assert lib.psi_game_load_gm(None, None) == PSI_ERR_INVALID
+    assert lib.psi_init_strat(None) == PSI_ERR_INVALID
+    assert lib.psi_switch_strategy(None, 0, None) == PSI_ERR_INVALID
+    assert "null" in psi.last_error()
+    assert lib.psi_solver_create(None, None, None) == PSI_ERR_INVALID
+
+
+def test_solver_without_gpu_fails_loudly():
+    """No CPU fallback: without a device, solver creation is an error."""
+    g = psi.Game.random(100, 2, 4, 100, 1)
+    h = C.c_void_p()
+    rc = lib.psi_solver_create(g._h, None, C.byref(h))
+    if rc == PSI_OK:
+        lib.psi_solver_destroy(h)
+        pytest.skip("a CUDA device is present")
+    assert rc == PSI_ERR_NO_DEVICE
+    with pytest.raises(psi.PsiError):
+        psi.GPUList(g)
+
+
+def test_invalid_options_rejected_before_device_use():
+    g = psi.Game.random(100, 2, 4, 100, 1)
+    for bad in (dict(sublist_len=1), dict(valuation_mode=7)):
+        o = psi.default_options(**bad)
+        h = C.c_void_p()
+        rc = lib.psi_solver_create(g._h, C.byref(o), C.byref(h))
+        assert rc in (PSI_ERR_INVALID, PSI_ERR_NO_DEVICE)
