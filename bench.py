@@ -198,7 +198,7 @@ def phase_bytes(phase, n, m, nsub, counters, calls, n_even, n_odd, iters, brs):
 
 
 KERNEL_OF_PHASE = {"switch": "k_switch", "sublist": "k_walk_sublists", "tour": "k_tour_link",
-                   "broadcast": "k_broadcast_depth", "reduced": "k_wyllie_round", "cycles": "k_jump_round"}
+                   "broadcast": "k_broadcast_depth", "reduced": "k_rank_reduced", "cycles": "k_cycles"}
 
 
 def cpu_baseline_sample(solves=3, seed=1):
@@ -352,6 +352,49 @@ def run_gb300(args, rank, world, local):
     return 0
 
 
+def run_batch(args, rank, world, local):
+    """Batched workload (not the headline line): `--batch-games` random games
+    with sizes log-uniform in [100, 200000], out-degree U[2,8], priority
+    U[0,n_i), solved together (psi_batch_solve) against the same kind of games
+    solved one at a time on the same GPU (every `--solo-stride`-th game, each
+    with its own resident solver).  Both rates are games per second of
+    synchronous host calls (wall clock)."""
+    import psi
+
+    sizes = psi.batch_sizes(args.batch_games, 100, 200000, args.seed)
+    games = [psi.Game.random(int(n), 2, 8, int(n), args.seed * 100003 + i) for i, n in enumerate(sizes)]
+    batch = psi.Batch(games, device=local)
+    for _ in range(args.warmup):
+        batch.solve()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        it, br = batch.solve()
+    t_batch = (time.perf_counter() - t0) / args.steps
+    solo_idx = list(range(0, len(games), args.solo_stride))
+    solvers = [psi.GPUList(games[k], device=local) for k in solo_idx]
+    for s in solvers[:8]:
+        s.solve()
+    t0 = time.perf_counter()
+    solo_res = [s.solve() for s in solvers]
+    t_solo = time.perf_counter() - t0
+    exact = all(tuple(solo_res[j]) == (int(it[k]), int(br[k])) for j, k in enumerate(solo_idx))
+    _, nv, ne = batch.info()
+    line = {
+        "metric": "games/s (batched)", "value": len(games) / t_batch, "unit": "games/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t_batch, "higher_is_better": True,
+        "dtype": "int32", "data": "synthetic",
+        "config": {"workload": f"{len(games)} random games, n_i log-uniform in [100,200000], out-degree U[2,8], "
+                               f"priority U[0,n_i)", "total_vertices": nv, "total_edges": ne,
+                   "max_iters": int(it.max()), "max_brs": int(br.max())},
+        "one_by_one": {"games": len(solo_idx), "games_per_s": len(solo_idx) / t_solo},
+        "speedup_vs_one_by_one": (len(games) / t_batch) / (len(solo_idx) / t_solo),
+        "counts_match_solo": exact,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -362,12 +405,18 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--sublist-len", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--workload", choices=("single", "batch"), default="single",
+                    help="single: the 2^24 game (headline); batch: many mixed-size games")
+    ap.add_argument("--batch-games", type=int, default=4096)
+    ap.add_argument("--solo-stride", type=int, default=16)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     rank, world, local = dist_env()
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload == "batch":
+        return run_batch(args, rank, world, local)
     return run_gb300(args, rank, world, local)
 
 

@@ -160,6 +160,27 @@ int64_t psi_launch_count(void);
 int psi_solver_timer_begin(psi_solver *s);
 int psi_solver_timer_end(psi_solver *s, double *ms);
 
+/* ---------------------------------------------------------------- batches
+ * Many games solved together: they are packed into one segmented CSR (a
+ * disjoint union) that every kernel processes at once, and solve_si runs over
+ * the union until no game switches.  Paths never cross games, so each game
+ * ends with exactly the strategies, winning sets and iteration/evaluation
+ * counts of a solo psi_solve; a game that converged early only sees steps that
+ * change nothing.  No counterpart in the reference, which solves one game per
+ * process run.  The batch may hold at most 2^30-2 vertices and 2^31-1 edges. */
+typedef struct psi_batch psi_batch;
+/* Sizes n_i = floor(n_lo * (n_hi / n_lo)^u), u uniform in [0,1), seeded. */
+int psi_generate_batch_sizes(int32_t count, int32_t n_lo, int32_t n_hi, uint64_t seed, int32_t *sizes);
+int psi_batch_create(const psi_game *const *games, int32_t count, const psi_options *opt, psi_batch **out);
+void psi_batch_destroy(psi_batch *b);
+int psi_batch_info(psi_batch *b, int32_t *games, int64_t *vertices, int64_t *edges);
+/* solve_si for every game (reset variant not supported); iter_counts and
+ * br_counts receive count entries each. */
+int psi_batch_solve(psi_batch *b, int32_t *iter_counts, int32_t *br_counts);
+/* Game-local results (vertex ids of the game, -1 = sink). */
+int psi_batch_get_strategy(psi_batch *b, int32_t game, int32_t *out);
+int psi_batch_get_winning(psi_batch *b, int32_t game, int32_t player, int32_t *out, int64_t cap, int64_t *count);
+
 /* ------------------------------------------------- evaluation without allocation
  * No counterpart in the reference.  For callers that must not allocate device
  * memory while they run -- e.g. a serving process that reserves its device

@@ -22,6 +22,12 @@ struct psi_solver {
     psi::Solver *s;
 };
 
+struct psi_batch {
+    psi::Solver *s = nullptr;
+    std::vector<int64_t> base;   // game k owns union vertices [base[k], base[k+1])
+    int64_t m = 0;
+};
+
 namespace psi {
 
 static thread_local std::string g_last_error;
@@ -323,6 +329,118 @@ int psi_solver_reset_times(psi_solver *s)
     if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null solver");
     s->s->reset_times();
     return PSI_OK;
+}
+
+int psi_generate_batch_sizes(int32_t count, int32_t n_lo, int32_t n_hi, uint64_t seed, int32_t *sizes)
+{
+    if (!sizes && count > 0) return psi::fail(PSI_ERR_INVALID, "null output");
+    int rc = psi::gen_batch_sizes(count, n_lo, n_hi, seed, sizes);
+    return rc ? psi::fail(rc, "invalid batch-size parameters") : PSI_OK;
+}
+
+int psi_batch_create(const psi_game *const *games, int32_t count, const psi_options *opt, psi_batch **out)
+{
+    if (!out || !games || count <= 0) return psi::fail(PSI_ERR_INVALID, "null or empty argument");
+    *out = nullptr;
+    PSI_GUARD_BEGIN
+    std::vector<const psi::HostGame *> gs;
+    for (int32_t k = 0; k < count; k++) {
+        if (!games[k]) return psi::fail(PSI_ERR_INVALID, "null game in batch");
+        gs.push_back(&games[k]->g);
+    }
+    psi::HostGame u;
+    std::vector<int64_t> base;
+    int rc = psi::pack_games(gs, u, base);
+    if (rc) return rc;
+    psi_options o;
+    psi_options_default(&o);
+    if (opt) o = *opt;
+    psi::Solver *s = nullptr;
+    rc = psi::Solver::create(u, o, &s);
+    if (rc) return rc;
+    rc = s->enable_batch(base);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    psi_batch *b = new psi_batch();
+    b->s = s;
+    b->base = std::move(base);
+    b->m = u.m;
+    *out = b;
+    return PSI_OK;
+    PSI_GUARD_END
+}
+
+void psi_batch_destroy(psi_batch *b)
+{
+    if (!b) return;
+    delete b->s;
+    delete b;
+}
+
+int psi_batch_info(psi_batch *b, int32_t *games, int64_t *vertices, int64_t *edges)
+{
+    if (!b || !b->s) return psi::fail(PSI_ERR_INVALID, "null batch");
+    if (games) *games = (int32_t)b->base.size() - 1;
+    if (vertices) *vertices = b->base.back();
+    if (edges) *edges = b->m;
+    return PSI_OK;
+}
+
+int psi_batch_solve(psi_batch *b, int32_t *iter_counts, int32_t *br_counts)
+{
+    if (!b || !b->s || !iter_counts || !br_counts) return psi::fail(PSI_ERR_INVALID, "null argument");
+    PSI_GUARD_BEGIN
+    return b->s->solve_batch(iter_counts, br_counts);
+    PSI_GUARD_END
+}
+
+static int batch_game(psi_batch *b, int32_t game, int64_t *v0, int64_t *n)
+{
+    if (!b || !b->s) return psi::fail(PSI_ERR_INVALID, "null batch");
+    if (game < 0 || game + 1 >= (int32_t)b->base.size()) return psi::fail(PSI_ERR_INVALID, "game index out of range");
+    *v0 = b->base[game];
+    *n = b->base[game + 1] - b->base[game];
+    return PSI_OK;
+}
+
+int psi_batch_get_strategy(psi_batch *b, int32_t game, int32_t *out)
+{
+    int64_t v0 = 0, n = 0;
+    int rc = batch_game(b, game, &v0, &n);
+    if (rc) return rc;
+    if (!out) return psi::fail(PSI_ERR_INVALID, "null output");
+    PSI_GUARD_BEGIN
+    rc = b->s->get_strategy_range(v0, n, out);
+    if (rc) return rc;
+    for (int64_t i = 0; i < n; i++)
+        if (out[i] >= 0) out[i] -= (int32_t)v0;
+    return PSI_OK;
+    PSI_GUARD_END
+}
+
+int psi_batch_get_winning(psi_batch *b, int32_t game, int32_t player, int32_t *out, int64_t cap, int64_t *count)
+{
+    int64_t v0 = 0, n = 0;
+    int rc = batch_game(b, game, &v0, &n);
+    if (rc) return rc;
+    if (player != 0 && player != 1) return psi::fail(PSI_ERR_INVALID, "player must be 0 or 1");
+    PSI_GUARD_BEGIN
+    std::vector<int32_t> inf((size_t)n);
+    rc = b->s->get_infinite_range(v0, n, inf.data());
+    if (rc) return rc;
+    int64_t k = 0;
+    for (int64_t i = 0; i < n; i++) {
+        bool w0 = inf[i] == 1;
+        if ((player == 0 && w0) || (player == 1 && !w0)) {
+            if (out && k < cap) out[k] = (int32_t)i;
+            k++;
+        }
+    }
+    if (count) *count = k;
+    return PSI_OK;
+    PSI_GUARD_END
 }
 
 }  // extern "C"

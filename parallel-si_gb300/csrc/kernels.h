@@ -59,10 +59,15 @@ void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ul
 // ---- all-switches (gpu_parity.cu:191-317, cpu_parity.cpp:154-263)
 // Switches the np vertices listed in plist (all owned by `player`).
 // stats[0..3] += compared edges, walk loads, changed vertices, strict
-// improvements.
+// improvements; with game_of (batches) also gcount[game] += improvements.
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player,
                    const int32_t *off, const int32_t *tgt, int32_t *strat, const int32_t *st,
-                   const PathNode *node, unsigned long long *stats, uint32_t *err);
+                   const PathNode *node, unsigned long long *stats, const int32_t *game_of,
+                   unsigned long long *gcount, uint32_t *err);
+// ---- batches: per-game accounting of solve_si (state[g] = brs, iters,
+// odd_done, done; gcount[g] = strict improvements of the last switch step)
+void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state,
+                          unsigned long long *gcount);
 // ---- dense valuation rows for export (the reference's ArrayVal layout)
 void launch_materialize(cudaStream_t s, int32_t v0, int32_t count, int32_t d, const int32_t *st,
                         const PathNode *node, int32_t *rows, uint32_t *err);

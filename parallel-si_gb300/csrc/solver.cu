@@ -306,7 +306,7 @@ int Solver::switch_strategy(int32_t player, int64_t *switched)
     phase_begin(PH_SWITCH);
     const int32_t np = (player == 0) ? np0_ : n_ - np0_;
     const int32_t *pl = plist_ + (player == 0 ? 0 : np0_);
-    launch_switch(stream_, np, pl, player, off_, tgt_, strat_, st_, node_, dw_->sw, &dw_->err);
+    launch_switch(stream_, np, pl, player, off_, tgt_, strat_, st_, node_, dw_->sw, game_of_, gcount_, &dw_->err);
     phase_end(PH_SWITCH);
     rc = sync_and_check("switch_strategy");
     if (rc) return rc;
@@ -349,6 +349,26 @@ int Solver::get_winning(int32_t player, std::vector<int32_t> &out)
         bool w0 = inf[v] == 1;
         if ((player == 0 && w0) || (player == 1 && !w0)) out.push_back(v);
     }
+    return PSI_OK;
+}
+
+int Solver::get_range(const int32_t *src, int64_t v0, int64_t count, int32_t *out)
+{
+    if (v0 < 0 || count < 0 || v0 + count > n_) return fail(PSI_ERR_INVALID, "vertex range out of bounds");
+    int rc = set_device();
+    if (rc) return rc;
+    if (count) PSI_CUDA_TRY(cudaMemcpyAsync(out, src + v0, 4 * (size_t)count, cudaMemcpyDeviceToHost, stream_));
+    PSI_CUDA_TRY(cudaStreamSynchronize(stream_));
+    return PSI_OK;
+}
+
+int Solver::get_strategy_range(int64_t v0, int64_t count, int32_t *out) { return get_range(strat_, v0, count, out); }
+
+int Solver::get_infinite_range(int64_t v0, int64_t count, int32_t *out)
+{
+    int rc = get_range(st_, v0, count, out);
+    if (rc) return rc;
+    for (int64_t i = 0; i < count; i++) out[i] = st_infinite(out[i]);
     return PSI_OK;
 }
 
@@ -456,6 +476,78 @@ int Solver::solve(int32_t reset, int32_t *iters, int32_t *brs, int64_t max_evals
     }
     *iters = it;
     *brs = br;
+    return PSI_OK;
+}
+
+int Solver::enable_batch(const std::vector<int64_t> &base)
+{
+    if (games_) return fail(PSI_ERR_STATE, "batch partition already set");
+    int32_t g = (int32_t)base.size() - 1;
+    if (g < 1 || base[0] != 0 || base[g] != n_) return fail(PSI_ERR_INVALID, "batch partition does not cover the game");
+    int rc = set_device();
+    if (rc) return rc;
+    std::vector<int32_t> game_of(n_);
+    for (int32_t k = 0; k < g; k++) {
+        if (base[k + 1] <= base[k]) return fail(PSI_ERR_INVALID, "empty game in batch");
+        for (int64_t v = base[k]; v < base[k + 1]; v++) game_of[v] = k;
+    }
+    const struct {
+        void **ptr;
+        size_t bytes;
+    } arrays[] = {{(void **)&game_of_, 4 * (size_t)n_}, {(void **)&gstate_, sizeof(int4) * (size_t)g},
+                  {(void **)&gcount_, sizeof(unsigned long long) * (size_t)g}};
+    for (const auto &a : arrays) {
+        cudaError_t e = cudaMalloc(a.ptr, a.bytes);
+        if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        allocs_.push_back(*a.ptr);
+    }
+    PSI_CUDA_TRY(cudaMemcpyAsync(game_of_, game_of.data(), 4 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
+    PSI_CUDA_TRY(cudaMemsetAsync(gcount_, 0, 8 * (size_t)g, stream_));
+    PSI_CUDA_TRY(cudaStreamSynchronize(stream_));
+    games_ = g;
+    return PSI_OK;
+}
+
+// solve_si (main.cpp:20-55) over the union with per-game accounting
+// (launch_batch_account): the union's loops end when no game switches.
+int Solver::solve_batch(int32_t *iters, int32_t *brs)
+{
+    if (!games_) return fail(PSI_ERR_STATE, "not a batch");
+    int rc = init_strat();
+    if (rc) return rc;
+    PSI_CUDA_TRY(cudaMemsetAsync(gstate_, 0, 16 * (size_t)games_, stream_));
+    PSI_CUDA_TRY(cudaMemsetAsync(gcount_, 0, 8 * (size_t)games_, stream_));
+    for (;;) {
+        for (;;) {
+            rc = compute_valuation();
+            if (rc) return rc;
+            launch_batch_account(stream_, games_, 0, gstate_, gcount_);
+            rc = mark_solved(1);
+            if (rc) return rc;
+            int64_t sw = 0;
+            rc = switch_strategy(1, &sw);
+            if (rc) return rc;
+            launch_batch_account(stream_, games_, 1, gstate_, gcount_);
+            if (sw == 0) break;
+        }
+        rc = mark_solved(0);
+        if (rc) return rc;
+        launch_batch_account(stream_, games_, 2, gstate_, gcount_);
+        int64_t sw = 0;
+        rc = switch_strategy(0, &sw);
+        if (rc) return rc;
+        launch_batch_account(stream_, games_, 3, gstate_, gcount_);
+        if (sw == 0) break;
+    }
+    std::vector<int4> st((size_t)games_);
+    PSI_CUDA_TRY(cudaMemcpyAsync(st.data(), gstate_, 16 * (size_t)games_, cudaMemcpyDeviceToHost, stream_));
+    rc = sync_and_check("solve_batch");
+    if (rc) return rc;
+    for (int32_t k = 0; k < games_; k++) {
+        brs[k] = st[k].x;
+        iters[k] = st[k].y;
+        if (!st[k].w) return fail(PSI_ERR_STATE, "batch loop ended with an unfinished game");
+    }
     return PSI_OK;
 }
 

@@ -43,6 +43,8 @@ public:
     int reset_opponent_strategy();
 
     int get_strategy(int32_t *out);
+    int get_strategy_range(int64_t v0, int64_t count, int32_t *out);
+    int get_infinite_range(int64_t v0, int64_t count, int32_t *out);
     int set_strategy(const int32_t *in);
     int get_infinite(int32_t *out);
     int get_solved(int32_t *out);
@@ -62,10 +64,18 @@ public:
     int timer_begin();
     int timer_end(double *ms);
 
+    // Batches: the solver's game is a disjoint union of games, game g owning
+    // vertices [base[g], base[g+1]).  solve_batch runs solve_si over the union
+    // and returns each game's own iteration and evaluation counts.
+    int enable_batch(const std::vector<int64_t> &base);
+    int solve_batch(int32_t *iters, int32_t *brs);
+    int32_t batch_games() const { return games_; }
+
 private:
     Solver() = default;
     int alloc(const HostGame &g, const psi_options &opt);
     int sync_and_check(const char *what);
+    int get_range(const int32_t *src, int64_t v0, int64_t count, int32_t *out);
     int set_device();
 
     int device_ = 0;
@@ -92,6 +102,11 @@ private:
     int8_t *owner_ = nullptr;
     int32_t *pri_ = nullptr, *off_ = nullptr, *tgt_ = nullptr, *plist_ = nullptr;
     int32_t np0_ = 0;
+    // batch partition (games_ == 0 for a single game)
+    int32_t games_ = 0;
+    int32_t *game_of_ = nullptr;
+    int4 *gstate_ = nullptr;
+    unsigned long long *gcount_ = nullptr;
     // state
     int32_t *strat_ = nullptr, *st_ = nullptr;
     uint8_t *solved_ = nullptr;

@@ -131,12 +131,15 @@ __device__ __forceinline__ int2 summary_of(const PathNode *__restrict__ node, in
 // One thread per vertex of plist (all owned by `player`).
 // stats[0] += compared edges, stats[1] += parent/priority loads of tier-3
 // walks, stats[2] += vertices whose strategy changed, stats[3] += strict
-// improvements.
+// improvements.  For a batch of games (game_of != nullptr) the strict
+// improvements are also added to gcount[game of the vertex].
 __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__restrict__ plist, int32_t player,
                                                    const int32_t *__restrict__ off, const int32_t *__restrict__ tgt,
                                                    int32_t *__restrict__ strat, const int32_t *__restrict__ st,
                                                    const PathNode *__restrict__ node,
                                                    unsigned long long *__restrict__ stats,
+                                                   const int32_t *__restrict__ game_of,
+                                                   unsigned long long *__restrict__ gcount,
                                                    uint32_t *__restrict__ err)
 {
     int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -171,7 +174,10 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
                 moves++;
             }
         }
-        if (moves) strat[v] = cur;
+        if (moves) {
+            strat[v] = cur;
+            if (game_of) atomicAdd(&gcount[game_of[v]], (unsigned long long)moves);
+        }
     }
     typedef cub::BlockReduce<int4, kBlock> Reduce;
     __shared__ typename Reduce::TempStorage tmp;
@@ -185,6 +191,42 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
         if (tot.z) atomicAdd(&stats[2], (unsigned long long)tot.z);
         if (tot.w) atomicAdd(&stats[3], (unsigned long long)tot.w);
     }
+}
+
+// Per-game accounting of the solve_si loop (main.cpp:20-55) run over a batch
+// of games packed as one disjoint union.  Paths never leave their game, so a
+// game's strategies and valuations evolve exactly as in a solo solve; a game
+// whose loop has already converged only sees steps that change nothing.  The
+// counters below therefore reproduce each game's solo iteration and
+// evaluation counts.  state[g] = (evaluations, iterations, Odd's best response
+// reached, game done); gcount[g] = strict improvements of game g in the last
+// switch step (read and cleared here).
+//   event 0: an evaluation      -> evaluations++ for games inside their best-response loop
+//   event 1: after switch(Odd)  -> a game whose Odd made no improvement has its best response
+//   event 2: before switch(Even)-> iterations++ for games not done
+//   event 3: after switch(Even) -> a game whose Even made no improvement is done; the others
+//                                  re-enter their best-response loop
+__global__ void k_batch_account(int32_t games, int32_t event, int4 *__restrict__ state,
+                                unsigned long long *__restrict__ gcount)
+{
+    int32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= games) return;
+    int4 s = state[g];
+    if (event == 0) {
+        if (!s.w && !s.z) s.x++;
+    } else if (event == 1) {
+        if (!s.w && !s.z && gcount[g] == 0) s.z = 1;
+        gcount[g] = 0;
+    } else if (event == 2) {
+        if (!s.w) s.y++;
+    } else {
+        if (!s.w) {
+            if (gcount[g] == 0) s.w = 1;
+            else s.z = 0;
+        }
+        gcount[g] = 0;
+    }
+    state[g] = s;
 }
 
 // Dense row of v: counts of the priorities on its strategy path (the reference
@@ -215,11 +257,19 @@ __global__ void k_materialize(int32_t v0, int32_t count, int32_t d, const int32_
 
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player, const int32_t *off,
                    const int32_t *tgt, int32_t *strat, const int32_t *st, const PathNode *node,
-                   unsigned long long *stats, uint32_t *err)
+                   unsigned long long *stats, const int32_t *game_of, unsigned long long *gcount, uint32_t *err)
 {
     if (np <= 0) return;
     count_launch();
-    k_switch<<<grid_for(np), kBlock, 0, s>>>(np, plist, player, off, tgt, strat, st, node, stats, err);
+    k_switch<<<grid_for(np), kBlock, 0, s>>>(np, plist, player, off, tgt, strat, st, node, stats, game_of,
+                                             gcount, err);
+}
+
+void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state, unsigned long long *gcount)
+{
+    if (games <= 0) return;
+    count_launch();
+    k_batch_account<<<grid_for(games), kBlock, 0, s>>>(games, event, state, gcount);
 }
 
 void launch_materialize(cudaStream_t s, int32_t v0, int32_t count, int32_t d, const int32_t *st,

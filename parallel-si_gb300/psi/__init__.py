@@ -21,7 +21,7 @@ def launch_count() -> int:
     """Kernel launches issued by the native library in this process."""
     return int(lib.psi_launch_count())
 
-__all__ = ["Game", "GPUList", "PsiError", "Options", "solve_si", "default_options", "version"]
+__all__ = ["Game", "GPUList", "Batch", "PsiError", "Options", "solve_si", "batch_sizes", "default_options", "version"]
 
 
 def version() -> str:
@@ -250,6 +250,64 @@ class GPUList:
     def close(self) -> None:
         if self._h:
             lib.psi_solver_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_sizes(count: int, n_lo: int, n_hi: int, seed: int = 1) -> np.ndarray:
+    """Seeded sizes log-uniform in [n_lo, n_hi] (psi_generate_batch_sizes)."""
+    out = np.empty(count, np.int32)
+    check(lib.psi_generate_batch_sizes(count, n_lo, n_hi, C.c_uint64(seed), ptr(out)))
+    return out
+
+
+class Batch:
+    """Many games solved together on one GPU (psi_batch_*).  Each game ends
+    with the results of its own solo solve."""
+
+    def __init__(self, games, options: Optional[Options] = None, **kw):
+        o = options if options is not None else default_options(**kw)
+        self.sizes = [g.n for g in games]
+        handles = (C.c_void_p * len(games))(*[g._h.value for g in games])
+        self._h = C.c_void_p()
+        check(lib.psi_batch_create(C.cast(handles, C.c_void_p), len(games), C.byref(o), C.byref(self._h)))
+
+    def __len__(self):
+        return len(self.sizes)
+
+    def info(self):
+        g = C.c_int32()
+        v = C.c_int64()
+        e = C.c_int64()
+        check(lib.psi_batch_info(self._h, C.byref(g), C.byref(v), C.byref(e)))
+        return g.value, v.value, e.value
+
+    def solve(self):
+        """(iter_counts, br_counts) per game."""
+        it = np.empty(len(self), np.int32)
+        br = np.empty(len(self), np.int32)
+        check(lib.psi_batch_solve(self._h, ptr(it), ptr(br)))
+        return it, br
+
+    def get_strategy(self, game: int) -> np.ndarray:
+        out = np.empty(self.sizes[game], np.int32)
+        check(lib.psi_batch_get_strategy(self._h, game, ptr(out)))
+        return out
+
+    def get_winning(self, game: int, player: int) -> np.ndarray:
+        out = np.empty(self.sizes[game], np.int32)
+        k = C.c_int64()
+        check(lib.psi_batch_get_winning(self._h, game, player, ptr(out), len(out), C.byref(k)))
+        return out[: k.value]
+
+    def close(self) -> None:
+        if self._h:
+            lib.psi_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):

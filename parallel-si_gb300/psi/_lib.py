@@ -95,6 +95,13 @@ _SIGS = {
     "psi_launch_count": ([], C.c_int64),
     "psi_solver_timer_begin": ([_vp], C.c_int),
     "psi_solver_timer_end": ([_vp, C.POINTER(C.c_double)], C.c_int),
+    "psi_generate_batch_sizes": ([C.c_int32, C.c_int32, C.c_int32, C.c_uint64, _vp], C.c_int),
+    "psi_batch_create": ([_vp, C.c_int32, C.POINTER(Options), _pp], C.c_int),
+    "psi_batch_destroy": ([_vp], None),
+    "psi_batch_info": ([_vp, _i32p, _i64p, _i64p], C.c_int),
+    "psi_batch_solve": ([_vp, _vp, _vp], C.c_int),
+    "psi_batch_get_strategy": ([_vp, C.c_int32, _vp], C.c_int),
+    "psi_batch_get_winning": ([_vp, C.c_int32, C.c_int32, _vp, C.c_int64, _i64p], C.c_int),
 }
 
 COUNTERS = ("evals", "switches", "sw_edges", "sw_loads", "sw_changed", "unreached", "jump_rounds")

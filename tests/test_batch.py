@@ -1,0 +1,60 @@
+"""Batched solving: games packed into one segmented CSR and solved together
+must each end exactly as their solo solve -- strategy, winning sets, iteration
+and evaluation counts (the C4 workload shape: sizes log-uniform, out-degree
+U[2,8], priority U[0,n_i))."""
+import numpy as np
+import pytest
+
+import oracle
+import psi
+
+
+def c4_games(count, n_lo, n_hi, seed):
+    sizes = psi.batch_sizes(count, n_lo, n_hi, seed)
+    return [psi.Game.random(int(n), 2, 8, int(n), seed * 100003 + i) for i, n in enumerate(sizes)]
+
+
+def test_batch_sizes_are_log_uniform_and_seeded():
+    a = psi.batch_sizes(4096, 100, 200000, 7)
+    assert np.array_equal(a, psi.batch_sizes(4096, 100, 200000, 7))
+    assert a.min() >= 100 and a.max() <= 200000
+    logs = np.log(a.astype(np.float64))
+    assert abs(np.median(logs) - (np.log(100) + np.log(200000)) / 2) < 0.3
+
+
+@pytest.mark.gpu
+def test_batch_matches_solo_oracle():
+    games = c4_games(40, 20, 3000, 3) + [psi.Game.longpath(500, 64, 9)]
+    b = psi.Batch(games)
+    assert b.info()[0] == len(games)
+    it, br = b.solve()
+    for k, g in enumerate(games):
+        o = oracle.Oracle(*g.csr())
+        assert (it[k], br[k]) == o.solve(), f"game {k}"
+        assert np.array_equal(b.get_strategy(k), o.get_strategy()), f"game {k}"
+        assert np.array_equal(b.get_winning(k, 0), o.get_winning(0)), f"game {k}"
+        assert np.array_equal(b.get_winning(k, 1), o.get_winning(1)), f"game {k}"
+
+
+@pytest.mark.gpu
+def test_batch_matches_solo_gpu_on_larger_games():
+    games = c4_games(12, 1000, 60000, 5)
+    b = psi.Batch(games)
+    it, br = b.solve()
+    for k, g in enumerate(games):
+        s = psi.GPUList(g)
+        assert (it[k], br[k]) == s.solve(), f"game {k}"
+        assert np.array_equal(b.get_strategy(k), s.get_strategy())
+        assert np.array_equal(b.get_winning(k, 0), s.get_winning(0))
+        s.close()
+
+
+@pytest.mark.gpu
+def test_batch_solve_is_repeatable():
+    games = c4_games(25, 50, 5000, 11)
+    b = psi.Batch(games)
+    first = b.solve()
+    strats = [b.get_strategy(k) for k in range(len(games))]
+    again = b.solve()
+    assert all(np.array_equal(x, y) for x, y in zip(first, again))
+    assert all(np.array_equal(s, b.get_strategy(k)) for k, s in enumerate(strats))
