@@ -395,6 +395,99 @@ def run_batch(args, rank, world, local):
     return 0
 
 
+def serve_once(srv, games, arrivals):
+    """Feeds `games` to the server at the given arrival times (seconds from
+    the start; wall clock) and steps it until all finished.  Returns (elapsed
+    s, per-game latency s, per-game (iters, brs), steps, mean resident games)."""
+    import numpy as np
+
+    order = np.argsort(arrivals, kind="stable")
+    lat = np.zeros(len(games))
+    counts = [None] * len(games)
+    of_ticket = {}
+    done = steps = resident_sum = 0
+    i = 0
+    t0 = time.perf_counter()
+    while done < len(games):
+        now = time.perf_counter() - t0
+        while i < len(games) and arrivals[order[i]] <= now:
+            k = int(order[i])
+            of_ticket[srv.submit(games[k])] = k
+            i += 1
+        r, q, _, _ = srv.info()
+        if r == 0 and q == 0:
+            time.sleep(max(0.0, arrivals[order[i]] - now))
+            continue
+        srv.step()
+        steps += 1
+        resident_sum += r
+        t_end = time.perf_counter() - t0
+        for t in srv.finished():
+            k = of_ticket.pop(int(t))
+            _, it, br = srv.status(int(t))
+            counts[k] = (it, br)
+            lat[k] = t_end - arrivals[k]
+            srv.take(int(t))
+            done += 1
+    return time.perf_counter() - t0, lat, counts, steps, resident_sum / max(steps, 1)
+
+
+def run_serve(args, rank, world, local):
+    """Serving workload (not the headline line): `--serve-games` random games
+    (sizes log-uniform in [100, 200000], out-degree U[2,8], priority U[0,n_i))
+    arrive at one continuous-batching server (psi_server_*) whose arena holds
+    `--arena-vertices` vertex slots.  First all arrive at once (saturated:
+    the throughput ceiling); then they arrive as a Poisson process at fixed
+    fractions of that ceiling.  Latency = arrival to the end of the step in
+    which the game finished (wall clock); every game's iteration and
+    evaluation counts are checked against solo solves of a stride sample."""
+    import numpy as np
+    import psi
+
+    sizes = psi.batch_sizes(args.serve_games, 100, 200000, args.seed)
+    games = [psi.Game.random(int(n), 2, 8, int(n), args.seed * 100003 + i) for i, n in enumerate(sizes)]
+    srv = psi.Server(args.arena_vertices, 8 * args.arena_vertices, args.serve_slots, device=local)
+    warm = games[: max(8, len(games) // 16)]
+    for _ in range(args.warmup):
+        serve_once(srv, warm, np.zeros(len(warm)))
+    el, lat, counts, steps, mres = serve_once(srv, games, np.zeros(len(games)))
+    sat = len(games) / el
+    loads = []
+    rng = np.random.default_rng(args.seed)
+    for frac in (0.5, 0.8):
+        rate = frac * sat
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, len(games)))
+        el2, lat2, counts2, steps2, mres2 = serve_once(srv, games, arrivals)
+        assert counts2 == counts
+        loads.append({"offered_games_per_s": rate, "games_per_s": len(games) / el2,
+                      "p50_ms": 1000 * float(np.percentile(lat2, 50)),
+                      "p99_ms": 1000 * float(np.percentile(lat2, 99)), "steps": steps2,
+                      "mean_resident_games": mres2})
+    solo_idx = list(range(0, len(games), args.solo_stride))
+    exact = True
+    for k in solo_idx:
+        s = psi.GPUList(games[k], device=local)
+        exact = exact and tuple(s.solve()) == tuple(counts[k])
+        s.close()
+    line = {
+        "metric": "games/s (served, saturated)", "value": sat, "unit": "games/s", "n_gpus": world,
+        "steps": 1, "warmup": args.warmup, "ms_per_step": 1000 * el, "higher_is_better": True,
+        "dtype": "int32", "data": "synthetic",
+        "config": {"workload": f"{len(games)} random games served, n_i log-uniform in [100,200000], out-degree "
+                               f"U[2,8], priority U[0,n_i)", "arena_vertices": args.arena_vertices,
+                   "arena_edges": 8 * args.arena_vertices, "max_games": args.serve_slots,
+                   "total_vertices": int(sum(sizes))},
+        "saturated": {"games_per_s": sat, "p50_ms": 1000 * float(np.percentile(lat, 50)),
+                      "p99_ms": 1000 * float(np.percentile(lat, 99)), "steps": steps,
+                      "mean_resident_games": mres},
+        "poisson": loads,
+        "counts_match_solo": exact, "solo_checked": len(solo_idx),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -405,10 +498,14 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--sublist-len", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
-    ap.add_argument("--workload", choices=("single", "batch"), default="single",
-                    help="single: the 2^24 game (headline); batch: many mixed-size games")
+    ap.add_argument("--workload", choices=("single", "batch", "serve"), default="single",
+                    help="single: the 2^24 game (headline); batch: many mixed-size games solved together; "
+                         "serve: the same kind of games arriving at a continuous-batching server")
     ap.add_argument("--batch-games", type=int, default=4096)
     ap.add_argument("--solo-stride", type=int, default=16)
+    ap.add_argument("--serve-games", type=int, default=2048)
+    ap.add_argument("--serve-slots", type=int, default=4096)
+    ap.add_argument("--arena-vertices", type=int, default=1 << 24)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -417,6 +514,8 @@ def main():
         return run_reference(args, rank, world)
     if args.workload == "batch":
         return run_batch(args, rank, world, local)
+    if args.workload == "serve":
+        return run_serve(args, rank, world, local)
     return run_gb300(args, rank, world, local)
 
 

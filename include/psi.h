@@ -181,6 +181,48 @@ int psi_batch_solve(psi_batch *b, int32_t *iter_counts, int32_t *br_counts);
 int psi_batch_get_strategy(psi_batch *b, int32_t game, int32_t *out);
 int psi_batch_get_winning(psi_batch *b, int32_t game, int32_t player, int32_t *out, int64_t cap, int64_t *count);
 
+/* ---------------------------------------------------------------- serving
+ * Continuous batching: games are submitted at any time and solved together in
+ * one resident arena of vertex and edge ranges on the device.  Each
+ * psi_server_step admits queued games in arrival order as far as ranges and
+ * game slots allow (first fit: a game that does not fit yet waits without
+ * blocking smaller ones behind it), runs one solve_si step (an evaluation,
+ * Odd's switch, and Even's switch for the games whose Odd step made no strict
+ * improvement) of every resident game at once, and retires the games that
+ * finished, freeing their ranges for the next admissions.  Each game follows
+ * exactly the step sequence of its solo psi_solve, so its strategy, winning
+ * sets and iteration/evaluation counts do not depend on what else is
+ * resident.  No counterpart in the reference, which solves one game per
+ * process run.  A game of n vertices and m edges takes n+1 vertex slots and m
+ * edge slots. */
+typedef struct psi_server psi_server;
+/* max_vertices: vertex slots (at most 2^30-2); max_edges: edge slots (at most
+ * 2^31-1); max_games: games resident at once; reset != 0: the reset variant
+ * of solve_si.  The device memory is allocated here, once. */
+int psi_server_create(int64_t max_vertices, int64_t max_edges, int32_t max_games, int32_t reset,
+                      const psi_options *opt, psi_server **out);
+void psi_server_destroy(psi_server *s);
+/* Queues a copy of the game (the handle may be freed afterwards); *ticket
+ * names the request.  PSI_ERR_TOO_LARGE if the game can never fit the arena. */
+int psi_server_submit(psi_server *s, const psi_game *g, int64_t *ticket);
+/* One serving step (see above); *finished receives the number of games that
+ * finished in it (may be NULL). */
+int psi_server_step(psi_server *s, int32_t *finished);
+/* Tickets of the games that finished in the last psi_server_step, in slot
+ * order: *count receives how many, at most cap are copied to tickets. */
+int psi_server_finished(psi_server *s, int64_t *tickets, int32_t cap, int32_t *count);
+/* state: PSI_REQ_QUEUED, PSI_REQ_RESIDENT or PSI_REQ_FINISHED; iter_count and
+ * br_count are the solve_si counts once finished.  Any output may be NULL. */
+enum { PSI_REQ_QUEUED = 0, PSI_REQ_RESIDENT = 1, PSI_REQ_FINISHED = 2 };
+int psi_server_status(psi_server *s, int64_t ticket, int32_t *state, int32_t *iter_count, int32_t *br_count);
+/* Result of a finished request, in the game's own vertex ids: strategy[n]
+ * (-1 = the sink) and infinite[n] (+1 / -1 / 0 as psi_get_infinite: Even
+ * wins exactly the vertices with +1).  Either output may be NULL.  The request
+ * is forgotten afterwards. */
+int psi_server_take(psi_server *s, int64_t ticket, int32_t *strategy, int32_t *infinite);
+/* Games resident and queued; vertex and edge slots in use. */
+int psi_server_info(psi_server *s, int32_t *resident, int32_t *queued, int64_t *used_vertices, int64_t *used_edges);
+
 /* ------------------------------------------------- evaluation without allocation
  * No counterpart in the reference.  For callers that must not allocate device
  * memory while they run -- e.g. a serving process that reserves its device

@@ -12,6 +12,7 @@
 #include "kernels.h"
 #include "psi.h"
 #include "psi_internal.h"
+#include "serve.h"
 #include "solver.h"
 
 struct psi_game {
@@ -26,6 +27,10 @@ struct psi_batch {
     psi::Solver *s = nullptr;
     std::vector<int64_t> base;   // game k owns union vertices [base[k], base[k+1])
     int64_t m = 0;
+};
+
+struct psi_server {
+    psi::Server *s = nullptr;
 };
 
 namespace psi {
@@ -441,6 +446,80 @@ int psi_batch_get_winning(psi_batch *b, int32_t game, int32_t player, int32_t *o
     if (count) *count = k;
     return PSI_OK;
     PSI_GUARD_END
+}
+
+int psi_server_create(int64_t max_vertices, int64_t max_edges, int32_t max_games, int32_t reset,
+                      const psi_options *opt, psi_server **out)
+{
+    if (!out) return psi::fail(PSI_ERR_INVALID, "null output");
+    *out = nullptr;
+    if (max_vertices > (1ll << 30) - 2 || max_edges > INT32_MAX)
+        return psi::fail(PSI_ERR_TOO_LARGE, "arena beyond the int32 layout");
+    PSI_GUARD_BEGIN
+    psi_options o;
+    psi_options_default(&o);
+    if (opt) o = *opt;
+    psi::Server *srv = nullptr;
+    int rc = psi::make_server(max_vertices, max_edges, max_games, reset != 0, o, &srv);
+    if (rc) return rc;
+    psi_server *h = new psi_server();
+    h->s = srv;
+    *out = h;
+    return PSI_OK;
+    PSI_GUARD_END
+}
+
+void psi_server_destroy(psi_server *s)
+{
+    if (!s) return;
+    if (s->s) psi::server_destroy(s->s);
+    delete s;
+}
+
+int psi_server_submit(psi_server *s, const psi_game *g, int64_t *ticket)
+{
+    if (!s || !s->s || !g || !ticket) return psi::fail(PSI_ERR_INVALID, "null argument");
+    PSI_GUARD_BEGIN
+    return psi::server_submit(s->s, g->g, ticket);
+    PSI_GUARD_END
+}
+
+int psi_server_step(psi_server *s, int32_t *finished)
+{
+    if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null server");
+    PSI_GUARD_BEGIN
+    int32_t k = 0;
+    int rc = psi::server_step(s->s, &k);
+    if (finished) *finished = k;
+    return rc;
+    PSI_GUARD_END
+}
+
+int psi_server_finished(psi_server *s, int64_t *tickets, int32_t cap, int32_t *count)
+{
+    if (!s || !s->s || !count || (cap > 0 && !tickets)) return psi::fail(PSI_ERR_INVALID, "null argument");
+    return psi::server_finished(s->s, tickets, cap, count);
+}
+
+int psi_server_status(psi_server *s, int64_t ticket, int32_t *state, int32_t *iter_count, int32_t *br_count)
+{
+    if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null server");
+    return psi::server_status(s->s, ticket, state, iter_count, br_count);
+}
+
+int psi_server_take(psi_server *s, int64_t ticket, int32_t *strategy, int32_t *infinite)
+{
+    if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null server");
+    PSI_GUARD_BEGIN
+    return psi::server_take(s->s, ticket, strategy, infinite);
+    PSI_GUARD_END
+}
+
+int psi_server_info(psi_server *s, int32_t *resident, int32_t *queued, int64_t *used_vertices, int64_t *used_edges)
+{
+    if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null server");
+    psi::server_info(s->s, resident, queued, used_vertices, used_edges);
+    return PSI_OK;
 }
 
 }  // extern "C"

@@ -15,11 +15,10 @@
 //     (pick_heads, gpu_list_ranking.cu:96-110); one thread per sublist walks to
 //     the next head accumulating +1/-1 depth steps (walk_sublists,
 //     gpu_list_ranking.cu:114-193).  The reduced list of sublists is ranked on
-//     the device -- the reference copies it to the host and walks it serially
-//     (gpu_list_ranking.cu:197-240): a second Helman-JaJa level groups the
-//     sublists into segments (red_walk), one block ranks the segments by Wyllie
-//     pointer jumping (red_block), and red_finish gives every sublist its
-//     suffix sum and whether the list start reaches it.
+//     the device by Wyllie pointer jumping in one cooperative launch
+//     (rank_reduced) -- the reference copies it to the host and walks it
+//     serially (gpu_list_ranking.cu:197-240) -- giving every sublist its suffix
+//     sum and whether the list start reaches it.
 //  3. Broadcast (broadcast_depth, gpu_list_ranking.cu:244-277): a vertex the
 //     sink reaches gets its path length; its parent and priority are snapshot
 //     for the comparison walks of the following switch step.  Vertices the
@@ -385,13 +384,19 @@ __global__ void __launch_bounds__(kBlock) k_cycles(const int32_t *__restrict__ u
 
 // mark_solved restricted to the last evaluation's unreached vertices: every
 // other non-solved vertex is finite.
+// With game_of/gmask (served games), only vertices of games whose mask is set.
 __global__ void k_mark_solved(const int32_t *__restrict__ ucount, const int32_t *__restrict__ ulist,
-                              int32_t player, const int32_t *__restrict__ st, uint8_t *__restrict__ solved)
+                              int32_t player, const int32_t *__restrict__ st, uint8_t *__restrict__ solved,
+                              const int32_t *__restrict__ game_of, const int32_t *__restrict__ gmask)
 {
     int32_t nu = *ucount;
     int32_t target = (player == 0) ? ST_POS_INF : ST_NEG_INF;
     for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nu; i += gridDim.x * blockDim.x) {
         int32_t u = ulist[i];
+        if (gmask) {
+            int32_t g = game_of[u];
+            if (g < 0 || !gmask[g]) continue;
+        }
         if (st[u] == target) solved[u] = 1;
     }
 }
@@ -513,10 +518,10 @@ int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, c
 }
 
 void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, int32_t player,
-                        const int32_t *st, uint8_t *solved)
+                        const int32_t *st, uint8_t *solved, const int32_t *game_of, const int32_t *gmask)
 {
     count_launch();
-    k_mark_solved<<<608, kBlock, 0, s>>>(ucount, ulist, player, st, solved);
+    k_mark_solved<<<608, kBlock, 0, s>>>(ucount, ulist, player, st, solved, game_of, gmask);
 }
 
 }  // namespace psi

@@ -52,22 +52,50 @@ void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *nod
 int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, const int32_t *strat,
                   const int32_t *pri, const uint8_t *solved, int32_t *st, int2 *ja, int2 *jb, int32_t *la,
                   int32_t *lb, int32_t *cnt, uint32_t *err);
-// mark_solved over the last evaluation's unreached vertices (cpu_parity.cpp:265-274)
+// mark_solved over the last evaluation's unreached vertices (cpu_parity.cpp:265-274);
+// with game_of/gmask only for games whose mask is set (nullptr: all).
 void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, int32_t player,
-                        const int32_t *st, uint8_t *solved);
+                        const int32_t *st, uint8_t *solved, const int32_t *game_of = nullptr,
+                        const int32_t *gmask = nullptr);
 
 // ---- all-switches (gpu_parity.cu:191-317, cpu_parity.cpp:154-263)
 // Switches the np vertices listed in plist (all owned by `player`).
 // stats[0..3] += compared edges, walk loads, changed vertices, strict
-// improvements; with game_of (batches) also gcount[game] += improvements.
+// improvements; with game_of (batches) also gcount[game] += improvements,
+// and with gmask only vertices of games whose mask is set switch.
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player,
                    const int32_t *off, const int32_t *tgt, int32_t *strat, const int32_t *st,
                    const PathNode *node, unsigned long long *stats, const int32_t *game_of,
-                   unsigned long long *gcount, uint32_t *err);
+                   unsigned long long *gcount, const int32_t *gmask, uint32_t *err);
 // ---- batches: per-game accounting of solve_si (state[g] = brs, iters,
 // odd_done, done; gcount[g] = strict improvements of the last switch step)
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state,
                           unsigned long long *gcount);
+// ---- serving arena (serve_kernels.cu)
+// Places the games of one admission, uploaded as a packed union (game k owns
+// union vertices [ub[k], ub[k+1]); u_roff/u_rsrc: the union's reverse CSR), at
+// vertices [vb[k], vb[k] + n_k] (the last one an inert sentinel) and edges
+// from eb[k]; resets the slot state of each.
+void launch_arena_place(cudaStream_t s, int32_t nu, int32_t k_games, const int32_t *ub, const int32_t *vb,
+                        const int32_t *eb, const int32_t *slot, const int32_t *u_owner, const int32_t *u_pri,
+                        const int32_t *u_off, const int32_t *u_tgt, const int32_t *u_roff, const int32_t *u_rsrc,
+                        int8_t *owner, int32_t *pri, int32_t *off, int32_t *tgt, int32_t *rev_off, int32_t *rev_src,
+                        int32_t *strat, int32_t *st, uint8_t *solved, int32_t *game_of, int4 *gstate,
+                        unsigned long long *gcount);
+void launch_arena_clear(cudaStream_t s, int32_t vb, int32_t count, uint8_t *solved, int32_t *game_of, int32_t *st);
+// Appends the vertices of `player` that belong to a game to plist (*count += k).
+void launch_build_plist(cudaStream_t s, int32_t n, int32_t player, const int8_t *owner, const int32_t *game_of,
+                        int32_t *plist, int32_t *count);
+// Per-slot solve_si state machine: event 0 after an evaluation, 1 after
+// switch(Odd), 2 after switch(Even) (see serve_kernels.cu).
+void launch_serve_account(cudaStream_t s, int32_t slots, int32_t event, int4 *state, unsigned long long *gcount,
+                          int32_t *gmask);
+// Reset variant: Odd's vertices (plist[0..np)) of games whose masked Even step
+// switched go back to their first successor.
+void launch_serve_reset_odd(cudaStream_t s, int32_t np, const int32_t *plist, const int32_t *game_of,
+                            const int32_t *gmask, const unsigned long long *gcount, const int32_t *off,
+                            const int32_t *tgt, int32_t *strat);
+
 // ---- dense valuation rows for export (the reference's ArrayVal layout)
 void launch_materialize(cudaStream_t s, int32_t v0, int32_t count, int32_t d, const int32_t *st,
                         const PathNode *node, int32_t *rows, uint32_t *err);

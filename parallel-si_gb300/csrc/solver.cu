@@ -28,22 +28,34 @@ int Solver::set_device()
     return PSI_OK;
 }
 
-int Solver::create(const HostGame &g, const psi_options &opt, Solver **out)
+namespace {
+
+int check_options(const psi_options &opt)
 {
-    *out = nullptr;
-    if (g.n <= 0) return fail(PSI_ERR_INVALID, "game has no vertices");
-    if (2 * (int64_t)g.n + 2 > INT32_MAX) return fail(PSI_ERR_TOO_LARGE, "n too large for int32 tour ids");
     if (opt.valuation_mode != PSI_VAL_PATH) return fail(PSI_ERR_INVALID, "unknown valuation_mode");
     if (opt.sublist_len < 2) return fail(PSI_ERR_INVALID, "sublist_len must be >= 2");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0) return fail(PSI_ERR_NO_DEVICE, "no CUDA device available");
     if (opt.device < 0 || opt.device >= ndev) return fail(PSI_ERR_INVALID, "device ordinal out of range");
+    return PSI_OK;
+}
+
+}  // namespace
+
+int Solver::create(const HostGame &g, const psi_options &opt, Solver **out)
+{
+    *out = nullptr;
+    if (g.n <= 0) return fail(PSI_ERR_INVALID, "game has no vertices");
+    if (2 * (int64_t)g.n + 2 > INT32_MAX) return fail(PSI_ERR_TOO_LARGE, "n too large for int32 tour ids");
+    int rc = check_options(opt);
+    if (rc) return rc;
     Solver *s = new Solver();
     s->device_ = opt.device;
     s->timing_ = opt.timing != 0;
     s->stride_ = opt.sublist_len;
-    int rc = s->alloc(g, opt);
+    rc = s->alloc_arrays(g.n, g.m);
+    if (!rc) rc = s->upload_game(g);
     if (rc) {
         delete s;
         return rc;
@@ -52,17 +64,48 @@ int Solver::create(const HostGame &g, const psi_options &opt, Solver **out)
     return PSI_OK;
 }
 
-int Solver::alloc(const HostGame &g, const psi_options &)
+int Solver::create_arena(int64_t max_vertices, int64_t max_edges, int32_t slots, const psi_options &opt,
+                         Solver **out)
 {
-    int rc = set_device();
+    *out = nullptr;
+    if (max_vertices < 2 || max_edges < 1 || slots < 1) return fail(PSI_ERR_INVALID, "empty arena");
+    if (2 * max_vertices + 2 > INT32_MAX || max_edges > INT32_MAX)
+        return fail(PSI_ERR_TOO_LARGE, "arena too large for int32 ids");
+    int rc = check_options(opt);
     if (rc) return rc;
-    n_ = g.n;
-    m_ = g.m;
-    max_pri_ = g.max_pri;
+    Solver *s = new Solver();
+    s->device_ = opt.device;
+    s->timing_ = opt.timing != 0;
+    s->stride_ = opt.sublist_len;
+    rc = s->alloc_arrays(max_vertices, max_edges);
+    if (!rc) rc = s->init_arena(slots);
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return PSI_OK;
+}
+
+// Vertex count the kernels process: the tour has 2n+2 nodes, the sublist
+// heads follow from the stride.
+void Solver::set_extent(int32_t n)
+{
+    n_ = n;
     L_ = 2 * (int64_t)n_ + 2;
     // heads at node j*stride for j < nsub-1, plus the list start (node L-1)
     nsub_ = (int32_t)(ceil_div(L_ - 1, stride_) + 1);
-    game_ = &g;
+}
+
+// Device arrays for games of up to cap_n vertices and cap_m edges.
+int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
+{
+    int rc = set_device();
+    if (rc) return rc;
+    cap_n_ = cap_n;
+    cap_m_ = cap_m;
+    const int64_t capL = 2 * cap_n + 2;
+    const int64_t cap_sub = ceil_div(capL - 1, stride_) + 1;
     PSI_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     for (auto &p : ph_) {
         PSI_CUDA_TRY(cudaEventCreate(&p.a));
@@ -70,47 +113,48 @@ int Solver::alloc(const HostGame &g, const psi_options &)
     }
     PSI_CUDA_TRY(cudaEventCreate(&region_a_));
     PSI_CUDA_TRY(cudaEventCreate(&region_b_));
-
-    auto dalloc = [&](void **p, size_t bytes) -> int {
-        cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
-        if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-        allocs_.push_back(*p);
-        return PSI_OK;
+    const struct {
+        void **ptr;
+        size_t bytes;
+    } arrays[] = {
+        {(void **)&owner_, (size_t)cap_n},
+        {(void **)&pri_, 4 * (size_t)cap_n},
+        {(void **)&off_, 4 * ((size_t)cap_n + 1)},
+        {(void **)&tgt_, 4 * (size_t)cap_m},
+        {(void **)&rev_off_, 4 * ((size_t)cap_n + 1)},
+        {(void **)&rev_src_, 4 * (size_t)cap_m},
+        {(void **)&plist_, 4 * (size_t)cap_n},
+        {(void **)&strat_, 4 * (size_t)cap_n},
+        {(void **)&st_, 4 * (size_t)cap_n},
+        {(void **)&solved_, (size_t)cap_n},
+        {(void **)&node_, sizeof(PathNode) * (size_t)cap_n},
+        {(void **)&succ_, 4 * (size_t)capL},
+        {(void **)&hsucc_, 4 * (size_t)cap_sub},
+        {(void **)&ulist_, 4 * (size_t)cap_n},
+        {(void **)&vloc_, 8 * (size_t)cap_n},
+        {(void **)&redA_, 8 * (size_t)cap_sub},
+        {(void **)&redB_, 8 * (size_t)cap_sub},
+        {(void **)&redC_, 8 * (size_t)cap_sub},
+        {(void **)&jA_, 8 * (size_t)cap_n},
+        {(void **)&jB_, 8 * (size_t)cap_n},
+        {(void **)&dw_, sizeof(Words)},
     };
-#define PSI_DALLOC(ptr, bytes)                                  \
-    do {                                                        \
-        int r__ = dalloc((void **)&(ptr), (size_t)(bytes));     \
-        if (r__) return r__;                                    \
-    } while (0)
-    PSI_DALLOC(owner_, n_);
-    PSI_DALLOC(pri_, 4 * (size_t)n_);
-    PSI_DALLOC(off_, 4 * ((size_t)n_ + 1));
-    PSI_DALLOC(tgt_, 4 * (size_t)m_);
-    PSI_DALLOC(plist_, 4 * (size_t)n_);
-    PSI_DALLOC(strat_, 4 * (size_t)n_);
-    PSI_DALLOC(st_, 4 * (size_t)n_);
-    PSI_DALLOC(solved_, n_);
-    PSI_DALLOC(node_, sizeof(PathNode) * (size_t)n_);
-    PSI_DALLOC(succ_, 4 * (size_t)L_);
-    PSI_DALLOC(hsucc_, 4 * (size_t)nsub_);
-    PSI_DALLOC(ulist_, 4 * (size_t)n_);
-    PSI_DALLOC(vloc_, 8 * (size_t)n_);
-    PSI_DALLOC(redA_, 8 * (size_t)nsub_);
-    PSI_DALLOC(redB_, 8 * (size_t)nsub_);
-    PSI_DALLOC(redC_, 8 * (size_t)nsub_);
-    PSI_DALLOC(jA_, 8 * (size_t)n_);
-    PSI_DALLOC(jB_, 8 * (size_t)n_);
-    PSI_DALLOC(dw_, sizeof(Words));
-#undef PSI_DALLOC
-    PSI_CUDA_TRY(cudaMallocHost((void **)&hw_, sizeof(Words)));
-
-    {
-        int r1 = dalloc((void **)&rev_off_, 4 * ((size_t)n_ + 1));
-        if (r1) return r1;
-        int r2 = dalloc((void **)&rev_src_, 4 * std::max<size_t>((size_t)m_, 1));
-        if (r2) return r2;
+    for (const auto &a : arrays) {
+        cudaError_t e = cudaMalloc(a.ptr, a.bytes ? a.bytes : 16);
+        if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        allocs_.push_back(*a.ptr);
     }
+    PSI_CUDA_TRY(cudaMallocHost((void **)&hw_, sizeof(Words)));
+    PSI_CUDA_TRY(cudaMemsetAsync(dw_, 0, sizeof(Words), stream_));
+    return PSI_OK;
+}
 
+// One game filling the arrays: upload, player lists, reverse CSR.
+int Solver::upload_game(const HostGame &g)
+{
+    set_extent(g.n);
+    m_ = g.m;
+    max_pri_ = g.max_pri;
     std::vector<int8_t> own8(g.owner.begin(), g.owner.end());
     std::vector<int32_t> plist;
     plist.reserve(n_);
@@ -119,6 +163,7 @@ int Solver::alloc(const HostGame &g, const psi_options &)
     np0_ = (int32_t)plist.size();
     for (int32_t v = 0; v < n_; v++)
         if (g.owner[v] == 1) plist.push_back(v);
+    np_ = n_;
     PSI_CUDA_TRY(cudaMemcpyAsync(plist_, plist.data(), 4 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
     PSI_CUDA_TRY(cudaMemcpyAsync(owner_, own8.data(), n_, cudaMemcpyHostToDevice, stream_));
     PSI_CUDA_TRY(cudaMemcpyAsync(pri_, g.priority.data(), 4 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
@@ -126,13 +171,11 @@ int Solver::alloc(const HostGame &g, const psi_options &)
     if (m_) PSI_CUDA_TRY(cudaMemcpyAsync(tgt_, g.targets.data(), 4 * (size_t)m_, cudaMemcpyHostToDevice, stream_));
     PSI_CUDA_TRY(cudaMemsetAsync(solved_, 0, n_, stream_));
     PSI_CUDA_TRY(cudaMemsetAsync(st_, 0, 4 * (size_t)n_, stream_));
-    PSI_CUDA_TRY(cudaMemsetAsync(dw_, 0, sizeof(Words), stream_));
     // reverse CSR on the device (distinct in-neighbours, increasing order)
     int64_t rev_m = 0;
     int ce = build_reverse_csr(stream_, n_, m_, off_, tgt_, rev_off_, rev_src_, &rev_m);
     if (ce) return fail(PSI_ERR_CUDA, std::string("reverse CSR: ") + cudaGetErrorString((cudaError_t)ce));
     PSI_CUDA_TRY(cudaStreamSynchronize(stream_));
-    game_ = nullptr;
     return PSI_OK;
 }
 
@@ -291,7 +334,7 @@ int Solver::mark_solved(int32_t player)
     if (!val_ready_) return fail(PSI_ERR_STATE, "mark_solved before compute_valuation");
     int rc = set_device();
     if (rc) return rc;
-    launch_mark_solved(stream_, &dw_->ucount, ulist_, player, st_, solved_);
+    launch_mark_solved(stream_, &dw_->ucount, ulist_, player, st_, solved_, gmask_ ? game_of_ : nullptr, gmask_);
     PSI_CUDA_TRY(cudaGetLastError());
     return PSI_OK;   // ordered on the stream before the next call
 }
@@ -304,9 +347,10 @@ int Solver::switch_strategy(int32_t player, int64_t *switched)
     if (rc) return rc;
     PSI_CUDA_TRY(cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_));
     phase_begin(PH_SWITCH);
-    const int32_t np = (player == 0) ? np0_ : n_ - np0_;
+    const int32_t np = (player == 0) ? np0_ : np_ - np0_;
     const int32_t *pl = plist_ + (player == 0 ? 0 : np0_);
-    launch_switch(stream_, np, pl, player, off_, tgt_, strat_, st_, node_, dw_->sw, game_of_, gcount_, &dw_->err);
+    launch_switch(stream_, np, pl, player, off_, tgt_, strat_, st_, node_, dw_->sw, game_of_, gcount_, gmask_,
+                  &dw_->err);
     phase_end(PH_SWITCH);
     rc = sync_and_check("switch_strategy");
     if (rc) return rc;
@@ -548,6 +592,173 @@ int Solver::solve_batch(int32_t *iters, int32_t *brs)
         iters[k] = st[k].y;
         if (!st[k].w) return fail(PSI_ERR_STATE, "batch loop ended with an unfinished game");
     }
+    return PSI_OK;
+}
+
+// ---- serving arena ------------------------------------------------------
+
+int Solver::init_arena(int32_t slots)
+{
+    set_extent(0);
+    m_ = 0;
+    max_pri_ = 0;
+    np0_ = np_ = 0;
+    const struct {
+        void **ptr;
+        size_t bytes;
+    } arrays[] = {{(void **)&game_of_, 4 * (size_t)cap_n_},
+                  {(void **)&gstate_, sizeof(int4) * (size_t)slots},
+                  {(void **)&gcount_, sizeof(unsigned long long) * (size_t)slots},
+                  {(void **)&gmask_, 4 * (size_t)slots}};
+    for (const auto &a : arrays) {
+        cudaError_t e = cudaMalloc(a.ptr, a.bytes);
+        if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        allocs_.push_back(*a.ptr);
+    }
+    games_ = slots;
+    arena_ = true;
+    PSI_CUDA_TRY(cudaMemsetAsync(solved_, 1, (size_t)cap_n_, stream_));          // every slot inert
+    PSI_CUDA_TRY(cudaMemsetAsync(game_of_, 0xff, 4 * (size_t)cap_n_, stream_));   // -1: in no game
+    PSI_CUDA_TRY(cudaMemsetAsync(st_, 0, 4 * (size_t)cap_n_, stream_));            // no finite depths
+    PSI_CUDA_TRY(cudaMemsetAsync(gstate_, 0, sizeof(int4) * (size_t)slots, stream_));
+    PSI_CUDA_TRY(cudaMemsetAsync(gcount_, 0, sizeof(unsigned long long) * (size_t)slots, stream_));
+    PSI_CUDA_TRY(cudaMemsetAsync(gmask_, 0, 4 * (size_t)slots, stream_));
+    PSI_CUDA_TRY(cudaStreamSynchronize(stream_));
+    strat_ready_ = true;
+    return PSI_OK;
+}
+
+// Places the games admitted in one step: one packed upload of their union,
+// one reverse-CSR build over it and one placement launch.
+int Solver::arena_add(const std::vector<const HostGame *> &gs, const std::vector<int32_t> &vb,
+                      const std::vector<int32_t> &eb, const std::vector<int32_t> &slot, int32_t extent)
+{
+    if (!arena_) return fail(PSI_ERR_STATE, "not an arena");
+    const int32_t K = (int32_t)gs.size();
+    if (K == 0) return PSI_OK;
+    if ((int32_t)vb.size() != K || (int32_t)eb.size() != K || (int32_t)slot.size() != K || extent > cap_n_)
+        return fail(PSI_ERR_INVALID, "arena placement lists disagree");
+    for (int32_t k = 0; k < K; k++) {
+        const HostGame &g = *gs[k];
+        if (slot[k] < 0 || slot[k] >= games_ || vb[k] < 0 || eb[k] < 0 || (int64_t)vb[k] + g.n + 1 > extent ||
+            (int64_t)eb[k] + g.m > cap_m_)
+            return fail(PSI_ERR_INVALID, "arena placement out of range");
+    }
+    HostGame u;
+    std::vector<int64_t> base;
+    int rc = pack_games(gs, u, base);
+    if (rc) return rc;
+    rc = set_device();
+    if (rc) return rc;
+    // per-game table: ub[K+1], vb[K], eb[K], slot[K]
+    std::vector<int32_t> table(4 * (size_t)K + 1);
+    for (int32_t k = 0; k <= K; k++) table[k] = (int32_t)base[k];
+    for (int32_t k = 0; k < K; k++) {
+        table[K + 1 + k] = vb[k];
+        table[2 * K + 1 + k] = eb[k];
+        table[3 * K + 1 + k] = slot[k];
+    }
+    const int64_t n = u.n, m = u.m;
+    int32_t *d_tab = nullptr, *u_owner = nullptr, *u_pri = nullptr, *u_off = nullptr, *u_tgt = nullptr,
+            *u_roff = nullptr, *u_rsrc = nullptr;
+    int32_t **bufs[] = {&d_tab, &u_owner, &u_pri, &u_off, &u_tgt, &u_roff, &u_rsrc};
+    const size_t sizes[] = {4 * table.size(),   4 * (size_t)n,       4 * (size_t)n,      4 * ((size_t)n + 1),
+                            4 * (size_t)m,      4 * ((size_t)n + 1), 4 * (size_t)m};
+    const void *src[] = {table.data(), u.owner.data(), u.priority.data(), u.offsets.data(), u.targets.data()};
+    cudaError_t e = cudaSuccess;
+    int64_t mr = 0;
+    int ce = 0;
+    for (int i = 0; i < 7 && e == cudaSuccess; i++) e = cudaMallocAsync((void **)bufs[i], sizes[i], stream_);
+    for (int i = 0; i < 5 && e == cudaSuccess; i++)
+        e = cudaMemcpyAsync(*bufs[i], src[i], sizes[i], cudaMemcpyHostToDevice, stream_);
+    if (e == cudaSuccess) ce = build_reverse_csr(stream_, (int32_t)n, m, u_off, u_tgt, u_roff, u_rsrc, &mr);
+    if (e == cudaSuccess && !ce) {
+        e = cudaMemsetAsync(&dw_->ucount, 0, sizeof(int32_t), stream_);   // the unreached list is stale
+        launch_arena_place(stream_, (int32_t)n, K, d_tab, d_tab + K + 1, d_tab + 2 * K + 1, d_tab + 3 * K + 1,
+                           u_owner, u_pri, u_off, u_tgt, u_roff, u_rsrc, owner_, pri_, off_, tgt_, rev_off_, rev_src_,
+                           strat_, st_, solved_, game_of_, gstate_, gcount_);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+    }
+    for (int i = 0; i < 7; i++)
+        if (*bufs[i]) cudaFreeAsync(*bufs[i], stream_);
+    if (ce) return fail(PSI_ERR_CUDA, std::string("reverse CSR: ") + cudaGetErrorString((cudaError_t)ce));
+    if (e != cudaSuccess) return fail(PSI_ERR_CUDA, std::string("arena_add: ") + cudaGetErrorString(e));
+    if (u.max_pri > max_pri_) max_pri_ = u.max_pri;
+    set_extent(extent);
+    return sync_and_check("arena_add");
+}
+
+int Solver::arena_remove(int32_t vb, int32_t count, int32_t slot, int32_t extent)
+{
+    if (!arena_) return fail(PSI_ERR_STATE, "not an arena");
+    if (slot < 0 || slot >= games_ || vb < 0 || (int64_t)vb + count > cap_n_)
+        return fail(PSI_ERR_INVALID, "arena range out of range");
+    int rc = set_device();
+    if (rc) return rc;
+    launch_arena_clear(stream_, vb, count, solved_, game_of_, st_);
+    PSI_CUDA_TRY(cudaMemsetAsync(gstate_ + slot, 0, sizeof(int4), stream_));
+    PSI_CUDA_TRY(cudaMemsetAsync(&dw_->ucount, 0, sizeof(int32_t), stream_));
+    set_extent(extent);
+    return sync_and_check("arena_remove");
+}
+
+// Player lists of the vertices that belong to games (Even's first).
+int Solver::arena_rebuild_lists()
+{
+    int rc = set_device();
+    if (rc) return rc;
+    PSI_CUDA_TRY(cudaMemsetAsync(&dw_->sinkcount, 0, sizeof(int32_t), stream_));
+    launch_build_plist(stream_, n_, 0, owner_, game_of_, plist_, &dw_->sinkcount);
+    rc = sync_and_check("arena_rebuild_lists");
+    if (rc) return rc;
+    np0_ = hw_->sinkcount;
+    launch_build_plist(stream_, n_, 1, owner_, game_of_, plist_, &dw_->sinkcount);   // appends after Even's
+    rc = sync_and_check("arena_rebuild_lists");
+    if (rc) return rc;
+    np_ = hw_->sinkcount;
+    return PSI_OK;
+}
+
+// One solve_si step (main.cpp:20-55) of every resident game, each by its own
+// state machine (launch_serve_account): evaluate all, switch Odd in all, then
+// mark_solved(Even) and switch Even only in the games whose Odd made no
+// strict improvement in this step.
+int Solver::arena_step(bool reset, std::vector<int32_t> &done, std::vector<int32_t> &iters,
+                       std::vector<int32_t> &brs)
+{
+    done.clear();
+    iters.clear();
+    brs.clear();
+    if (!arena_) return fail(PSI_ERR_STATE, "not an arena");
+    if (n_ == 0 || np_ == 0) return PSI_OK;
+    int rc = compute_valuation();
+    if (rc) return rc;
+    launch_serve_account(stream_, games_, 0, gstate_, gcount_, gmask_);
+    int32_t *mask = gmask_;
+    gmask_ = nullptr;                       // Odd's step: every resident game
+    rc = mark_solved(1);
+    int64_t sw = 0;
+    if (!rc) rc = switch_strategy(1, &sw);
+    gmask_ = mask;
+    if (rc) return rc;
+    launch_serve_account(stream_, games_, 1, gstate_, gcount_, gmask_);
+    rc = mark_solved(0);                    // Even's step: games with gmask set
+    if (!rc) rc = switch_strategy(0, &sw);
+    if (rc) return rc;
+    if (reset)
+        launch_serve_reset_odd(stream_, np_ - np0_, plist_ + np0_, game_of_, gmask_, gcount_, off_, tgt_, strat_);
+    launch_serve_account(stream_, games_, 2, gstate_, gcount_, gmask_);
+    std::vector<int4> st((size_t)games_);
+    PSI_CUDA_TRY(cudaMemcpyAsync(st.data(), gstate_, sizeof(int4) * (size_t)games_, cudaMemcpyDeviceToHost, stream_));
+    rc = sync_and_check("arena_step");
+    if (rc) return rc;
+    for (int32_t k = 0; k < games_; k++)
+        if ((st[k].z & 1) && (st[k].z & 2)) {
+            done.push_back(k);
+            iters.push_back(st[k].y);
+            brs.push_back(st[k].x);
+        }
     return PSI_OK;
 }
 

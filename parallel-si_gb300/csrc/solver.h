@@ -31,6 +31,10 @@ struct SolverTimes {
 class Solver {
 public:
     static int create(const HostGame &g, const psi_options &opt, Solver **out);
+    // An empty arena for served games (serve.cpp): up to max_vertices vertex
+    // slots (each game takes n+1), max_edges edges, `slots` games at a time.
+    static int create_arena(int64_t max_vertices, int64_t max_edges, int32_t slots, const psi_options &opt,
+                            Solver **out);
     ~Solver();
 
     // The StrategyImprovement interface (si.h:6-16).
@@ -71,9 +75,26 @@ public:
     int solve_batch(int32_t *iters, int32_t *brs);
     int32_t batch_games() const { return games_; }
 
+    // Arena operations (serve.cpp).  A game occupies vertices [vb, vb+n] (vb+n
+    // is an inert sentinel) and edges [eb, eb+m); `extent` is the new number of
+    // vertex slots in use (one past the highest occupied one).  arena_add
+    // places several games at once (game k at vb[k], eb[k] in slot[k]).
+    int arena_add(const std::vector<const HostGame *> &gs, const std::vector<int32_t> &vb,
+                  const std::vector<int32_t> &eb, const std::vector<int32_t> &slot, int32_t extent);
+    int arena_remove(int32_t vb, int32_t count, int32_t slot, int32_t extent);
+    int arena_rebuild_lists();
+    // One solve_si step of every resident game (its reset variant when `reset`);
+    // `done` receives the slots that finished in this step with their
+    // (iterations, evaluations).
+    int arena_step(bool reset, std::vector<int32_t> &done, std::vector<int32_t> &iters, std::vector<int32_t> &brs);
+    int32_t arena_extent() const { return n_; }
+
 private:
     Solver() = default;
-    int alloc(const HostGame &g, const psi_options &opt);
+    int alloc_arrays(int64_t cap_n, int64_t cap_m);
+    int upload_game(const HostGame &g);
+    int init_arena(int32_t slots);
+    void set_extent(int32_t n);
     int sync_and_check(const char *what);
     int get_range(const int32_t *src, int64_t v0, int64_t count, int32_t *out);
     int set_device();
@@ -91,10 +112,10 @@ private:
     void phase_end(Phase p);
     int collect_phases();
     SolverTimes times_;
-    const HostGame *game_ = nullptr;
 
     int32_t n_ = 0, max_pri_ = 0, nsub_ = 0, stride_ = 64;
-    int64_t m_ = 0, L_ = 0;
+    int64_t m_ = 0, L_ = 0, cap_n_ = 0, cap_m_ = 0;
+    int32_t np_ = 0;   // entries in plist_ (Even's np0_ first)
     bool strat_ready_ = false, val_ready_ = false;
     int last_unreached_ = 0;
 
@@ -102,11 +123,13 @@ private:
     int8_t *owner_ = nullptr;
     int32_t *pri_ = nullptr, *off_ = nullptr, *tgt_ = nullptr, *plist_ = nullptr;
     int32_t np0_ = 0;
-    // batch partition (games_ == 0 for a single game)
+    // batch partition or arena slots (games_ == 0 for a single game)
     int32_t games_ = 0;
+    bool arena_ = false;
     int32_t *game_of_ = nullptr;
     int4 *gstate_ = nullptr;
     unsigned long long *gcount_ = nullptr;
+    int32_t *gmask_ = nullptr;   // when set, switch/mark_solved act only on games whose entry is non-zero
     // state
     int32_t *strat_ = nullptr, *st_ = nullptr;
     uint8_t *solved_ = nullptr;

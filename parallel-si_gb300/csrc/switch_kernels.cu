@@ -132,7 +132,8 @@ __device__ __forceinline__ int2 summary_of(const PathNode *__restrict__ node, in
 // stats[0] += compared edges, stats[1] += parent/priority loads of tier-3
 // walks, stats[2] += vertices whose strategy changed, stats[3] += strict
 // improvements.  For a batch of games (game_of != nullptr) the strict
-// improvements are also added to gcount[game of the vertex].
+// improvements are also added to gcount[game of the vertex]; with gmask only
+// vertices of games whose mask is set switch.
 __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__restrict__ plist, int32_t player,
                                                    const int32_t *__restrict__ off, const int32_t *__restrict__ tgt,
                                                    int32_t *__restrict__ strat, const int32_t *__restrict__ st,
@@ -140,12 +141,14 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
                                                    unsigned long long *__restrict__ stats,
                                                    const int32_t *__restrict__ game_of,
                                                    unsigned long long *__restrict__ gcount,
+                                                   const int32_t *__restrict__ gmask,
                                                    uint32_t *__restrict__ err)
 {
     int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     int32_t n_edges = 0, n_loads = 0, moves = 0;
-    if (i < np) {
-        int32_t v = plist[i];
+    int32_t v = (i < np) ? plist[i] : -1;
+    if (v >= 0 && gmask && !gmask[game_of[v]]) v = -1;
+    if (v >= 0) {
         int32_t cur = strat[v];
         int32_t scur = (cur >= 0) ? st[cur] : 0;
         int2 rcur = summary_of(node, cur, scur);
@@ -257,12 +260,13 @@ __global__ void k_materialize(int32_t v0, int32_t count, int32_t d, const int32_
 
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player, const int32_t *off,
                    const int32_t *tgt, int32_t *strat, const int32_t *st, const PathNode *node,
-                   unsigned long long *stats, const int32_t *game_of, unsigned long long *gcount, uint32_t *err)
+                   unsigned long long *stats, const int32_t *game_of, unsigned long long *gcount,
+                   const int32_t *gmask, uint32_t *err)
 {
     if (np <= 0) return;
     count_launch();
     k_switch<<<grid_for(np), kBlock, 0, s>>>(np, plist, player, off, tgt, strat, st, node, stats, game_of,
-                                             gcount, err);
+                                             gcount, gmask, err);
 }
 
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state, unsigned long long *gcount)

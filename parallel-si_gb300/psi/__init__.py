@@ -21,7 +21,7 @@ def launch_count() -> int:
     """Kernel launches issued by the native library in this process."""
     return int(lib.psi_launch_count())
 
-__all__ = ["Game", "GPUList", "Batch", "PsiError", "Options", "solve_si", "batch_sizes", "default_options", "version"]
+__all__ = ["Game", "GPUList", "Batch", "Server", "PsiError", "Options", "solve_si", "batch_sizes", "default_options", "version"]
 
 
 def version() -> str:
@@ -308,6 +308,87 @@ class Batch:
     def close(self) -> None:
         if self._h:
             lib.psi_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching solver (psi_server_*): games submitted at any time
+    join the resident set at the next step; each finishes with the results of
+    its own solo solve."""
+
+    QUEUED, RESIDENT, FINISHED = 0, 1, 2
+
+    def __init__(self, max_vertices: int, max_edges: int, max_games: int, reset: bool = False,
+                 options: Optional[Options] = None, **kw):
+        o = options if options is not None else default_options(**kw)
+        self._h = C.c_void_p()
+        self._n = {}
+        check(lib.psi_server_create(max_vertices, max_edges, max_games, int(bool(reset)), C.byref(o),
+                                    C.byref(self._h)))
+
+    def submit(self, game: "Game") -> int:
+        t = C.c_int64()
+        check(lib.psi_server_submit(self._h, game._h, C.byref(t)))
+        self._n[t.value] = game.n
+        return t.value
+
+    def step(self) -> int:
+        """One serving step; returns how many games finished in it."""
+        k = C.c_int32()
+        check(lib.psi_server_step(self._h, C.byref(k)))
+        return k.value
+
+    def finished(self) -> np.ndarray:
+        """Tickets of the games that finished in the last step."""
+        k = C.c_int32()
+        check(lib.psi_server_finished(self._h, None, 0, C.byref(k)))
+        out = np.empty(k.value, np.int64)
+        if k.value:
+            check(lib.psi_server_finished(self._h, ptr(out), k.value, C.byref(k)))
+        return out
+
+    def status(self, ticket: int):
+        """(state, iter_count, br_count)."""
+        st, it, br = C.c_int32(), C.c_int32(), C.c_int32()
+        check(lib.psi_server_status(self._h, ticket, C.byref(st), C.byref(it), C.byref(br)))
+        return st.value, it.value, br.value
+
+    def take(self, ticket: int):
+        """(strategy, infinite) of a finished request, in its own vertex ids."""
+        n = self._n[ticket]
+        strat = np.empty(n, np.int32)
+        inf = np.empty(n, np.int32)
+        check(lib.psi_server_take(self._h, ticket, ptr(strat), ptr(inf)))
+        del self._n[ticket]
+        return strat, inf
+
+    def info(self):
+        """(resident games, queued games, vertex slots used, edge slots used)."""
+        r, q = C.c_int32(), C.c_int32()
+        v, e = C.c_int64(), C.c_int64()
+        check(lib.psi_server_info(self._h, C.byref(r), C.byref(q), C.byref(v), C.byref(e)))
+        return r.value, q.value, v.value, e.value
+
+    def drain(self, max_steps: int = 1 << 30) -> int:
+        """Steps until nothing is resident or queued; returns the steps taken."""
+        steps = 0
+        while steps < max_steps:
+            r, q, _, _ = self.info()
+            if r == 0 and q == 0:
+                break
+            self.step()
+            steps += 1
+        return steps
+
+    def close(self) -> None:
+        if self._h:
+            lib.psi_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

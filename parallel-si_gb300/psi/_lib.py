@@ -102,6 +102,14 @@ _SIGS = {
     "psi_batch_solve": ([_vp, _vp, _vp], C.c_int),
     "psi_batch_get_strategy": ([_vp, C.c_int32, _vp], C.c_int),
     "psi_batch_get_winning": ([_vp, C.c_int32, C.c_int32, _vp, C.c_int64, _i64p], C.c_int),
+    "psi_server_create": ([C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Options), _pp], C.c_int),
+    "psi_server_destroy": ([_vp], None),
+    "psi_server_submit": ([_vp, _vp, _i64p], C.c_int),
+    "psi_server_step": ([_vp, _i32p], C.c_int),
+    "psi_server_finished": ([_vp, _vp, C.c_int32, _i32p], C.c_int),
+    "psi_server_status": ([_vp, C.c_int64, _i32p, _i32p, _i32p], C.c_int),
+    "psi_server_take": ([_vp, C.c_int64, _vp, _vp], C.c_int),
+    "psi_server_info": ([_vp, _i32p, _i32p, _i64p, _i64p], C.c_int),
 }
 
 COUNTERS = ("evals", "switches", "sw_edges", "sw_loads", "sw_changed", "unreached", "jump_rounds")
