@@ -26,6 +26,8 @@ import subprocess
 import sys
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "parallel-si_gb300")
 for _p in (ROOT, PKG):
@@ -255,8 +257,6 @@ def run_reference(args, rank, world):
 
 
 def run_gb300(args, rank, world, local):
-    import numpy as np
-
     import psi
 
     dist = Dist(world, local)
@@ -358,40 +358,53 @@ def run_batch(args, rank, world, local):
     U[0,n_i), solved together (psi_batch_solve) against the same kind of games
     solved one at a time on the same GPU (every `--solo-stride`-th game, each
     with its own resident solver).  Both rates are games per second of
-    synchronous host calls (wall clock)."""
+    synchronous host calls (wall clock).  With N ranks the games are split by
+    footprint (psi.shard_games; game i keeps its seed, so the union is the
+    1-GPU workload) and each rank solves its share; the time is the maximum
+    over ranks."""
     import psi
 
+    dist = Dist(world, local)
     sizes = psi.batch_sizes(args.batch_games, 100, 200000, args.seed)
-    games = [psi.Game.random(int(n), 2, 8, int(n), args.seed * 100003 + i) for i, n in enumerate(sizes)]
+    mine = psi.shard_games(sizes.astype(np.int64) + 1, world)[rank]
+    games = [psi.Game.random(int(sizes[i]), 2, 8, int(sizes[i]), args.seed * 100003 + int(i)) for i in mine]
     batch = psi.Batch(games, device=local)
     for _ in range(args.warmup):
         batch.solve()
+    dist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         it, br = batch.solve()
-    t_batch = (time.perf_counter() - t0) / args.steps
+    dist.barrier()
+    t_batch = dist.max((time.perf_counter() - t0) / args.steps)
     solo_idx = list(range(0, len(games), args.solo_stride))
     solvers = [psi.GPUList(games[k], device=local) for k in solo_idx]
     for s in solvers[:8]:
         s.solve()
     t0 = time.perf_counter()
     solo_res = [s.solve() for s in solvers]
-    t_solo = time.perf_counter() - t0
-    exact = all(tuple(solo_res[j]) == (int(it[k]), int(br[k])) for j, k in enumerate(solo_idx))
+    t_solo = dist.max(time.perf_counter() - t0)
+    n_solo = dist.sum(len(solo_idx))
+    exact = dist.sum(0 if all(tuple(solo_res[j]) == (int(it[k]), int(br[k])) for j, k in enumerate(solo_idx))
+                     else 1) == 0
     _, nv, ne = batch.info()
+    nv, ne = int(dist.sum(nv)), int(dist.sum(ne))
+    max_it, max_br = int(dist.max(int(it.max()))), int(dist.max(int(br.max())))
     line = {
-        "metric": "games/s (batched)", "value": len(games) / t_batch, "unit": "games/s", "n_gpus": world,
+        "metric": "games/s (batched)", "value": len(sizes) / t_batch, "unit": "games/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t_batch, "higher_is_better": True,
-        "dtype": "int32", "data": "synthetic",
-        "config": {"workload": f"{len(games)} random games, n_i log-uniform in [100,200000], out-degree U[2,8], "
+        "scaling": "strong", "dtype": "int32", "data": "synthetic",
+        "config": {"workload": f"{len(sizes)} random games, n_i log-uniform in [100,200000], out-degree U[2,8], "
                                f"priority U[0,n_i)", "total_vertices": nv, "total_edges": ne,
-                   "max_iters": int(it.max()), "max_brs": int(br.max())},
-        "one_by_one": {"games": len(solo_idx), "games_per_s": len(solo_idx) / t_solo},
-        "speedup_vs_one_by_one": (len(games) / t_batch) / (len(solo_idx) / t_solo),
+                   "max_iters": max_it, "max_brs": max_br,
+                   "parallelism": f"games sharded by footprint over {world} rank(s)"},
+        "one_by_one": {"games": int(n_solo), "games_per_s": n_solo / t_solo},
+        "speedup_vs_one_by_one": (len(sizes) / t_batch) / (n_solo / t_solo),
         "counts_match_solo": exact,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
+    dist.close()
     return 0
 
 
@@ -399,8 +412,6 @@ def serve_once(srv, games, arrivals):
     """Feeds `games` to the server at the given arrival times (seconds from
     the start; wall clock) and steps it until all finished.  Returns (elapsed
     s, per-game latency s, per-game (iters, brs), steps, mean resident games)."""
-    import numpy as np
-
     order = np.argsort(arrivals, kind="stable")
     lat = np.zeros(len(games))
     counts = [None] * len(games)
@@ -434,57 +445,69 @@ def serve_once(srv, games, arrivals):
 
 def run_serve(args, rank, world, local):
     """Serving workload (not the headline line): `--serve-games` random games
-    (sizes log-uniform in [100, 200000], out-degree U[2,8], priority U[0,n_i))
-    arrive at one continuous-batching server (psi_server_*) whose arena holds
-    `--arena-vertices` vertex slots.  First all arrive at once (saturated:
-    the throughput ceiling); then they arrive as a Poisson process at fixed
-    fractions of that ceiling.  Latency = arrival to the end of the step in
-    which the game finished (wall clock); every game's iteration and
-    evaluation counts are checked against solo solves of a stride sample."""
-    import numpy as np
+    (sizes log-uniform in [--serve-lo, --serve-hi], default [10^3, 2*10^6],
+    out-degree U[2,8], priority U[0,n_i)) arrive at one continuous-batching
+    server (psi_server_*) whose arena holds `--arena-vertices` vertex slots.
+    First all arrive at once (saturated: the throughput ceiling); then they
+    arrive as a Poisson process at fixed fractions of that ceiling.  Latency =
+    arrival to the end of the step in which the game finished (wall clock);
+    every game's iteration and evaluation counts are checked against solo
+    solves of a stride sample.  With N ranks each runs its own server on its
+    footprint share of the games (psi.shard_games) and its share of the
+    arrival rate; throughputs add up, latency percentiles are the worst
+    rank's."""
     import psi
 
-    sizes = psi.batch_sizes(args.serve_games, 100, 200000, args.seed)
-    games = [psi.Game.random(int(n), 2, 8, int(n), args.seed * 100003 + i) for i, n in enumerate(sizes)]
+    dist = Dist(world, local)
+    sizes = psi.batch_sizes(args.serve_games, args.serve_lo, args.serve_hi, args.seed)
+    mine = psi.shard_games(sizes.astype(np.int64) + 1, world)[rank]
+    games = [psi.Game.random(int(sizes[i]), 2, 8, int(sizes[i]), args.seed * 100003 + int(i)) for i in mine]
     srv = psi.Server(args.arena_vertices, 8 * args.arena_vertices, args.serve_slots, device=local)
-    warm = games[: max(8, len(games) // 16)]
+    warm = games[: max(4, len(games) // 16)]
     for _ in range(args.warmup):
         serve_once(srv, warm, np.zeros(len(warm)))
+    dist.barrier()
     el, lat, counts, steps, mres = serve_once(srv, games, np.zeros(len(games)))
-    sat = len(games) / el
+    el = dist.max(el)
+    sat = len(sizes) / el
     loads = []
-    rng = np.random.default_rng(args.seed)
+    rng = np.random.default_rng(args.seed * 7919 + rank)
     for frac in (0.5, 0.8):
-        rate = frac * sat
+        rate = frac * sat / world     # this rank's share of the offered load
         arrivals = np.cumsum(rng.exponential(1.0 / rate, len(games)))
+        dist.barrier()
         el2, lat2, counts2, steps2, mres2 = serve_once(srv, games, arrivals)
         assert counts2 == counts
-        loads.append({"offered_games_per_s": rate, "games_per_s": len(games) / el2,
-                      "p50_ms": 1000 * float(np.percentile(lat2, 50)),
-                      "p99_ms": 1000 * float(np.percentile(lat2, 99)), "steps": steps2,
-                      "mean_resident_games": mres2})
+        loads.append({"offered_games_per_s": rate * world, "games_per_s": dist.sum(len(games) / el2),
+                      "p50_ms": dist.max(1000 * float(np.percentile(lat2, 50))),
+                      "p99_ms": dist.max(1000 * float(np.percentile(lat2, 99))), "steps": int(dist.max(steps2)),
+                      "mean_resident_games": dist.sum(mres2)})
     solo_idx = list(range(0, len(games), args.solo_stride))
-    exact = True
+    bad = 0
     for k in solo_idx:
         s = psi.GPUList(games[k], device=local)
-        exact = exact and tuple(s.solve()) == tuple(counts[k])
+        bad += tuple(s.solve()) != tuple(counts[k])
         s.close()
+    exact = dist.sum(bad) == 0
     line = {
         "metric": "games/s (served, saturated)", "value": sat, "unit": "games/s", "n_gpus": world,
         "steps": 1, "warmup": args.warmup, "ms_per_step": 1000 * el, "higher_is_better": True,
-        "dtype": "int32", "data": "synthetic",
-        "config": {"workload": f"{len(games)} random games served, n_i log-uniform in [100,200000], out-degree "
-                               f"U[2,8], priority U[0,n_i)", "arena_vertices": args.arena_vertices,
+        "scaling": "strong", "dtype": "int32", "data": "synthetic",
+        "config": {"workload": f"{len(sizes)} random games served, n_i log-uniform in [{args.serve_lo},"
+                               f"{args.serve_hi}], out-degree U[2,8], priority U[0,n_i)",
+                   "arena_vertices": args.arena_vertices,
                    "arena_edges": 8 * args.arena_vertices, "max_games": args.serve_slots,
-                   "total_vertices": int(sum(sizes))},
-        "saturated": {"games_per_s": sat, "p50_ms": 1000 * float(np.percentile(lat, 50)),
-                      "p99_ms": 1000 * float(np.percentile(lat, 99)), "steps": steps,
-                      "mean_resident_games": mres},
+                   "total_vertices": int(sizes.astype(np.int64).sum()),
+                   "parallelism": f"games sharded by footprint over {world} rank(s), one server each"},
+        "saturated": {"games_per_s": sat, "p50_ms": dist.max(1000 * float(np.percentile(lat, 50))),
+                      "p99_ms": dist.max(1000 * float(np.percentile(lat, 99))), "steps": int(dist.max(steps)),
+                      "mean_resident_games": dist.sum(mres)},
         "poisson": loads,
-        "counts_match_solo": exact, "solo_checked": len(solo_idx),
+        "counts_match_solo": exact, "solo_checked": int(dist.sum(len(solo_idx))),
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
+    dist.close()
     return 0
 
 
@@ -503,9 +526,11 @@ def main():
                          "serve: the same kind of games arriving at a continuous-batching server")
     ap.add_argument("--batch-games", type=int, default=4096)
     ap.add_argument("--solo-stride", type=int, default=16)
-    ap.add_argument("--serve-games", type=int, default=2048)
-    ap.add_argument("--serve-slots", type=int, default=4096)
-    ap.add_argument("--arena-vertices", type=int, default=1 << 24)
+    ap.add_argument("--serve-games", type=int, default=256)
+    ap.add_argument("--serve-lo", type=int, default=1000)
+    ap.add_argument("--serve-hi", type=int, default=2000000)
+    ap.add_argument("--serve-slots", type=int, default=1024)
+    ap.add_argument("--arena-vertices", type=int, default=1 << 25)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")

@@ -21,7 +21,7 @@ def launch_count() -> int:
     """Kernel launches issued by the native library in this process."""
     return int(lib.psi_launch_count())
 
-__all__ = ["Game", "GPUList", "Batch", "Server", "PsiError", "Options", "solve_si", "batch_sizes", "default_options", "version"]
+__all__ = ["Game", "GPUList", "Batch", "Server", "PsiError", "Options", "solve_si", "batch_sizes", "shard_games", "default_options", "version"]
 
 
 def version() -> str:
@@ -264,6 +264,26 @@ def batch_sizes(count: int, n_lo: int, n_hi: int, seed: int = 1) -> np.ndarray:
     out = np.empty(count, np.int32)
     check(lib.psi_generate_batch_sizes(count, n_lo, n_hi, C.c_uint64(seed), ptr(out)))
     return out
+
+
+def shard_games(footprints, world: int):
+    """Footprint-balanced partition of independent games over `world` ranks
+    (one GPU each): games in decreasing footprint order, each to the rank
+    with the smallest total so far (ties: the lower rank, then the lower game
+    index first).  Deterministic; returns one increasing index array per
+    rank.  Games never interact, so the ranks need no collective beyond
+    gathering results."""
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    fp = np.asarray(footprints, dtype=np.int64)
+    order = sorted(range(len(fp)), key=lambda k: (-int(fp[k]), k))
+    load = [0] * world
+    parts = [[] for _ in range(world)]
+    for k in order:
+        r = min(range(world), key=lambda j: (load[j], j))
+        load[r] += int(fp[k])
+        parts[r].append(k)
+    return [np.array(sorted(p), dtype=np.int64) for p in parts]
 
 
 class Batch:
