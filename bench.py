@@ -311,22 +311,21 @@ def run_gb300(args, rank, world, local):
             lr[p] = {"ms_per_call": pm / pc, "GBps": b / (pm / pc / 1e3) / 1e9, "frac": b / (pm / pc / 1e3) / 1e9 / peak}
 
     # end to end through the C ABI from host buffers
-    csr = [np.ascontiguousarray(a) for a in game.csr()]
-    h2d = game.n * 1 + 4 * game.n + 4 * (game.n + 1) + 4 * game.m
-    d2h = 8 * game.n
+    csr = [np.ascontiguousarray(a, dtype=np.int32) for a in game.csr()]
+    h2d = sum(int(a.nbytes) for a in csr)        # owner, priority, offsets, targets (int32)
     del solver
     dist.barrier()
     t0 = time.perf_counter()
     e2e_iters = 0
+    d2h = 0
     for _ in range(args.steps):
-        g2 = psi.Game.from_csr(*csr)
-        s2 = psi.GPUList(g2, device=local, sublist_len=args.sublist_len)
+        s2 = psi.GPUList.from_csr(*csr, device=local, sublist_len=args.sublist_len)
         it, _ = s2.solve()
-        s2.get_winning(0)
-        s2.get_strategy()
+        w0 = s2.get_winning(0)
+        strat = s2.get_strategy()
         s2.close()
-        g2.close()
         e2e_iters += it
+        d2h = 4 * (len(w0) + 1) + int(strat.nbytes)   # winning set and its size, strategy
     e2e_s = time.perf_counter() - t0
     e2e_max = dist.max(e2e_s)
     e2e_iters_all = dist.sum(e2e_iters)

@@ -182,7 +182,29 @@ int psi_solver_create(const psi_game *g, const psi_options *opt, psi_solver **ou
     psi_options_default(&o);
     if (opt) o = *opt;
     psi::Solver *s = nullptr;
-    int rc = psi::Solver::create(g->g, o, &s);
+    int rc = psi::Solver::create(psi::view_of(g->g), o, &s);
+    if (rc) return rc;
+    psi_solver *h = new psi_solver();
+    h->s = s;
+    *out = h;
+    return PSI_OK;
+    PSI_GUARD_END
+}
+
+int psi_solver_create_csr(int32_t n, const int32_t *owner, const int32_t *priority, const int32_t *offsets,
+                          const int32_t *targets, const psi_options *opt, psi_solver **out)
+{
+    if (!out || !owner || !priority || !offsets || !targets) return psi::fail(PSI_ERR_INVALID, "null argument");
+    *out = nullptr;
+    PSI_GUARD_BEGIN
+    psi::CsrView v;
+    int rc = psi::make_view(n, owner, priority, offsets, targets, v);
+    if (rc) return rc;
+    psi_options o;
+    psi_options_default(&o);
+    if (opt) o = *opt;
+    psi::Solver *s = nullptr;
+    rc = psi::Solver::create(v, o, &s);
     if (rc) return rc;
     psi_solver *h = new psi_solver();
     h->s = s;
@@ -220,14 +242,14 @@ int psi_get_winning(psi_solver *s, int32_t player, int32_t *out, int64_t cap, in
 {
     if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null solver");
     PSI_GUARD_BEGIN
-    std::vector<int32_t> w;
-    int rc = s->s->get_winning(player, w);
+    int64_t total = 0;
+    int rc = s->s->winning_ids(player, &total);
     if (rc) return rc;
-    if (out) {
-        int64_t k = (int64_t)w.size() < cap ? (int64_t)w.size() : cap;
-        if (k > 0) std::memcpy(out, w.data(), 4 * (size_t)k);
+    if (out && cap > 0) {
+        rc = s->s->copy_winning(out, total < cap ? total : cap);
+        if (rc) return rc;
     }
-    if (count) *count = (int64_t)w.size();
+    if (count) *count = total;
     return PSI_OK;
     PSI_GUARD_END
 }
@@ -361,7 +383,7 @@ int psi_batch_create(const psi_game *const *games, int32_t count, const psi_opti
     psi_options_default(&o);
     if (opt) o = *opt;
     psi::Solver *s = nullptr;
-    rc = psi::Solver::create(u, o, &s);
+    rc = psi::Solver::create(psi::view_of(u), o, &s);
     if (rc) return rc;
     rc = s->enable_batch(base);
     if (rc) {

@@ -33,6 +33,17 @@ struct __align__(16) PathNode {
 };
 constexpr int32_t RM_UNKNOWN = INT32_MIN;
 
+// Comparison key of a vertex after an evaluation (8 bytes, what the switch
+// step gathers per compared edge): (rmax, rcnt) of its root path if its
+// valuation is finite (rmax >= 0: the path holds the vertex itself), or
+// (KEY_NEG_INF / KEY_POS_INF, 0).  The sink's key is (-1, 0).
+constexpr int32_t KEY_NEG_INF = -2;
+constexpr int32_t KEY_POS_INF = -3;
+__host__ __device__ __forceinline__ int32_t key_infinite(int32_t kx)
+{
+    return kx == KEY_POS_INF ? 1 : (kx == KEY_NEG_INF ? -1 : 0);
+}
+
 // Tour node ids (an Euler tour of the strategy forest, two nodes per vertex):
 // node 2v is v's "down" node (leaving v's subtree toward the sink), 2v+1 its
 // "up" node (entering it); 2n / 2n+1 are the sink's down / up nodes.  The list

@@ -9,12 +9,16 @@
 // priorities and successor ids outside [0, n).  Files ending in .gz are read
 // through zlib when the library was built with it (the reference uses boost
 // iostreams for .gz and .bz2, main.cpp:140-151; .bz2 is not supported).
+#include <algorithm>
+#include <atomic>
 #include <cerrno>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <climits>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #ifdef PSI_HAVE_ZLIB
@@ -86,7 +90,7 @@ int parse_gm(const char *text, int64_t len, HostGame &g)
     const char *nl = (const char *)memchr(p, '\n', end - p);
     p = nl ? nl + 1 : end;
     line_no = 1;
-    std::vector<int32_t> offsets;
+    IVec offsets;
     offsets.push_back(0);
     while (p < end) {
         nl = (const char *)memchr(p, '\n', end - p);
@@ -206,36 +210,117 @@ int write_gm(const HostGame &g, const char *path)
     return ok ? PSI_OK : fail(PSI_ERR_IO, std::string("write error: ") + path);
 }
 
+void parallel_chunks(int64_t count, const std::function<void(int64_t, int64_t)> &f)
+{
+    int64_t threads = (int64_t)std::thread::hardware_concurrency();
+    threads = std::max<int64_t>(1, std::min<int64_t>(threads, 16));
+    threads = std::min<int64_t>(threads, count / (1 << 20) + 1);
+    if (threads <= 1) {
+        if (count > 0) f(0, count);
+        return;
+    }
+    std::vector<std::thread> pool;
+    for (int64_t t = 0; t < threads; t++) {
+        int64_t lo = count * t / threads, hi = count * (t + 1) / threads;
+        pool.emplace_back([&f, lo, hi] { f(lo, hi); });
+    }
+    for (auto &th : pool) th.join();
+}
+
+namespace {
+
+// First failing vertex check (in vertex order) over [lo, hi): 1 bad player,
+// 2 negative priority, 3 no successor; returns (vertex, kind) or (-1, 0).
+std::pair<int64_t, int> first_bad_vertex(int64_t lo, int64_t hi, const int32_t *owner, const int32_t *priority,
+                                         const int32_t *offsets)
+{
+    for (int64_t v = lo; v < hi; v++) {
+        if (owner[v] != 0 && owner[v] != 1) return {v, 1};
+        if (priority[v] < 0) return {v, 2};
+        if (offsets[v + 1] <= offsets[v]) return {v, 3};
+    }
+    return {-1, 0};
+}
+
+}  // namespace
+
 int validate_csr(int32_t n, const int32_t *owner, const int32_t *priority, const int32_t *offsets,
                  const int32_t *targets)
 {
     if (n <= 0) return fail(PSI_ERR_INVALID, "game has no vertices");
     if (offsets[0] != 0) return fail(PSI_ERR_INVALID, "offsets[0] must be 0");
-    for (int32_t v = 0; v < n; v++) {
-        if (owner[v] != 0 && owner[v] != 1) return fail(PSI_ERR_INVALID, "invalid player at vertex " + std::to_string(v));
-        if (priority[v] < 0) return fail(PSI_ERR_INVALID, "negative priority at vertex " + std::to_string(v));
-        if (offsets[v + 1] <= offsets[v]) return fail(PSI_ERR_INVALID, "vertex " + std::to_string(v) + " has no successor");
+    // vertex checks per chunk; the lowest failing vertex decides the message
+    std::mutex mu;
+    std::pair<int64_t, int> worst{-1, 0};
+    parallel_chunks(n, [&](int64_t lo, int64_t hi) {
+        auto b = first_bad_vertex(lo, hi, owner, priority, offsets);
+        if (b.first < 0) return;
+        std::lock_guard<std::mutex> lk(mu);
+        if (worst.first < 0 || b.first < worst.first) worst = b;
+    });
+    if (worst.first >= 0) {
+        std::string v = std::to_string(worst.first);
+        if (worst.second == 1) return fail(PSI_ERR_INVALID, "invalid player at vertex " + v);
+        if (worst.second == 2) return fail(PSI_ERR_INVALID, "negative priority at vertex " + v);
+        return fail(PSI_ERR_INVALID, "vertex " + v + " has no successor");
     }
-    int64_t m = offsets[n];
-    for (int64_t e = 0; e < m; e++)
-        if (targets[e] < 0 || targets[e] >= n) return fail(PSI_ERR_INVALID, "successor out of range");
+    std::atomic<bool> bad_edge{false};
+    parallel_chunks(offsets[n], [&](int64_t lo, int64_t hi) {
+        for (int64_t e = lo; e < hi; e++)
+            if (targets[e] < 0 || targets[e] >= n) {
+                bad_edge = true;
+                return;
+            }
+    });
+    if (bad_edge) return fail(PSI_ERR_INVALID, "successor out of range");
     return PSI_OK;
 }
 
-int make_game(int32_t n, const int32_t *owner, const int32_t *priority, const int32_t *offsets,
-              const int32_t *targets, HostGame &g)
+namespace {
+
+int32_t max_priority(int32_t n, const int32_t *priority)
+{
+    std::mutex mu;
+    int32_t mp = 0;
+    parallel_chunks(n, [&](int64_t lo, int64_t hi) {
+        int32_t local = 0;
+        for (int64_t v = lo; v < hi; v++) local = priority[v] > local ? priority[v] : local;
+        std::lock_guard<std::mutex> lk(mu);
+        mp = local > mp ? local : mp;
+    });
+    return mp;
+}
+
+}  // namespace
+
+int make_view(int32_t n, const int32_t *owner, const int32_t *priority, const int32_t *offsets,
+              const int32_t *targets, CsrView &v)
 {
     int rc = validate_csr(n, owner, priority, offsets, targets);
     if (rc) return rc;
+    v = CsrView{n, offsets[n], max_priority(n, priority), owner, priority, offsets, targets};
+    return PSI_OK;
+}
+
+// Validation is read-only and runs on several threads; the copy stays on one
+// (first-touch page faults from many threads were slower than one copy).
+int make_game(int32_t n, const int32_t *owner, const int32_t *priority, const int32_t *offsets,
+              const int32_t *targets, HostGame &g)
+{
+    CsrView v;
+    int rc = make_view(n, owner, priority, offsets, targets, v);
+    if (rc) return rc;
     g.n = n;
-    g.m = offsets[n];
-    g.owner.assign(owner, owner + n);
-    g.priority.assign(priority, priority + n);
-    g.offsets.assign(offsets, offsets + n + 1);
-    g.targets.assign(targets, targets + g.m);
-    int32_t mp = 0;
-    for (int32_t v = 0; v < n; v++) mp = priority[v] > mp ? priority[v] : mp;
-    g.max_pri = mp;
+    g.m = v.m;
+    g.max_pri = v.max_pri;
+    g.owner.resize(n);
+    g.priority.resize(n);
+    g.offsets.resize((size_t)n + 1);
+    g.targets.resize(g.m);
+    std::memcpy(g.owner.data(), owner, 4 * (size_t)n);
+    std::memcpy(g.priority.data(), priority, 4 * (size_t)n);
+    std::memcpy(g.offsets.data(), offsets, 4 * ((size_t)n + 1));
+    std::memcpy(g.targets.data(), targets, 4 * (size_t)g.m);
     return PSI_OK;
 }
 

@@ -20,6 +20,15 @@ long long launch_count();
 int build_reverse_csr(cudaStream_t s, int32_t n, int64_t m, const int32_t *off, const int32_t *tgt,
                       int32_t *rev_off, int32_t *rev_src, int64_t *rev_m);
 
+// Owner int32 -> int8 on the device (the upload sends the caller's int32 array).
+void launch_narrow_owner(cudaStream_t s, int32_t n, const int32_t *in, int8_t *out);
+// plist = Even's vertices in increasing order, then Odd's (in decreasing
+// order); *n_even (device) = Even's count.  Returns a cudaError_t value.
+int partition_players(cudaStream_t s, int32_t n, const int8_t *owner, int32_t *plist, int32_t *n_even);
+// Winning set of `player` from the status words, in increasing vertex order
+// (out: up to n ids; *count on the device).  Returns a cudaError_t value.
+int select_winning(cudaStream_t s, int32_t n, int32_t player, const int32_t *st, int32_t *out, int32_t *count);
+
 // ---- strategy set-up (gpu_parity.cu:38-56, cpu_parity.cpp:276-286, 300-307)
 void launch_init_strat(cudaStream_t s, int32_t n, const int8_t *owner, const int32_t *off,
                        const int32_t *tgt, int32_t *strat, int32_t *st);
@@ -44,14 +53,16 @@ int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, 
 void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const int2 *fin,
                             const int32_t *strat, const int32_t *pri, const uint8_t *solved,
                             int32_t *st, PathNode *node, int32_t *ulist, int32_t *ucount);
-// Root-path summaries (rmax, rcnt) of every reached vertex.
-void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, uint32_t *err);
-// Cycle parity of the *ucount vertices in ulist (cooperative launch).  ja, jb:
-// n entries; la, lb: n entries (active lists); cnt: 3 counters.  Returns a
-// cudaError_t value.
+// Root-path summaries (rmax, rcnt) of every reached vertex, also stored as its
+// comparison key when key != nullptr.
+void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, int2 *key, uint32_t *err);
+// Cycle parity of the *ucount vertices in ulist (cooperative launch), also
+// stored as their comparison keys when key != nullptr.  ja, jb: n entries;
+// la, lb: n entries (active lists); cnt: 3 counters.  Returns a cudaError_t
+// value.
 int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, const int32_t *strat,
-                  const int32_t *pri, const uint8_t *solved, int32_t *st, int2 *ja, int2 *jb, int32_t *la,
-                  int32_t *lb, int32_t *cnt, uint32_t *err);
+                  const int32_t *pri, const uint8_t *solved, int32_t *st, int2 *key, int2 *ja, int2 *jb,
+                  int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err);
 // mark_solved over the last evaluation's unreached vertices (cpu_parity.cpp:265-274);
 // with game_of/gmask only for games whose mask is set (nullptr: all).
 void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, int32_t player,
@@ -65,7 +76,7 @@ void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ul
 // and with gmask only vertices of games whose mask is set switch.
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player,
                    const int32_t *off, const int32_t *tgt, int32_t *strat, const int32_t *st,
-                   const PathNode *node, unsigned long long *stats, const int32_t *game_of,
+                   const int2 *key, const PathNode *node, unsigned long long *stats, const int32_t *game_of,
                    unsigned long long *gcount, const int32_t *gmask, uint32_t *err);
 // ---- batches: per-game accounting of solve_si (state[g] = brs, iters,
 // odd_done, done; gcount[g] = strict improvements of the last switch step)

@@ -198,7 +198,8 @@ extern "C" int psi_evaluate_strategy_noalloc(int32_t n, const int32_t *strategy,
     if (re) return fail(PSI_ERR_CUDA, std::string("reduced-list kernel launch: ") + cudaGetErrorString((cudaError_t)re));
     launch_broadcast_depth(s, n, vloc, fin, strategy, priority, solved, status, node, list, &w->ucount);
     int32_t *la = reinterpret_cast<int32_t *>(vloc), *lb = la + n;
-    int ce = launch_cycles(s, &w->ucount, list, strategy, priority, solved, status, ja, jb, la, lb, w->cnt, &w->err);
+    int ce = launch_cycles(s, &w->ucount, list, strategy, priority, solved, status, nullptr, ja, jb, la, lb, w->cnt,
+                           &w->err);
     if (ce) return fail(PSI_ERR_CUDA, std::string("cycle kernel launch: ") + cudaGetErrorString((cudaError_t)ce));
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(PSI_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e));

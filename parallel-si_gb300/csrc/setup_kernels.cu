@@ -1,9 +1,13 @@
-// setup_kernels.cu -- one-time device set-up of a game: the reverse CSR
-// (distinct in-neighbours of every vertex, in increasing order) that the tour
-// build scans to link each parent's children without atomics.
+// setup_kernels.cu -- device set-up of a game and ordered selections: the
+// reverse CSR (distinct in-neighbours of every vertex, in increasing order)
+// that the tour build scans to link each parent's children without atomics,
+// the owner narrowing and player lists built at upload, and the winning-set
+// selection read back at the end of a solve.
+#include <cub/device/device_partition.cuh>
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 #include <cub/device/device_select.cuh>
+#include <thrust/iterator/counting_iterator.h>
 
 #include "device_common.cuh"
 #include "kernels.h"
@@ -38,6 +42,26 @@ __global__ void k_rev_count(const unsigned long long *__restrict__ keys, const i
         src[i] = (int32_t)(uint32_t)(key & 0xffffffffull);
     }
 }
+
+__global__ void k_narrow_owner(int32_t n, const int32_t *__restrict__ in, int8_t *__restrict__ out)
+{
+    int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < n) out[v] = (int8_t)in[v];
+}
+
+struct OwnedBy {
+    const int8_t *owner;
+    int8_t player;
+    __device__ bool operator()(int32_t v) const { return owner[v] == player; }
+};
+
+// get_winning (cpu_parity.cpp:288-297): Even wins the +inf vertices, Odd every
+// other vertex.
+struct WonBy {
+    const int32_t *st;
+    int32_t player;
+    __device__ bool operator()(int32_t v) const { return (st[v] == ST_POS_INF) == (player == 0); }
+};
 
 int bits_for(int64_t x)
 {
@@ -99,6 +123,41 @@ out:
     if (deg) cudaFreeAsync(deg, s);
     if (tmp) cudaFreeAsync(tmp, s);
     return (int)e;
+}
+
+void launch_narrow_owner(cudaStream_t s, int32_t n, const int32_t *in, int8_t *out)
+{
+    if (n <= 0) return;
+    count_launch();
+    k_narrow_owner<<<grid_for(n), kBlock, 0, s>>>(n, in, out);
+}
+
+int partition_players(cudaStream_t s, int32_t n, const int8_t *owner, int32_t *plist, int32_t *n_even)
+{
+    thrust::counting_iterator<int32_t> ids(0);
+    OwnedBy even{owner, 0};
+    size_t bytes = 0;
+    cudaError_t e = cub::DevicePartition::If(nullptr, bytes, ids, plist, n_even, n, even, s);
+    if (e) return e;
+    void *tmp = nullptr;
+    if ((e = cudaMallocAsync(&tmp, bytes, s))) return e;
+    e = cub::DevicePartition::If(tmp, bytes, ids, plist, n_even, n, even, s);
+    cudaFreeAsync(tmp, s);
+    return e;
+}
+
+int select_winning(cudaStream_t s, int32_t n, int32_t player, const int32_t *st, int32_t *out, int32_t *count)
+{
+    thrust::counting_iterator<int32_t> ids(0);
+    WonBy won{st, player};
+    size_t bytes = 0;
+    cudaError_t e = cub::DeviceSelect::If(nullptr, bytes, ids, out, count, n, won, s);
+    if (e) return e;
+    void *tmp = nullptr;
+    if ((e = cudaMallocAsync(&tmp, bytes, s))) return e;
+    e = cub::DeviceSelect::If(tmp, bytes, ids, out, count, n, won, s);
+    cudaFreeAsync(tmp, s);
+    return e;
 }
 
 }  // namespace psi

@@ -43,7 +43,7 @@ int check_options(const psi_options &opt)
 
 }  // namespace
 
-int Solver::create(const HostGame &g, const psi_options &opt, Solver **out)
+int Solver::create(const CsrView &g, const psi_options &opt, Solver **out)
 {
     *out = nullptr;
     if (g.n <= 0) return fail(PSI_ERR_INVALID, "game has no vertices");
@@ -128,6 +128,7 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
         {(void **)&st_, 4 * (size_t)cap_n},
         {(void **)&solved_, (size_t)cap_n},
         {(void **)&node_, sizeof(PathNode) * (size_t)cap_n},
+        {(void **)&key_, 8 * (size_t)cap_n},
         {(void **)&succ_, 4 * (size_t)capL},
         {(void **)&hsucc_, 4 * (size_t)cap_sub},
         {(void **)&ulist_, 4 * (size_t)cap_n},
@@ -149,33 +150,32 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
     return PSI_OK;
 }
 
-// One game filling the arrays: upload, player lists, reverse CSR.
-int Solver::upload_game(const HostGame &g)
+// One game filling the arrays: upload, player lists, reverse CSR.  The
+// owner array goes up as the caller's int32 (into st_, free until the first
+// evaluation) and is narrowed on the device; the player lists are an ordered
+// partition on the device.
+int Solver::upload_game(const CsrView &g)
 {
     set_extent(g.n);
     m_ = g.m;
     max_pri_ = g.max_pri;
-    std::vector<int8_t> own8(g.owner.begin(), g.owner.end());
-    std::vector<int32_t> plist;
-    plist.reserve(n_);
-    for (int32_t v = 0; v < n_; v++)
-        if (g.owner[v] == 0) plist.push_back(v);
-    np0_ = (int32_t)plist.size();
-    for (int32_t v = 0; v < n_; v++)
-        if (g.owner[v] == 1) plist.push_back(v);
     np_ = n_;
-    PSI_CUDA_TRY(cudaMemcpyAsync(plist_, plist.data(), 4 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
-    PSI_CUDA_TRY(cudaMemcpyAsync(owner_, own8.data(), n_, cudaMemcpyHostToDevice, stream_));
-    PSI_CUDA_TRY(cudaMemcpyAsync(pri_, g.priority.data(), 4 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
-    PSI_CUDA_TRY(cudaMemcpyAsync(off_, g.offsets.data(), 4 * ((size_t)n_ + 1), cudaMemcpyHostToDevice, stream_));
-    if (m_) PSI_CUDA_TRY(cudaMemcpyAsync(tgt_, g.targets.data(), 4 * (size_t)m_, cudaMemcpyHostToDevice, stream_));
+    PSI_CUDA_TRY(cudaMemcpyAsync(st_, g.owner, 4 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
+    PSI_CUDA_TRY(cudaMemcpyAsync(pri_, g.priority, 4 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
+    PSI_CUDA_TRY(cudaMemcpyAsync(off_, g.offsets, 4 * ((size_t)n_ + 1), cudaMemcpyHostToDevice, stream_));
+    if (m_) PSI_CUDA_TRY(cudaMemcpyAsync(tgt_, g.targets, 4 * (size_t)m_, cudaMemcpyHostToDevice, stream_));
+    launch_narrow_owner(stream_, n_, st_, owner_);
+    int ce = partition_players(stream_, n_, owner_, plist_, &dw_->sinkcount);
+    if (ce) return fail(PSI_ERR_CUDA, std::string("player lists: ") + cudaGetErrorString((cudaError_t)ce));
     PSI_CUDA_TRY(cudaMemsetAsync(solved_, 0, n_, stream_));
     PSI_CUDA_TRY(cudaMemsetAsync(st_, 0, 4 * (size_t)n_, stream_));
     // reverse CSR on the device (distinct in-neighbours, increasing order)
     int64_t rev_m = 0;
-    int ce = build_reverse_csr(stream_, n_, m_, off_, tgt_, rev_off_, rev_src_, &rev_m);
+    ce = build_reverse_csr(stream_, n_, m_, off_, tgt_, rev_off_, rev_src_, &rev_m);
     if (ce) return fail(PSI_ERR_CUDA, std::string("reverse CSR: ") + cudaGetErrorString((cudaError_t)ce));
-    PSI_CUDA_TRY(cudaStreamSynchronize(stream_));
+    int rc = sync_and_check("upload");
+    if (rc) return rc;
+    np0_ = hw_->sinkcount;
     return PSI_OK;
 }
 
@@ -306,14 +306,14 @@ int Solver::compute_valuation()
     //    (ulist held the sink's children until here)
     phase_begin(PH_BROADCAST);
     launch_broadcast_depth(stream_, n_, vloc_, fin, strat_, pri_, solved_, st_, node_, ulist_, &dw_->ucount);
-    launch_rootinfo(stream_, n_, st_, node_, &dw_->err);
+    launch_rootinfo(stream_, n_, st_, node_, key_, &dw_->err);
     phase_end(PH_BROADCAST);
     // 4. cycle parity by pointer jumping over the unreached vertices
     phase_begin(PH_CYCLES);
     // the tour's vloc array is free again: it holds the two active lists
     int32_t *la = reinterpret_cast<int32_t *>(vloc_), *lb = la + n_;
-    int ce = launch_cycles(stream_, &dw_->ucount, ulist_, strat_, pri_, solved_, st_, jA_, jB_, la, lb, dw_->cnt,
-                           &dw_->err);
+    int ce = launch_cycles(stream_, &dw_->ucount, ulist_, strat_, pri_, solved_, st_, key_, jA_, jB_, la, lb,
+                           dw_->cnt, &dw_->err);
     if (ce) return fail(PSI_ERR_CUDA, std::string("cycle kernel launch: ") + cudaGetErrorString((cudaError_t)ce));
     phase_end(PH_CYCLES);
     phase_end(PH_EVAL);
@@ -349,7 +349,7 @@ int Solver::switch_strategy(int32_t player, int64_t *switched)
     phase_begin(PH_SWITCH);
     const int32_t np = (player == 0) ? np0_ : np_ - np0_;
     const int32_t *pl = plist_ + (player == 0 ? 0 : np0_);
-    launch_switch(stream_, np, pl, player, off_, tgt_, strat_, st_, node_, dw_->sw, game_of_, gcount_, gmask_,
+    launch_switch(stream_, np, pl, player, off_, tgt_, strat_, st_, key_, node_, dw_->sw, game_of_, gcount_, gmask_,
                   &dw_->err);
     phase_end(PH_SWITCH);
     rc = sync_and_check("switch_strategy");
@@ -384,15 +384,32 @@ int Solver::get_depth(int32_t *out)
 
 int Solver::get_winning(int32_t player, std::vector<int32_t> &out)
 {
-    if (player != 0 && player != 1) return fail(PSI_ERR_INVALID, "player must be 0 or 1");
-    std::vector<int32_t> inf(n_);
-    int rc = get_infinite(inf.data());
+    int64_t k = 0;
+    int rc = winning_ids(player, &k);
     if (rc) return rc;
-    out.clear();
-    for (int32_t v = 0; v < n_; v++) {
-        bool w0 = inf[v] == 1;
-        if ((player == 0 && w0) || (player == 1 && !w0)) out.push_back(v);
-    }
+    out.resize((size_t)k);
+    return copy_winning(out.data(), k);
+}
+
+// The winning set of `player` selected on the device into succ_ (free between
+// evaluations); *count receives its size.
+int Solver::winning_ids(int32_t player, int64_t *count)
+{
+    if (player != 0 && player != 1) return fail(PSI_ERR_INVALID, "player must be 0 or 1");
+    int rc = set_device();
+    if (rc) return rc;
+    int ce = select_winning(stream_, n_, player, st_, succ_, &dw_->sinkcount);
+    if (ce) return fail(PSI_ERR_CUDA, std::string("winning set: ") + cudaGetErrorString((cudaError_t)ce));
+    rc = sync_and_check("get_winning");
+    if (rc) return rc;
+    *count = hw_->sinkcount;
+    return PSI_OK;
+}
+
+int Solver::copy_winning(int32_t *out, int64_t k)
+{
+    if (k > 0) PSI_CUDA_TRY(cudaMemcpyAsync(out, succ_, 4 * (size_t)k, cudaMemcpyDeviceToHost, stream_));
+    PSI_CUDA_TRY(cudaStreamSynchronize(stream_));
     return PSI_OK;
 }
 

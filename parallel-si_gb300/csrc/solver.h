@@ -30,7 +30,7 @@ struct SolverTimes {
 
 class Solver {
 public:
-    static int create(const HostGame &g, const psi_options &opt, Solver **out);
+    static int create(const CsrView &g, const psi_options &opt, Solver **out);
     // An empty arena for served games (serve.cpp): up to max_vertices vertex
     // slots (each game takes n+1), max_edges edges, `slots` games at a time.
     static int create_arena(int64_t max_vertices, int64_t max_edges, int32_t slots, const psi_options &opt,
@@ -44,6 +44,9 @@ public:
     int mark_solved(int32_t player);
     int switch_strategy(int32_t player, int64_t *switched);
     int get_winning(int32_t player, std::vector<int32_t> &out);
+    // Device-side selection of the winning set, then a copy of its first k ids.
+    int winning_ids(int32_t player, int64_t *count);
+    int copy_winning(int32_t *out, int64_t k);
     int reset_opponent_strategy();
 
     int get_strategy(int32_t *out);
@@ -92,7 +95,7 @@ public:
 private:
     Solver() = default;
     int alloc_arrays(int64_t cap_n, int64_t cap_m);
-    int upload_game(const HostGame &g);
+    int upload_game(const CsrView &g);
     int init_arena(int32_t slots);
     void set_extent(int32_t n);
     int sync_and_check(const char *what);
@@ -134,6 +137,7 @@ private:
     int32_t *strat_ = nullptr, *st_ = nullptr;
     uint8_t *solved_ = nullptr;
     PathNode *node_ = nullptr;   // parent, priority and root-path summary (evaluation snapshot)
+    int2 *key_ = nullptr;        // comparison key per vertex (device_common.cuh)
     // evaluation scratch
     int32_t *succ_ = nullptr, *hsucc_ = nullptr, *ulist_ = nullptr;
     int32_t *rev_off_ = nullptr, *rev_src_ = nullptr;   // distinct in-neighbours (static)

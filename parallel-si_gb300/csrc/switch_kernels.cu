@@ -112,23 +112,10 @@ __device__ int walk_compare(const PathNode *__restrict__ node, int32_t u, int32_
     return 0;
 }
 
-// Comparison of finite u and w, u != w; ru, rw their root-path summaries
-// ((-1, 0) for the sink).
-__device__ __forceinline__ int compare_finite(const PathNode *__restrict__ node, int32_t u, int32_t su, int2 ru,
-                                              int32_t w, int32_t sw, int2 rw, int32_t &loads,
-                                              uint32_t *__restrict__ err)
-{
-    if (ru.x != rw.x) return ru.x > rw.x ? decide(ru.x, ru.y, 0) : decide(rw.x, 0, rw.y);
-    if (ru.y != rw.y) return decide(ru.x, ru.y, rw.y);
-    return walk_compare(node, u, su, w, sw, loads, err);
-}
-
-__device__ __forceinline__ int2 summary_of(const PathNode *__restrict__ node, int32_t x, int32_t sx)
-{
-    return (x >= 0 && sx >= 1) ? *reinterpret_cast<const int2 *>(&node[x].rmax) : make_int2(-1, 0);
-}
-
-// One thread per vertex of plist (all owned by `player`).
+// One thread per vertex of plist (all owned by `player`).  Per compared edge
+// the common case reads one 8-byte comparison key: infinite flags settle the
+// comparison, and so do different root-path summaries (tier 2); only equal
+// summaries of distinct finite vertices load their depths and walk (tier 3).
 // stats[0] += compared edges, stats[1] += parent/priority loads of tier-3
 // walks, stats[2] += vertices whose strategy changed, stats[3] += strict
 // improvements.  For a batch of games (game_of != nullptr) the strict
@@ -137,6 +124,7 @@ __device__ __forceinline__ int2 summary_of(const PathNode *__restrict__ node, in
 __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__restrict__ plist, int32_t player,
                                                    const int32_t *__restrict__ off, const int32_t *__restrict__ tgt,
                                                    int32_t *__restrict__ strat, const int32_t *__restrict__ st,
+                                                   const int2 *__restrict__ key,
                                                    const PathNode *__restrict__ node,
                                                    unsigned long long *__restrict__ stats,
                                                    const int32_t *__restrict__ game_of,
@@ -150,30 +138,28 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
     if (v >= 0 && gmask && !gmask[game_of[v]]) v = -1;
     if (v >= 0) {
         int32_t cur = strat[v];
-        int32_t scur = (cur >= 0) ? st[cur] : 0;
-        int2 rcur = summary_of(node, cur, scur);
+        int2 kc = (cur >= 0) ? key[cur] : make_int2(-1, 0);
         int32_t e0 = off[v], e1 = off[v + 1];
         n_edges = e1 - e0;
         for (int32_t e = e0; e < e1; e++) {
             int32_t u = tgt[e];
-            int32_t su = st[u];
-            int iu = st_infinite(su), ic = st_infinite(scur);
+            int2 ku = key[u];
+            int iu = key_infinite(ku.x), ic = key_infinite(kc.x);
             int c;
-            bool have_ru = false;
-            int2 ru = make_int2(-1, 0);
             if (iu | ic) {
                 c = (iu && ic) ? (iu == ic ? 0 : (iu == 1 ? 1 : -1)) : (iu ? iu : -ic);
             } else if (u == cur) {
                 c = 0;
+            } else if (ku.x != kc.x) {
+                c = ku.x > kc.x ? decide(ku.x, ku.y, 0) : decide(kc.x, 0, kc.y);
+            } else if (ku.y != kc.y) {
+                c = decide(ku.x, ku.y, kc.y);
             } else {
-                ru = summary_of(node, u, su);
-                have_ru = true;
-                c = compare_finite(node, u, su, ru, cur, scur, rcur, n_loads, err);
+                c = walk_compare(node, u, st[u], cur, cur >= 0 ? st[cur] : 0, n_loads, err);
             }
             if ((player == 0 && c > 0) || (player == 1 && c < 0)) {
                 cur = u;
-                scur = su;
-                rcur = have_ru ? ru : summary_of(node, u, su);
+                kc = ku;
                 moves++;
             }
         }
@@ -259,13 +245,13 @@ __global__ void k_materialize(int32_t v0, int32_t count, int32_t d, const int32_
 }  // namespace
 
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player, const int32_t *off,
-                   const int32_t *tgt, int32_t *strat, const int32_t *st, const PathNode *node,
+                   const int32_t *tgt, int32_t *strat, const int32_t *st, const int2 *key, const PathNode *node,
                    unsigned long long *stats, const int32_t *game_of, unsigned long long *gcount,
                    const int32_t *gmask, uint32_t *err)
 {
     if (np <= 0) return;
     count_launch();
-    k_switch<<<grid_for(np), kBlock, 0, s>>>(np, plist, player, off, tgt, strat, st, node, stats, game_of,
+    k_switch<<<grid_for(np), kBlock, 0, s>>>(np, plist, player, off, tgt, strat, st, key, node, stats, game_of,
                                              gcount, gmask, err);
 }
 

@@ -137,12 +137,29 @@ class GPUList:
     allocates the device state (GPUList, gpu_list_ranking.cu:14-36).
     """
 
-    def __init__(self, game: Game, options: Optional[Options] = None, **kw):
+    def __init__(self, game: Optional[Game], options: Optional[Options] = None, **kw):
+        self._h = C.c_void_p()
+        if game is None:       # filled in by from_csr
+            return
         o = options if options is not None else default_options(**kw)
         self.n = game.n
         self.max_pri = game.max_pri
-        self._h = C.c_void_p()
         check(lib.psi_solver_create(game._h, C.byref(o), C.byref(self._h)))
+
+    @classmethod
+    def from_csr(cls, owner, priority, offsets, targets, options: Optional[Options] = None, **kw) -> "GPUList":
+        """A solver straight from host CSR arrays (psi_solver_create_csr: no
+        intermediate host copy of the game)."""
+        o = options if options is not None else default_options(**kw)
+        ow = np.ascontiguousarray(owner, dtype=np.int32)
+        pr = np.ascontiguousarray(priority, dtype=np.int32)
+        off = np.ascontiguousarray(offsets, dtype=np.int32)
+        tg = np.ascontiguousarray(targets, dtype=np.int32)
+        s = cls(None)
+        check(lib.psi_solver_create_csr(len(ow), ptr(ow), ptr(pr), ptr(off), ptr(tg), C.byref(o), C.byref(s._h)))
+        s.n = len(ow)
+        s.max_pri = int(pr.max()) if len(pr) else 0
+        return s
 
     # ---- StrategyImprovement
     def init_strat(self) -> None:

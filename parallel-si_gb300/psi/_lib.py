@@ -72,6 +72,7 @@ _SIGS = {
     "psi_game_free": ([_vp], None),
     "psi_options_default": ([C.POINTER(Options)], None),
     "psi_solver_create": ([_vp, C.POINTER(Options), _pp], C.c_int),
+    "psi_solver_create_csr": ([C.c_int32, _vp, _vp, _vp, _vp, C.POINTER(Options), _pp], C.c_int),
     "psi_solver_destroy": ([_vp], None),
     "psi_init_strat": ([_vp], C.c_int),
     "psi_compute_valuation": ([_vp], C.c_int),

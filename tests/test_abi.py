@@ -4,6 +4,7 @@ import ctypes as C
 import os
 import re
 
+import numpy as np
 import pytest
 
 import psi
@@ -65,3 +66,45 @@ def test_invalid_options_rejected_before_device_use():
         h = C.c_void_p()
         rc = lib.psi_solver_create(g._h, C.byref(o), C.byref(h))
         assert rc in (PSI_ERR_INVALID, PSI_ERR_NO_DEVICE)
+
+
+def test_solver_from_host_csr_validates_before_device_use():
+    g = psi.Game.random(200, 2, 4, 200, 3)
+    ow, pr, off, tg = [np.ascontiguousarray(a, dtype=np.int32) for a in g.csr()]
+    h = C.c_void_p()
+    bad = tg.copy()
+    bad[5] = 200                     # successor out of range
+    assert lib.psi_solver_create_csr(len(ow), psi._lib.ptr(ow), psi._lib.ptr(pr), psi._lib.ptr(off),
+                                     psi._lib.ptr(bad), None, C.byref(h)) == PSI_ERR_INVALID
+    assert "successor" in psi.last_error()
+    neg = pr.copy()
+    neg[7] = -1
+    assert lib.psi_solver_create_csr(len(ow), psi._lib.ptr(ow), psi._lib.ptr(neg), psi._lib.ptr(off),
+                                     psi._lib.ptr(tg), None, C.byref(h)) == PSI_ERR_INVALID
+    assert "vertex 7" in psi.last_error()
+    rc = lib.psi_solver_create_csr(len(ow), psi._lib.ptr(ow), psi._lib.ptr(pr), psi._lib.ptr(off),
+                                   psi._lib.ptr(tg), None, C.byref(h))
+    if rc == PSI_OK:
+        lib.psi_solver_destroy(h)
+        pytest.skip("a CUDA device is present")
+    assert rc == PSI_ERR_NO_DEVICE
+
+
+def test_game_from_csr_reports_the_first_bad_vertex():
+    n = 3 << 20                      # large enough for the multi-threaded validation
+    owner = np.zeros(n, np.int32)
+    pri = np.ones(n, np.int32)
+    off = np.arange(n + 1, dtype=np.int32)
+    tg = (np.arange(n, dtype=np.int32) + 1) % n
+    owner[2_500_000] = 3
+    pri[1_000_000] = -4
+    with pytest.raises(psi.PsiError) as e:
+        psi.Game.from_csr(owner, pri, off, tg)
+    assert "negative priority at vertex 1000000" in str(e.value)
+    pri[1_000_000] = 1
+    with pytest.raises(psi.PsiError) as e:
+        psi.Game.from_csr(owner, pri, off, tg)
+    assert "invalid player at vertex 2500000" in str(e.value)
+    owner[2_500_000] = 1
+    g = psi.Game.from_csr(owner, pri, off, tg)
+    assert (g.n, g.m, g.max_pri) == (n, n, 1)

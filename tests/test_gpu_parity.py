@@ -74,3 +74,15 @@ def test_gpu_repeated_solves_are_identical():
         assert s.solve() == first
         assert np.array_equal(s.get_strategy(), strat)
         assert np.array_equal(s.get_winning(0), w0)
+
+
+def test_gpu_solver_from_host_csr_matches_game_handle():
+    g = make("c4", 30000, 71)
+    a = psi.GPUList(g)
+    b = psi.GPUList.from_csr(*g.csr())
+    assert a.solve() == b.solve()
+    assert np.array_equal(a.get_strategy(), b.get_strategy())
+    for p in (0, 1):
+        assert np.array_equal(a.get_winning(p), b.get_winning(p))
+    a.close()
+    b.close()
