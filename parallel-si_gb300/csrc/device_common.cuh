@@ -2,6 +2,7 @@
 #ifndef PSI_DEVICE_COMMON_CUH
 #define PSI_DEVICE_COMMON_CUH
 
+#include <climits>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -33,15 +34,30 @@ struct __align__(16) PathNode {
 };
 constexpr int32_t RM_UNKNOWN = INT32_MIN;
 
-// Comparison key of a vertex after an evaluation (8 bytes, what the switch
-// step gathers per compared edge): (rmax, rcnt) of its root path if its
-// valuation is finite (rmax >= 0: the path holds the vertex itself), or
-// (KEY_NEG_INF / KEY_POS_INF, 0).  The sink's key is (-1, 0).
-constexpr int32_t KEY_NEG_INF = -2;
-constexpr int32_t KEY_POS_INF = -3;
-__host__ __device__ __forceinline__ int32_t key_infinite(int32_t kx)
+// Comparison key of a vertex after an evaluation: 4 bytes, what the switch
+// step gathers per compared edge (n = 2^24 keys take 64 MiB and stay in L2).
+// With (M, c) the root-path summary of a finite vertex (the highest priority
+// on its path to the sink and its count), let
+//   q = M < KEY_MCAP ? (M << 7 | min(c, 126)) : KEY_MCAP << 7
+// and key = +q if M is even, -q if M is odd; +inf -> KEY_POS_INF, -inf ->
+// KEY_NEG_INF; the sink (empty path) -> 0.  The key is a monotone function of
+// the valuation order: between distinct summaries the highest priority whose
+// counts differ is max(M_u, M_w), so a higher even M is better and a higher
+// odd M worse, and at equal M a larger count is better if M is even, worse if
+// odd -- clamping c, or M together with c, only merges neighbours.  Hence
+// key_u > key_w implies u better than w, and equal keys of distinct finite
+// vertices are decided by their exact summaries, then by a walk.
+constexpr int32_t KEY_POS_INF = INT32_MAX;
+constexpr int32_t KEY_NEG_INF = -INT32_MAX;
+constexpr int32_t KEY_MCAP = (1 << 24) - 1;
+__host__ __device__ __forceinline__ int32_t finite_key(int32_t m, int32_t c)
 {
-    return kx == KEY_POS_INF ? 1 : (kx == KEY_NEG_INF ? -1 : 0);
+    int32_t q = (m < KEY_MCAP) ? ((m << 7) | (c < 126 ? c : 126)) : (KEY_MCAP << 7);
+    return (m & 1) ? -q : q;
+}
+__host__ __device__ __forceinline__ int key_infinite(int32_t k)
+{
+    return k == KEY_POS_INF ? 1 : (k == KEY_NEG_INF ? -1 : 0);
 }
 
 // Tour node ids (an Euler tour of the strategy forest, two nodes per vertex):

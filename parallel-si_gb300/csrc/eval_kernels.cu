@@ -257,7 +257,7 @@ __device__ __forceinline__ void top1_merge(int32_t &m, int32_t &c, int32_t m2, i
 // usually been done already).  A concurrent reader sees either RM_UNKNOWN or
 // the final pair, which is written as one 8-byte store.
 __global__ void k_rootinfo(int32_t n, const int32_t *__restrict__ st, PathNode *__restrict__ node,
-                           int2 *__restrict__ key, uint32_t *__restrict__ err)
+                           int32_t *__restrict__ key, uint32_t *__restrict__ err)
 {
     int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n || st[v] < 1) return;
@@ -278,7 +278,7 @@ __global__ void k_rootinfo(int32_t n, const int32_t *__restrict__ st, PathNode *
         }
     }
     *reinterpret_cast<int2 *>(&node[v].rmax) = make_int2(m, c);
-    if (key) key[v] = make_int2(m, c);
+    if (key) key[v] = finite_key(m, c);
 }
 
 // ---- cycle parity of the unreached vertices
@@ -297,7 +297,7 @@ constexpr int kSmallCycles = 4096;   // up to this many: one block, no grid barr
 template <bool GRID>
 __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const int32_t *__restrict__ strat,
                             const int32_t *__restrict__ pri, const uint8_t *__restrict__ solved,
-                            int32_t *__restrict__ st, int2 *__restrict__ key, int2 *__restrict__ ja,
+                            int32_t *__restrict__ st, int32_t *__restrict__ key, int2 *__restrict__ ja,
                             int2 *__restrict__ jb, int32_t *__restrict__ la, int32_t *__restrict__ lb,
                             int32_t *__restrict__ cnt, uint32_t *__restrict__ err)
 {
@@ -363,7 +363,7 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
         int32_t t = __ldcg(&in[u]).x;
         int32_t su = solved[t] ? st[t] : ((__ldcg(&in[t]).y % 2 == 0) ? ST_POS_INF : ST_NEG_INF);
         st[u] = su;
-        if (key) key[u] = make_int2(su == ST_POS_INF ? KEY_POS_INF : KEY_NEG_INF, 0);
+        if (key) key[u] = (su == ST_POS_INF) ? KEY_POS_INF : KEY_NEG_INF;
     }
 }
 
@@ -372,7 +372,7 @@ __global__ void __launch_bounds__(kBlock) k_cycles(const int32_t *__restrict__ u
                                                    const int32_t *__restrict__ strat,
                                                    const int32_t *__restrict__ pri,
                                                    const uint8_t *__restrict__ solved, int32_t *__restrict__ st,
-                                                   int2 *__restrict__ key, int2 *__restrict__ ja,
+                                                   int32_t *__restrict__ key, int2 *__restrict__ ja,
                                                    int2 *__restrict__ jb,
                                                    int32_t *__restrict__ la, int32_t *__restrict__ lb,
                                                    int32_t *__restrict__ cnt, uint32_t *__restrict__ err)
@@ -496,14 +496,14 @@ void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const i
     k_broadcast_depth<<<grid_for(n), kBlock, 0, s>>>(n, vloc, fin, strat, pri, solved, st, node, ulist, ucount);
 }
 
-void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, int2 *key, uint32_t *err)
+void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, int32_t *key, uint32_t *err)
 {
     count_launch();
     k_rootinfo<<<grid_for(n), kBlock, 0, s>>>(n, st, node, key, err);
 }
 
 int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, const int32_t *strat,
-                  const int32_t *pri, const uint8_t *solved, int32_t *st, int2 *key, int2 *ja, int2 *jb,
+                  const int32_t *pri, const uint8_t *solved, int32_t *st, int32_t *key, int2 *ja, int2 *jb,
                   int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err)
 {
     static int blocks = 0, blocks_dev = -1;

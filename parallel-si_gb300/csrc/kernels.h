@@ -55,13 +55,13 @@ void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const i
                             int32_t *st, PathNode *node, int32_t *ulist, int32_t *ucount);
 // Root-path summaries (rmax, rcnt) of every reached vertex, also stored as its
 // comparison key when key != nullptr.
-void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, int2 *key, uint32_t *err);
+void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, int32_t *key, uint32_t *err);
 // Cycle parity of the *ucount vertices in ulist (cooperative launch), also
 // stored as their comparison keys when key != nullptr.  ja, jb: n entries;
 // la, lb: n entries (active lists); cnt: 3 counters.  Returns a cudaError_t
 // value.
 int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, const int32_t *strat,
-                  const int32_t *pri, const uint8_t *solved, int32_t *st, int2 *key, int2 *ja, int2 *jb,
+                  const int32_t *pri, const uint8_t *solved, int32_t *st, int32_t *key, int2 *ja, int2 *jb,
                   int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err);
 // mark_solved over the last evaluation's unreached vertices (cpu_parity.cpp:265-274);
 // with game_of/gmask only for games whose mask is set (nullptr: all).
@@ -76,7 +76,7 @@ void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ul
 // and with gmask only vertices of games whose mask is set switch.
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player,
                    const int32_t *off, const int32_t *tgt, int32_t *strat, const int32_t *st,
-                   const int2 *key, const PathNode *node, unsigned long long *stats, const int32_t *game_of,
+                   const int32_t *key, const PathNode *node, unsigned long long *stats, const int32_t *game_of,
                    unsigned long long *gcount, const int32_t *gmask, uint32_t *err);
 // ---- batches: per-game accounting of solve_si (state[g] = brs, iters,
 // odd_done, done; gcount[g] = strict improvements of the last switch step)

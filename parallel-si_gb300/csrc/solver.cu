@@ -128,7 +128,7 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
         {(void **)&st_, 4 * (size_t)cap_n},
         {(void **)&solved_, (size_t)cap_n},
         {(void **)&node_, sizeof(PathNode) * (size_t)cap_n},
-        {(void **)&key_, 8 * (size_t)cap_n},
+        {(void **)&key_, 4 * (size_t)cap_n},
         {(void **)&succ_, 4 * (size_t)capL},
         {(void **)&hsucc_, 4 * (size_t)cap_sub},
         {(void **)&ulist_, 4 * (size_t)cap_n},

@@ -137,7 +137,7 @@ private:
     int32_t *strat_ = nullptr, *st_ = nullptr;
     uint8_t *solved_ = nullptr;
     PathNode *node_ = nullptr;   // parent, priority and root-path summary (evaluation snapshot)
-    int2 *key_ = nullptr;        // comparison key per vertex (device_common.cuh)
+    int32_t *key_ = nullptr;   // comparison key per vertex (device_common.cuh)
     // evaluation scratch
     int32_t *succ_ = nullptr, *hsucc_ = nullptr, *ulist_ = nullptr;
     int32_t *rev_off_ = nullptr, *rev_src_ = nullptr;   // distinct in-neighbours (static)

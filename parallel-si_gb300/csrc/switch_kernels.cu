@@ -112,19 +112,32 @@ __device__ int walk_compare(const PathNode *__restrict__ node, int32_t u, int32_
     return 0;
 }
 
+// Even's view of finite u against finite w (u != w) when their keys are
+// equal: the exact summaries decide, else a walk to the lowest common
+// ancestor (w = -1 is the sink).
+__device__ int compare_equal_keys(const PathNode *__restrict__ node, const int32_t *__restrict__ st,
+                                               int32_t u, int32_t w, int32_t &loads, uint32_t *__restrict__ err)
+{
+    const int2 ru = *reinterpret_cast<const int2 *>(&node[u].rmax);
+    const int2 rw = (w >= 0) ? *reinterpret_cast<const int2 *>(&node[w].rmax) : make_int2(-1, 0);
+    if (ru.x != rw.x) return ru.x > rw.x ? decide(ru.x, ru.y, 0) : decide(rw.x, 0, rw.y);
+    if (ru.y != rw.y) return decide(ru.x, ru.y, rw.y);
+    return walk_compare(node, u, st[u], w, w >= 0 ? st[w] : 0, loads, err);
+}
+
 // One thread per vertex of plist (all owned by `player`).  Per compared edge
-// the common case reads one 8-byte comparison key: infinite flags settle the
-// comparison, and so do different root-path summaries (tier 2); only equal
-// summaries of distinct finite vertices load their depths and walk (tier 3).
-// stats[0] += compared edges, stats[1] += parent/priority loads of tier-3
-// walks, stats[2] += vertices whose strategy changed, stats[3] += strict
-// improvements.  For a batch of games (game_of != nullptr) the strict
-// improvements are also added to gcount[game of the vertex]; with gmask only
-// vertices of games whose mask is set switch.
+// the common case is one 4-byte gather (the successor's comparison key) and
+// one integer comparison; equal keys of distinct finite vertices fall back to
+// the exact summaries and, rarely, a walk.  stats[0] += compared edges,
+// stats[1] += parent/priority loads of the walks, stats[2] += vertices whose
+// strategy changed, stats[3] += strict improvements.  For a batch of games
+// (game_of != nullptr) the strict improvements are also added to
+// gcount[game of the vertex]; with gmask only vertices of games whose mask is
+// set switch.
 __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__restrict__ plist, int32_t player,
                                                    const int32_t *__restrict__ off, const int32_t *__restrict__ tgt,
                                                    int32_t *__restrict__ strat, const int32_t *__restrict__ st,
-                                                   const int2 *__restrict__ key,
+                                                   const int32_t *__restrict__ key,
                                                    const PathNode *__restrict__ node,
                                                    unsigned long long *__restrict__ stats,
                                                    const int32_t *__restrict__ game_of,
@@ -138,29 +151,58 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
     if (v >= 0 && gmask && !gmask[game_of[v]]) v = -1;
     if (v >= 0) {
         int32_t cur = strat[v];
-        int2 kc = (cur >= 0) ? key[cur] : make_int2(-1, 0);
-        int32_t e0 = off[v], e1 = off[v + 1];
+        int32_t kc = (cur >= 0) ? key[cur] : 0;
+        const int32_t e0 = off[v], e1 = off[v + 1];
         n_edges = e1 - e0;
-        for (int32_t e = e0; e < e1; e++) {
-            int32_t u = tgt[e];
-            int2 ku = key[u];
-            int iu = key_infinite(ku.x), ic = key_infinite(kc.x);
-            int c;
-            if (iu | ic) {
-                c = (iu && ic) ? (iu == ic ? 0 : (iu == 1 ? 1 : -1)) : (iu ? iu : -ic);
-            } else if (u == cur) {
-                c = 0;
-            } else if (ku.x != kc.x) {
-                c = ku.x > kc.x ? decide(ku.x, ku.y, 0) : decide(kc.x, 0, kc.y);
-            } else if (ku.y != kc.y) {
-                c = decide(ku.x, ku.y, kc.y);
-            } else {
-                c = walk_compare(node, u, st[u], cur, cur >= 0 ? st[cur] : 0, n_loads, err);
+        // Fast pass: successors in batches of kBatch -- all ids, then all
+        // keys, before the comparisons (independent gathers in flight per
+        // thread).  Equal keys of distinct finite vertices end it; the exact
+        // pass then redoes the vertex with summaries and walks.
+        constexpr int kBatch = 4;
+        const int32_t cur0 = cur, kc0 = kc;
+        bool exact = false;
+        for (int32_t eb = e0; eb < e1 && !exact; eb += kBatch) {
+            const int32_t cnt = min(kBatch, e1 - eb);
+            int32_t us[kBatch], ks[kBatch];
+#pragma unroll
+            for (int j = 0; j < kBatch; j++) us[j] = (j < cnt) ? tgt[eb + j] : 0;
+#pragma unroll
+            for (int j = 0; j < kBatch; j++) ks[j] = (j < cnt) ? key[us[j]] : 0;
+#pragma unroll
+            for (int j = 0; j < kBatch; j++) {
+                if (j >= cnt) break;
+                const int32_t u = us[j], ku = ks[j];
+                int c;
+                if (ku != kc) {
+                    c = ku > kc ? 1 : -1;
+                } else if (u == cur || key_infinite(ku)) {
+                    c = 0;
+                } else {
+                    exact = true;
+                    break;
+                }
+                if ((player == 0 && c > 0) || (player == 1 && c < 0)) {
+                    cur = u;
+                    kc = ku;
+                    moves++;
+                }
             }
-            if ((player == 0 && c > 0) || (player == 1 && c < 0)) {
-                cur = u;
-                kc = ku;
-                moves++;
+        }
+        if (exact) {
+            cur = cur0;
+            kc = kc0;
+            moves = 0;
+            for (int32_t e = e0; e < e1; e++) {
+                const int32_t u = tgt[e], ku = key[u];
+                int c;
+                if (ku != kc) c = ku > kc ? 1 : -1;
+                else if (u == cur || key_infinite(ku)) c = 0;
+                else c = compare_equal_keys(node, st, u, cur, n_loads, err);
+                if ((player == 0 && c > 0) || (player == 1 && c < 0)) {
+                    cur = u;
+                    kc = ku;
+                    moves++;
+                }
             }
         }
         if (moves) {
@@ -245,7 +287,7 @@ __global__ void k_materialize(int32_t v0, int32_t count, int32_t d, const int32_
 }  // namespace
 
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player, const int32_t *off,
-                   const int32_t *tgt, int32_t *strat, const int32_t *st, const int2 *key, const PathNode *node,
+                   const int32_t *tgt, int32_t *strat, const int32_t *st, const int32_t *key, const PathNode *node,
                    unsigned long long *stats, const int32_t *game_of, unsigned long long *gcount,
                    const int32_t *gmask, uint32_t *err)
 {
