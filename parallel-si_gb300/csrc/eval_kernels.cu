@@ -101,9 +101,13 @@ __global__ void k_tour_init(int32_t n, int32_t *__restrict__ succ, int2 *__restr
 }
 
 // Thread p: (a) if p is a live child of the sink, append it to the sink list;
-// (b) if p is live, link its live children, found among its distinct
-// in-neighbours rev_src[rev_off[p] .. rev_off[p+1]), as
+// (b) if p is live, link its children, found among its distinct in-neighbours
+// rev_src[rev_off[p] .. rev_off[p+1]), as
 // up(p) -> up(c0) ... down(c0) -> up(c1) ... down(c_last) -> down(p).
+// A solved child is linked like any other (checking would cost a second
+// random gather per in-neighbour): its up/down pair adds +1-1 to no one's
+// depth, its own children stay unlinked (a solved parent links nothing), and
+// the broadcast skips it.
 __global__ void k_tour_link(int32_t n, const int32_t *__restrict__ strat, const uint8_t *__restrict__ solved,
                             const int32_t *__restrict__ rev_off, const int32_t *__restrict__ rev_src,
                             int32_t *__restrict__ succ, int32_t *__restrict__ sinklist,
@@ -118,7 +122,7 @@ __global__ void k_tour_link(int32_t n, const int32_t *__restrict__ strat, const 
     int32_t e1 = rev_off[p + 1];
     for (int32_t e = rev_off[p]; e < e1; e++) {
         int32_t u = rev_src[e];
-        if (strat[u] != p || solved[u]) continue;
+        if (strat[u] != p) continue;
         if (prev < 0) succ[2 * (int64_t)p + 1] = 2 * u + 1;
         else succ[2 * (int64_t)prev] = 2 * u + 1;
         prev = u;
