@@ -64,10 +64,7 @@ __host__ __device__ __forceinline__ int key_infinite(int32_t k)
 // node 2v is v's "down" node (leaving v's subtree toward the sink), 2v+1 its
 // "up" node (entering it); 2n / 2n+1 are the sink's down / up nodes.  The list
 // starts at the sink's up node and ends at the sink's down node (successor -1).
-// A successor entry below -1 marks a sublist head: -2 - j names sublist j.
 constexpr int32_t TOUR_END = -1;
-__host__ __device__ __forceinline__ int32_t head_mark(int32_t j) { return -2 - j; }
-__host__ __device__ __forceinline__ int32_t head_of_mark(int32_t x) { return -2 - x; }
 
 // Device-side error bits (a word the host reads back at sync points).
 constexpr uint32_t DERR_SUBLIST_CAP = 1u << 0;   // a sublist walk exceeded the list length

@@ -4,16 +4,22 @@
 // the sink) into a per-vertex status word (device_common.cuh):
 //
 //  1. Euler tour of the sink tree (tour_init, tour_link, sink_chain).  Every
-//     non-solved vertex's up/down node pair is spliced into its parent's list
-//     of children -- the reference builds the same list with one atomic
-//     exchange per vertex (gpu_list_ranking.cu:52-92).  Here each parent links
-//     its own children by scanning its in-neighbours in a reverse CSR that is
-//     built once per game, so the step needs no atomics and the child order
-//     (in-neighbour order) is deterministic; the sink's children, which can be
-//     millions, are compacted with one atomic per warp and chained.
-//  2. Helman-JaJa list ranking: `nsub` sublist heads at a fixed node stride
-//     (pick_heads, gpu_list_ranking.cu:96-110); one thread per sublist walks to
-//     the next head accumulating +1/-1 depth steps (walk_sublists,
+//     vertex's up/down node pair is spliced into its parent's list of
+//     children -- the reference builds the same list with one atomic exchange
+//     per vertex (gpu_list_ranking.cu:52-92), which serialises on popular
+//     parents.  Here each live parent links its own children by scanning its
+//     in-neighbours in a reverse CSR built once per game: no atomics, and the
+//     child order (in-neighbour order) is deterministic; the sink's children,
+//     which can be millions, are compacted with one atomic per warp and
+//     chained.  After the first evaluation the tour is kept up to date
+//     instead (tour_relink): only parents whose children changed since -- the
+//     old and new successor of each switched vertex, each newly solved vertex
+//     -- are relinked, a few percent of them per step.
+//  2. Helman-JaJa list ranking: `nsub` sublist heads at fixed tour nodes
+//     (node j*stride, and the list start; gpu_list_ranking.cu:96-110 marks
+//     heads in the successor array, here a node's head index follows from its
+//     id so the tour is never modified); one thread per sublist walks to the
+//     next head accumulating +1/-1 depth steps (walk_sublists,
 //     gpu_list_ranking.cu:114-193).  The reduced list of sublists is ranked on
 //     the device by Wyllie pointer jumping in one cooperative launch
 //     (rank_reduced) -- the reference copies it to the host and walks it
@@ -70,6 +76,32 @@ __device__ __forceinline__ void warp_append(bool flag, int32_t value, int32_t *_
     }
 }
 
+// Block-aggregated append: every thread of the block calls it (no early
+// return before); one atomic on the shared counter per block instead of one
+// per warp, which serialises when most warps append (the sink's children,
+// the unreached vertices, the dirty parents).
+__device__ __forceinline__ void block_append(bool flag, int32_t value, int32_t *__restrict__ list,
+                                             int32_t *__restrict__ count)
+{
+    __shared__ int32_t warp_base[kBlock / 32];
+    __shared__ int32_t block_base;
+    const unsigned mask = __ballot_sync(0xffffffffu, flag);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) warp_base[w] = __popc(mask);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int32_t sum = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+            int32_t t = warp_base[i];
+            warp_base[i] = sum;
+            sum += t;
+        }
+        block_base = sum ? atomicAdd(count, sum) : 0;
+    }
+    __syncthreads();
+    if (flag) list[block_base + warp_base[w] + __popc(mask & ((1u << lane) - 1))] = value;
+}
+
 __global__ void k_init_strat(int32_t n, const int8_t *__restrict__ owner, const int32_t *__restrict__ off,
                              const int32_t *__restrict__ tgt, int32_t *__restrict__ strat,
                              int32_t *__restrict__ st)
@@ -116,7 +148,7 @@ __global__ void k_tour_link(int32_t n, const int32_t *__restrict__ strat, const 
     int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
     bool live = p < n && !solved[p];
     bool to_sink = live && strat[p] < 0;
-    warp_append(to_sink, p, sinklist, sinkcount);
+    block_append(to_sink, p, sinklist, sinkcount);
     if (!live) return;
     int32_t prev = -1;
     int32_t e1 = rev_off[p + 1];
@@ -130,11 +162,67 @@ __global__ void k_tour_link(int32_t n, const int32_t *__restrict__ strat, const 
     if (prev >= 0) succ[2 * (int64_t)prev] = 2 * p;
 }
 
+// Incremental tour maintenance.  Between evaluations the tour lists persist
+// in succ; the switch step and mark_solved flag as dirty every parent whose set
+// of children may have changed (the old and the new parent of each changed
+// strategy, each newly solved vertex).  Thread p relinks a dirty p from its
+// in-neighbours: a live p chains its current children exactly as k_tour_link
+// does; a solved p links none and turns each of its children into an isolated
+// 2-cycle (down -> own up), so they are unreached and the cycle pass gives
+// them p's frozen value.  Parents that are not dirty keep their lists, which
+// are still exact.  The dirty parents are compacted first (k_dirty_list, which
+// also clears the flags), so the relinking threads are all busy.
+__global__ void k_dirty_list(int32_t n, uint8_t *__restrict__ dirty, int32_t *__restrict__ list,
+                             int32_t *__restrict__ count)
+{
+    int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    bool take = p < n && dirty[p];
+    if (take) dirty[p] = 0;
+    block_append(take, p, list, count);
+}
+
+__global__ void k_tour_relink(const int32_t *__restrict__ list, const int32_t *__restrict__ count,
+                              const int32_t *__restrict__ strat, const uint8_t *__restrict__ solved,
+                              const int32_t *__restrict__ rev_off, const int32_t *__restrict__ rev_src,
+                              int32_t *__restrict__ succ)
+{
+    const int32_t k = *count;
+    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k; i += gridDim.x * blockDim.x) {
+        const int32_t p = list[i];
+        const bool live = !solved[p];
+        int32_t prev = -1;
+        const int32_t e1 = rev_off[p + 1];
+        for (int32_t e = rev_off[p]; e < e1; e++) {
+            int32_t u = rev_src[e];
+            if (strat[u] != p) continue;
+            if (!live) {
+                succ[2 * (int64_t)u] = 2 * u + 1;
+                continue;
+            }
+            if (prev < 0) succ[2 * (int64_t)p + 1] = 2 * u + 1;
+            else succ[2 * (int64_t)prev] = 2 * u + 1;
+            prev = u;
+        }
+        if (prev >= 0) succ[2 * (int64_t)prev] = 2 * p;
+        else succ[2 * (int64_t)p + 1] = 2 * p;
+    }
+}
+
+// The sink's live children (the full build collects them in k_tour_link).
+__global__ void k_sink_list(int32_t n, const int32_t *__restrict__ strat, const uint8_t *__restrict__ solved,
+                            int32_t *__restrict__ sinklist, int32_t *__restrict__ sinkcount)
+{
+    int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    bool take = v < n && strat[v] < 0 && !solved[v];
+    block_append(take, v, sinklist, sinkcount);
+}
+
 // sink up -> up(c0) ... down(c0) -> up(c1) ... down(c_last) -> sink down
 __global__ void k_sink_chain(int32_t n, const int32_t *__restrict__ sinklist,
                              const int32_t *__restrict__ sinkcount, int32_t *__restrict__ succ)
 {
     int32_t k = *sinkcount;
+    if (k == 0 && blockIdx.x == 0 && threadIdx.x == 0) succ[2 * (int64_t)n + 1] = 2 * n;
     for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k; i += gridDim.x * blockDim.x) {
         int32_t v = sinklist[i];
         succ[2 * (int64_t)v] = (i + 1 < k) ? 2 * sinklist[i + 1] + 1 : 2 * n;
@@ -142,31 +230,35 @@ __global__ void k_sink_chain(int32_t n, const int32_t *__restrict__ sinklist,
     }
 }
 
-// Head j sits at node j*stride; the last head is the sink's up node (the list
-// start), so the reduced list starts at sublist nsub-1.
-__global__ void k_pick_heads(int64_t L, int32_t nsub, int32_t stride, int32_t *__restrict__ succ,
-                             int32_t *__restrict__ hsucc)
+// Sublist heads are fixed tour nodes: node j*stride is head j for j < nsub-1
+// and the list start (the sink's up node, L-1) is head nsub-1, so the reduced
+// list starts at sublist nsub-1.  A node's head index follows from its id,
+// and succ is never modified by the ranking (it persists between
+// evaluations).
+template <bool POW2>
+__device__ __forceinline__ int32_t head_index(int32_t x, int64_t L, int32_t nsub, int32_t stride)
 {
-    int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= nsub) return;
-    int64_t node = (j == nsub - 1) ? L - 1 : (int64_t)j * stride;
-    hsucc[j] = succ[node];
-    succ[node] = head_mark(j);
+    if (x == L - 1) return nsub - 1;
+    int32_t j = POW2 ? (x >> (__ffs(stride) - 1)) : x / stride;
+    bool at = POW2 ? (x & (stride - 1)) == 0 : j * stride == x;
+    return (at && j < nsub - 1) ? j : -1;
 }
 
 // One thread per sublist: walk from the head's successor up to and including
-// the next head (whose successor entry holds a mark), accumulating the depth
-// steps (+1 at a real vertex's up node, -1 at its down node, 0 at the sink's
-// nodes) and recording, at each up node, the sublist and the inclusive local
-// prefix.  red[j] = (next sublist or TOUR_END, sublist total).
-__global__ void k_walk_sublists(int32_t nsub, int32_t n, int64_t L, const int32_t *__restrict__ succ,
-                                const int32_t *__restrict__ hsucc, int2 *__restrict__ vloc,
+// the next head, accumulating the depth steps (+1 at a real vertex's up node,
+// -1 at its down node, 0 at the sink's nodes) and recording, at each up node,
+// the sublist and the inclusive local prefix.  red[j] = (next sublist or
+// TOUR_END, sublist total).
+template <bool POW2>
+__global__ void k_walk_sublists(int32_t nsub, int32_t n, int64_t L, int32_t stride,
+                                const int32_t *__restrict__ succ, int2 *__restrict__ vloc,
                                 int2 *__restrict__ red, uint32_t *__restrict__ err)
 {
     int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nsub) return;
-    int32_t x = hsucc[j];
-    int32_t acc = 0;
+    const int64_t h = (j == nsub - 1) ? L - 1 : (int64_t)j * stride;
+    int32_t x = __ldg(&succ[h]);
+    int32_t acc = 0, next = TOUR_END;
     int64_t steps = 0;
     const int32_t sink_down = 2 * n;
     while (x >= 0) {
@@ -178,14 +270,18 @@ __global__ void k_walk_sublists(int32_t nsub, int32_t n, int64_t L, const int32_
                 acc -= 1;
             }
         }
+        int32_t hx = head_index<POW2>(x, L, nsub, stride);
+        if (hx >= 0) {
+            next = hx;
+            break;
+        }
         x = __ldg(&succ[x]);
         if (++steps > L) {
             atomicOr(err, DERR_SUBLIST_CAP);
-            x = TOUR_END;
             break;
         }
     }
-    red[j] = make_int2(x == TOUR_END ? TOUR_END : head_of_mark(x), acc);
+    red[j] = make_int2(next, acc);
 }
 
 // ---- ranking of the reduced list (items = sublists, weight = sublist total)
@@ -240,7 +336,7 @@ __global__ void k_broadcast_depth(int32_t n, const int2 *__restrict__ vloc, cons
             unreached = true;
         }
     }
-    warp_append(unreached, v, ulist, ucount);
+    block_append(unreached, v, ulist, ucount);
 }
 
 // (max, count of max) of the union of two priority multisets
@@ -395,7 +491,8 @@ __global__ void __launch_bounds__(kBlock) k_cycles(const int32_t *__restrict__ u
 // With game_of/gmask (served games), only vertices of games whose mask is set.
 __global__ void k_mark_solved(const int32_t *__restrict__ ucount, const int32_t *__restrict__ ulist,
                               int32_t player, const int32_t *__restrict__ st, uint8_t *__restrict__ solved,
-                              const int32_t *__restrict__ game_of, const int32_t *__restrict__ gmask)
+                              uint8_t *__restrict__ dirty, const int32_t *__restrict__ game_of,
+                              const int32_t *__restrict__ gmask)
 {
     int32_t nu = *ucount;
     int32_t target = (player == 0) ? ST_POS_INF : ST_NEG_INF;
@@ -405,7 +502,10 @@ __global__ void k_mark_solved(const int32_t *__restrict__ ucount, const int32_t 
             int32_t g = game_of[u];
             if (g < 0 || !gmask[g]) continue;
         }
-        if (st[u] == target) solved[u] = 1;
+        if (st[u] == target) {
+            solved[u] = 1;
+            dirty[u] = 1;
+        }
     }
 }
 
@@ -458,17 +558,34 @@ void launch_tour_build(cudaStream_t s, int32_t n, const int32_t *strat, const ui
     k_sink_chain<<<g < 1216u ? g : 1216u, kBlock, 0, s>>>(n, sinklist, sinkcount, succ);
 }
 
-void launch_pick_heads(cudaStream_t s, int64_t L, int32_t nsub, int32_t stride, int32_t *succ, int32_t *hsucc)
+int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
+                       const int32_t *rev_off, const int32_t *rev_src, uint8_t *dirty, int32_t *succ, int2 *vloc,
+                       int32_t *sinklist, int32_t *sinkcount, int32_t *dlist, int32_t *dcount)
 {
+    cudaError_t e = cudaMemsetAsync(vloc, 0xff, 8 * (size_t)n, s);   // (-1, -1): on no walked sublist
+    if (e == cudaSuccess) e = cudaMemsetAsync(dcount, 0, sizeof(int32_t), s);
+    if (e != cudaSuccess) return (int)e;
     count_launch();
-    k_pick_heads<<<grid_for(nsub), kBlock, 0, s>>>(L, nsub, stride, succ, hsucc);
+    k_dirty_list<<<grid_for(n), kBlock, 0, s>>>(n, dirty, dlist, dcount);
+    count_launch();
+    unsigned g = grid_for(n);
+    g = g < 1216u ? g : 1216u;
+    k_tour_relink<<<g, kBlock, 0, s>>>(dlist, dcount, strat, solved, rev_off, rev_src, succ);
+    count_launch();
+    k_sink_list<<<grid_for(n), kBlock, 0, s>>>(n, strat, solved, sinklist, sinkcount);
+    count_launch();
+    k_sink_chain<<<g, kBlock, 0, s>>>(n, sinklist, sinkcount, succ);
+    return 0;
 }
 
-void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, const int32_t *succ,
-                          const int32_t *hsucc, int2 *vloc, int2 *red, uint32_t *err)
+void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, int32_t stride, const int32_t *succ,
+                          int2 *vloc, int2 *red, uint32_t *err)
 {
     count_launch();
-    k_walk_sublists<<<grid_for(nsub, 128), 128, 0, s>>>(nsub, n, L, succ, hsucc, vloc, red, err);
+    if ((stride & (stride - 1)) == 0)
+        k_walk_sublists<true><<<grid_for(nsub, 128), 128, 0, s>>>(nsub, n, L, stride, succ, vloc, red, err);
+    else
+        k_walk_sublists<false><<<grid_for(nsub, 128), 128, 0, s>>>(nsub, n, L, stride, succ, vloc, red, err);
 }
 
 int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, int2 *b, const int2 **fin)
@@ -526,10 +643,11 @@ int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, c
 }
 
 void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, int32_t player,
-                        const int32_t *st, uint8_t *solved, const int32_t *game_of, const int32_t *gmask)
+                        const int32_t *st, uint8_t *solved, uint8_t *dirty, const int32_t *game_of,
+                        const int32_t *gmask)
 {
     count_launch();
-    k_mark_solved<<<608, kBlock, 0, s>>>(ucount, ulist, player, st, solved, game_of, gmask);
+    k_mark_solved<<<608, kBlock, 0, s>>>(ucount, ulist, player, st, solved, dirty, game_of, gmask);
 }
 
 }  // namespace psi

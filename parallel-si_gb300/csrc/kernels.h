@@ -36,15 +36,22 @@ void launch_reset_odd(cudaStream_t s, int32_t n, const int8_t *owner, const int3
                       const int32_t *tgt, int32_t *strat);
 
 // ---- evaluation (gpu_list_ranking.cu:52-277)
-// Euler tour of the sink tree.  rev_off/rev_src: distinct in-neighbours of each
-// vertex.  *sinkcount must be 0 on entry; sinklist holds n entries.
+// Euler tour of the sink tree, built from scratch.  rev_off/rev_src: distinct
+// in-neighbours of each vertex.  *sinkcount must be 0 on entry; sinklist holds
+// n entries.
 void launch_tour_build(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
                        const int32_t *rev_off, const int32_t *rev_src, int32_t *succ, int2 *vloc,
                        int32_t *sinklist, int32_t *sinkcount);
-void launch_pick_heads(cudaStream_t s, int64_t L, int32_t nsub, int32_t stride, int32_t *succ,
-                       int32_t *hsucc);
-void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, const int32_t *succ,
-                          const int32_t *hsucc, int2 *vloc, int2 *red, uint32_t *err);
+// The same tour brought up to date from the previous one: only the parents
+// flagged in dirty (cleared here; dlist: n entries of scratch, dcount: one
+// counter) are relinked and the sink's list is rebuilt.  Returns a
+// cudaError_t value.
+int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
+                       const int32_t *rev_off, const int32_t *rev_src, uint8_t *dirty, int32_t *succ, int2 *vloc,
+                       int32_t *sinklist, int32_t *sinkcount, int32_t *dlist, int32_t *dcount);
+// Sublist walks; heads are the nodes j*stride (j < nsub-1) and the list start.
+void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, int32_t stride, const int32_t *succ,
+                          int2 *vloc, int2 *red, uint32_t *err);
 // Ranks the reduced list red[0..nsub) (next, weight) by Wyllie pointer jumping
 // (cooperative launch; a, b: nsub entries each).  *fin is set to the buffer
 // that will hold, per item, (TOUR_END if the list start reaches it, else >= 0;
@@ -65,19 +72,21 @@ int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, c
                   int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err);
 // mark_solved over the last evaluation's unreached vertices (cpu_parity.cpp:265-274);
 // with game_of/gmask only for games whose mask is set (nullptr: all).
+// Newly solved vertices are flagged in dirty (their children leave the tour).
 void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, int32_t player,
-                        const int32_t *st, uint8_t *solved, const int32_t *game_of = nullptr,
+                        const int32_t *st, uint8_t *solved, uint8_t *dirty, const int32_t *game_of = nullptr,
                         const int32_t *gmask = nullptr);
 
 // ---- all-switches (gpu_parity.cu:191-317, cpu_parity.cpp:154-263)
 // Switches the np vertices listed in plist (all owned by `player`).
 // stats[0..3] += compared edges, walk loads, changed vertices, strict
 // improvements; with game_of (batches) also gcount[game] += improvements,
-// and with gmask only vertices of games whose mask is set switch.
+// and with gmask only vertices of games whose mask is set switch.  The old and
+// the new successor of every changed vertex are flagged in dirty.
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player,
                    const int32_t *off, const int32_t *tgt, int32_t *strat, const int32_t *st,
                    const int32_t *key, const PathNode *node, unsigned long long *stats, const int32_t *game_of,
-                   unsigned long long *gcount, const int32_t *gmask, uint32_t *err);
+                   unsigned long long *gcount, const int32_t *gmask, uint8_t *dirty, uint32_t *err);
 // ---- batches: per-game accounting of solve_si (state[g] = brs, iters,
 // odd_done, done; gcount[g] = strict improvements of the last switch step)
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state,
@@ -105,7 +114,7 @@ void launch_serve_account(cudaStream_t s, int32_t slots, int32_t event, int4 *st
 // switched go back to their first successor.
 void launch_serve_reset_odd(cudaStream_t s, int32_t np, const int32_t *plist, const int32_t *game_of,
                             const int32_t *gmask, const unsigned long long *gcount, const int32_t *off,
-                            const int32_t *tgt, int32_t *strat);
+                            const int32_t *tgt, int32_t *strat, uint8_t *dirty);
 
 // ---- dense valuation rows for export (the reference's ArrayVal layout)
 void launch_materialize(cudaStream_t s, int32_t v0, int32_t count, int32_t d, const int32_t *st,

@@ -44,8 +44,7 @@ struct Layout {
     static constexpr size_t solved = align256(node + sizeof(PathNode) * (size_t)kMaxN);
     static constexpr size_t ja = align256(solved + (size_t)kMaxN);
     static constexpr size_t jb = align256(ja + 8 * (size_t)kMaxN);
-    static constexpr size_t hsucc = align256(jb + 8 * (size_t)kMaxN);
-    static constexpr size_t redA = align256(hsucc + 4 * (size_t)kMaxSub);
+    static constexpr size_t redA = align256(jb + 8 * (size_t)kMaxN);
     static constexpr size_t redB = align256(redA + 8 * (size_t)kMaxSub);
     static constexpr size_t redC = align256(redB + 8 * (size_t)kMaxSub);
     static constexpr size_t total = align256(redC + 8 * (size_t)kMaxSub);
@@ -173,7 +172,6 @@ extern "C" int psi_evaluate_strategy_noalloc(int32_t n, const int32_t *strategy,
     uint8_t *solved = reinterpret_cast<uint8_t *>(base + Layout::solved);
     int2 *ja = reinterpret_cast<int2 *>(base + Layout::ja);
     int2 *jb = reinterpret_cast<int2 *>(base + Layout::jb);
-    int32_t *hsucc = reinterpret_cast<int32_t *>(base + Layout::hsucc);
     int2 *redA = reinterpret_cast<int2 *>(base + Layout::redA);
     int2 *redB = reinterpret_cast<int2 *>(base + Layout::redB);
     int2 *redC = reinterpret_cast<int2 *>(base + Layout::redC);
@@ -191,8 +189,7 @@ extern "C" int psi_evaluate_strategy_noalloc(int32_t n, const int32_t *strategy,
     count_launch();
     unsigned g = grid_for(n);
     k_na_sink_chain<<<g < 1216u ? g : 1216u, kBlock, 0, s>>>(n, list, &w->sinkcount, succ);
-    launch_pick_heads(s, L, nsub, kStride, succ, hsucc);
-    launch_walk_sublists(s, nsub, n, L, succ, hsucc, vloc, redA, &w->err);
+    launch_walk_sublists(s, nsub, n, L, kStride, succ, vloc, redA, &w->err);
     const int2 *fin = nullptr;
     int re = launch_rank_reduced(s, nsub, redA, redB, redC, &fin);
     if (re) return fail(PSI_ERR_CUDA, std::string("reduced-list kernel launch: ") + cudaGetErrorString((cudaError_t)re));

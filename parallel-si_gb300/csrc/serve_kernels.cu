@@ -149,24 +149,29 @@ __global__ void k_serve_account(int32_t slots, int32_t event, int4 *__restrict__
 __global__ void k_serve_reset_odd(int32_t np, const int32_t *__restrict__ plist, const int32_t *__restrict__ game_of,
                                   const int32_t *__restrict__ gmask, const unsigned long long *__restrict__ gcount,
                                   const int32_t *__restrict__ off, const int32_t *__restrict__ tgt,
-                                  int32_t *__restrict__ strat)
+                                  int32_t *__restrict__ strat, uint8_t *__restrict__ dirty)
 {
     int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
     int32_t v = plist[i];
     int32_t g = game_of[v];
-    if (g >= 0 && gmask[g] && gcount[g] != 0) strat[v] = tgt[off[v]];
+    if (g < 0 || !gmask[g] || gcount[g] == 0) return;
+    int32_t old = strat[v], first = tgt[off[v]];
+    if (old == first) return;
+    strat[v] = first;
+    if (old >= 0) dirty[old] = 1;   // both parents' child lists change
+    dirty[first] = 1;
 }
 
 }  // namespace
 
 void launch_serve_reset_odd(cudaStream_t s, int32_t np, const int32_t *plist, const int32_t *game_of,
                             const int32_t *gmask, const unsigned long long *gcount, const int32_t *off,
-                            const int32_t *tgt, int32_t *strat)
+                            const int32_t *tgt, int32_t *strat, uint8_t *dirty)
 {
     if (np <= 0) return;
     count_launch();
-    k_serve_reset_odd<<<grid_for(np), kBlock, 0, s>>>(np, plist, game_of, gmask, gcount, off, tgt, strat);
+    k_serve_reset_odd<<<grid_for(np), kBlock, 0, s>>>(np, plist, game_of, gmask, gcount, off, tgt, strat, dirty);
 }
 
 void launch_arena_place(cudaStream_t s, int32_t nu, int32_t k_games, const int32_t *ub, const int32_t *vb,

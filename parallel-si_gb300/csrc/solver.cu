@@ -130,7 +130,7 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
         {(void **)&node_, sizeof(PathNode) * (size_t)cap_n},
         {(void **)&key_, 4 * (size_t)cap_n},
         {(void **)&succ_, 4 * (size_t)capL},
-        {(void **)&hsucc_, 4 * (size_t)cap_sub},
+        {(void **)&dirty_, (size_t)cap_n},
         {(void **)&ulist_, 4 * (size_t)cap_n},
         {(void **)&vloc_, 8 * (size_t)cap_n},
         {(void **)&redA_, 8 * (size_t)cap_sub},
@@ -147,6 +147,7 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
     }
     PSI_CUDA_TRY(cudaMallocHost((void **)&hw_, sizeof(Words)));
     PSI_CUDA_TRY(cudaMemsetAsync(dw_, 0, sizeof(Words), stream_));
+    PSI_CUDA_TRY(cudaMemsetAsync(dirty_, 0, (size_t)cap_n, stream_));
     return PSI_OK;
 }
 
@@ -269,6 +270,7 @@ int Solver::init_strat()
     if (rc) return rc;
     strat_ready_ = true;
     val_ready_ = false;
+    tour_valid_ = false;
     return PSI_OK;
 }
 
@@ -278,6 +280,7 @@ int Solver::reset_opponent_strategy()
     int rc = set_device();
     if (rc) return rc;
     launch_reset_odd(stream_, n_, owner_, off_, tgt_, strat_);
+    tour_valid_ = false;
     return sync_and_check("reset_opponent_strategy");
 }
 
@@ -290,12 +293,20 @@ int Solver::compute_valuation()
     // 1. Euler tour of the sink tree
     phase_begin(PH_TOUR);
     PSI_CUDA_TRY(cudaMemsetAsync(&dw_->ucount, 0, 2 * sizeof(int32_t), stream_));   // ucount, sinkcount
-    launch_tour_build(stream_, n_, strat_, solved_, rev_off_, rev_src_, succ_, vloc_, ulist_, &dw_->sinkcount);
-    launch_pick_heads(stream_, L_, nsub_, stride_, succ_, hsucc_);
+    if (tour_valid_) {
+        // the previous tour, relinked where strategies or solved flags changed
+        // jA_ is free until the cycle pass: it holds the list of dirty parents
+        int te = launch_tour_update(stream_, n_, strat_, solved_, rev_off_, rev_src_, dirty_, succ_, vloc_, ulist_,
+                                    &dw_->sinkcount, reinterpret_cast<int32_t *>(jA_), &dw_->cnt[0]);
+        if (te) return fail(PSI_ERR_CUDA, std::string("tour update: ") + cudaGetErrorString((cudaError_t)te));
+    } else {
+        PSI_CUDA_TRY(cudaMemsetAsync(dirty_, 0, (size_t)n_, stream_));
+        launch_tour_build(stream_, n_, strat_, solved_, rev_off_, rev_src_, succ_, vloc_, ulist_, &dw_->sinkcount);
+    }
     phase_end(PH_TOUR);
     // 2. Helman-JaJa sublists, then the reduced list ranked on the device
     phase_begin(PH_SUBLIST);
-    launch_walk_sublists(stream_, nsub_, n_, L_, succ_, hsucc_, vloc_, redA_, &dw_->err);
+    launch_walk_sublists(stream_, nsub_, n_, L_, stride_, succ_, vloc_, redA_, &dw_->err);
     phase_end(PH_SUBLIST);
     phase_begin(PH_REDUCED);
     const int2 *fin = nullptr;
@@ -325,6 +336,7 @@ int Solver::compute_valuation()
     if (nu > 0) times_.jump_rounds += ceil_log2(nu) + 1;
     times_.evals++;
     val_ready_ = true;
+    tour_valid_ = true;
     return PSI_OK;
 }
 
@@ -334,7 +346,8 @@ int Solver::mark_solved(int32_t player)
     if (!val_ready_) return fail(PSI_ERR_STATE, "mark_solved before compute_valuation");
     int rc = set_device();
     if (rc) return rc;
-    launch_mark_solved(stream_, &dw_->ucount, ulist_, player, st_, solved_, gmask_ ? game_of_ : nullptr, gmask_);
+    launch_mark_solved(stream_, &dw_->ucount, ulist_, player, st_, solved_, dirty_, gmask_ ? game_of_ : nullptr,
+                       gmask_);
     PSI_CUDA_TRY(cudaGetLastError());
     return PSI_OK;   // ordered on the stream before the next call
 }
@@ -350,7 +363,7 @@ int Solver::switch_strategy(int32_t player, int64_t *switched)
     const int32_t np = (player == 0) ? np0_ : np_ - np0_;
     const int32_t *pl = plist_ + (player == 0 ? 0 : np0_);
     launch_switch(stream_, np, pl, player, off_, tgt_, strat_, st_, key_, node_, dw_->sw, game_of_, gcount_, gmask_,
-                  &dw_->err);
+                  dirty_, &dw_->err);
     phase_end(PH_SWITCH);
     rc = sync_and_check("switch_strategy");
     if (rc) return rc;
@@ -473,6 +486,7 @@ int Solver::set_strategy(const int32_t *in)
     PSI_CUDA_TRY(cudaMemcpyAsync(strat_, in, 4 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
     PSI_CUDA_TRY(cudaStreamSynchronize(stream_));
     strat_ready_ = true;
+    tour_valid_ = false;
     return PSI_OK;
 }
 
@@ -703,6 +717,7 @@ int Solver::arena_add(const std::vector<const HostGame *> &gs, const std::vector
     if (e != cudaSuccess) return fail(PSI_ERR_CUDA, std::string("arena_add: ") + cudaGetErrorString(e));
     if (u.max_pri > max_pri_) max_pri_ = u.max_pri;
     set_extent(extent);
+    tour_valid_ = false;
     return sync_and_check("arena_add");
 }
 
@@ -717,6 +732,7 @@ int Solver::arena_remove(int32_t vb, int32_t count, int32_t slot, int32_t extent
     PSI_CUDA_TRY(cudaMemsetAsync(gstate_ + slot, 0, sizeof(int4), stream_));
     PSI_CUDA_TRY(cudaMemsetAsync(&dw_->ucount, 0, sizeof(int32_t), stream_));
     set_extent(extent);
+    tour_valid_ = false;
     return sync_and_check("arena_remove");
 }
 
@@ -764,7 +780,8 @@ int Solver::arena_step(bool reset, std::vector<int32_t> &done, std::vector<int32
     if (!rc) rc = switch_strategy(0, &sw);
     if (rc) return rc;
     if (reset)
-        launch_serve_reset_odd(stream_, np_ - np0_, plist_ + np0_, game_of_, gmask_, gcount_, off_, tgt_, strat_);
+        launch_serve_reset_odd(stream_, np_ - np0_, plist_ + np0_, game_of_, gmask_, gcount_, off_, tgt_, strat_,
+                               dirty_);
     launch_serve_account(stream_, games_, 2, gstate_, gcount_, gmask_);
     std::vector<int4> st((size_t)games_);
     PSI_CUDA_TRY(cudaMemcpyAsync(st.data(), gstate_, sizeof(int4) * (size_t)games_, cudaMemcpyDeviceToHost, stream_));

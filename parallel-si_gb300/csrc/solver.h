@@ -120,6 +120,7 @@ private:
     int64_t m_ = 0, L_ = 0, cap_n_ = 0, cap_m_ = 0;
     int32_t np_ = 0;   // entries in plist_ (Even's np0_ first)
     bool strat_ready_ = false, val_ready_ = false;
+    bool tour_valid_ = false;   // succ holds the last evaluation's tour (dirty_ lists what changed since)
     int last_unreached_ = 0;
 
     // game (device); plist_ lists Even's vertices then Odd's (np0_ of them are Even's)
@@ -139,7 +140,8 @@ private:
     PathNode *node_ = nullptr;   // parent, priority and root-path summary (evaluation snapshot)
     int32_t *key_ = nullptr;   // comparison key per vertex (device_common.cuh)
     // evaluation scratch
-    int32_t *succ_ = nullptr, *hsucc_ = nullptr, *ulist_ = nullptr;
+    int32_t *succ_ = nullptr, *ulist_ = nullptr;
+    uint8_t *dirty_ = nullptr;   // parents whose child lists changed since the last evaluation
     int32_t *rev_off_ = nullptr, *rev_src_ = nullptr;   // distinct in-neighbours (static)
     int2 *vloc_ = nullptr, *redA_ = nullptr, *redB_ = nullptr, *jA_ = nullptr, *jB_ = nullptr;
     int2 *redC_ = nullptr;

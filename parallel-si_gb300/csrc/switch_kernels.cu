@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
                                                    const int32_t *__restrict__ game_of,
                                                    unsigned long long *__restrict__ gcount,
                                                    const int32_t *__restrict__ gmask,
-                                                   uint32_t *__restrict__ err)
+                                                   uint8_t *__restrict__ dirty, uint32_t *__restrict__ err)
 {
     int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     int32_t n_edges = 0, n_loads = 0, moves = 0;
@@ -205,8 +205,10 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
                 }
             }
         }
-        if (moves) {
+        if (moves) {   // strict improvements never return to cur0: cur != cur0
             strat[v] = cur;
+            if (cur0 >= 0) dirty[cur0] = 1;
+            if (cur >= 0) dirty[cur] = 1;
             if (game_of) atomicAdd(&gcount[game_of[v]], (unsigned long long)moves);
         }
     }
@@ -289,12 +291,12 @@ __global__ void k_materialize(int32_t v0, int32_t count, int32_t d, const int32_
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player, const int32_t *off,
                    const int32_t *tgt, int32_t *strat, const int32_t *st, const int32_t *key, const PathNode *node,
                    unsigned long long *stats, const int32_t *game_of, unsigned long long *gcount,
-                   const int32_t *gmask, uint32_t *err)
+                   const int32_t *gmask, uint8_t *dirty, uint32_t *err)
 {
     if (np <= 0) return;
     count_launch();
     k_switch<<<grid_for(np), kBlock, 0, s>>>(np, plist, player, off, tgt, strat, st, key, node, stats, game_of,
-                                             gcount, gmask, err);
+                                             gcount, gmask, dirty, err);
 }
 
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state, unsigned long long *gcount)
