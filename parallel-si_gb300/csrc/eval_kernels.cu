@@ -61,21 +61,6 @@ __device__ __forceinline__ int ceil_log2_dev(int64_t x)
     return r;
 }
 
-// warp-aggregated append of `flag` lanes' values to list[*count ...]
-__device__ __forceinline__ void warp_append(bool flag, int32_t value, int32_t *__restrict__ list,
-                                            int32_t *__restrict__ count)
-{
-    unsigned mask = __ballot_sync(0xffffffffu, flag);
-    if (mask) {
-        int lane = threadIdx.x & 31;
-        int leader = __ffs(mask) - 1;
-        int32_t base = 0;
-        if (lane == leader) base = atomicAdd(count, __popc(mask));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (flag) list[base + __popc(mask & ((1u << lane) - 1))] = value;
-    }
-}
-
 // Block-aggregated append: every thread of the block calls it (no early
 // return before); one atomic on the shared counter per block instead of one
 // per warp, which serialises when most warps append (the sink's children,
@@ -432,7 +417,10 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
     for (int r = 0; r < rounds && na > 0; r++) {
         int32_t *c = &cnt[r % 3];
         if (tid == 0) cnt[(r + 1) % 3] = 0;    // next round's counter (last read two rounds ago)
-        for (int64_t i0 = tid; i0 - (threadIdx.x & 31) < na; i0 += nth) {
+        // block-uniform iterations, so the survivors are appended with one
+        // atomic per block
+        for (int64_t b0 = tid - threadIdx.x; b0 < na; b0 += nth) {
+            const int64_t i0 = b0 + threadIdx.x;
             bool keep = false;
             int32_t u = -1;
             if (i0 < na) {
@@ -448,7 +436,7 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
                     else keep = true;
                 }
             }
-            warp_append(keep, u, next, c);
+            block_append(keep, u, next, c);
         }
         barrier();
         na = *(volatile int32_t *)c;
