@@ -145,15 +145,19 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
                                                    const int32_t *__restrict__ gmask,
                                                    uint8_t *__restrict__ dirty, uint32_t *__restrict__ err)
 {
-    int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    int32_t n_edges = 0, n_loads = 0, moves = 0;
-    int32_t v = (i < np) ? plist[i] : -1;
-    if (v >= 0 && gmask && !gmask[game_of[v]]) v = -1;
-    if (v >= 0) {
+    // Grid-stride over plist with a bounded grid: the work counters are
+    // reduced once per block (a few thousand atomics per launch instead of a
+    // set per 256 vertices).  A thread sees a few dozen vertices at most, so
+    // its own counters fit 32 bits.
+    int32_t t_edges = 0, t_loads = 0, t_changed = 0, t_moves = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t v = plist[i];
+        if (gmask && !gmask[game_of[v]]) continue;
         int32_t cur = strat[v];
         int32_t kc = (cur >= 0) ? key[cur] : 0;
         const int32_t e0 = off[v], e1 = off[v + 1];
-        n_edges = e1 - e0;
+        t_edges += e1 - e0;
+        int32_t moves = 0;
         // Fast pass: successors in batches of kBatch -- all ids, then all
         // keys, before the comparisons (independent gathers in flight per
         // thread).  Equal keys of distinct finite vertices end it; the exact
@@ -197,7 +201,7 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
                 int c;
                 if (ku != kc) c = ku > kc ? 1 : -1;
                 else if (u == cur || key_infinite(ku)) c = 0;
-                else c = compare_equal_keys(node, st, u, cur, n_loads, err);
+                else c = compare_equal_keys(node, st, u, cur, t_loads, err);
                 if ((player == 0 && c > 0) || (player == 1 && c < 0)) {
                     cur = u;
                     kc = ku;
@@ -210,13 +214,15 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
             if (cur0 >= 0) dirty[cur0] = 1;
             if (cur >= 0) dirty[cur] = 1;
             if (game_of) atomicAdd(&gcount[game_of[v]], (unsigned long long)moves);
+            t_changed++;
+            t_moves += moves;
         }
     }
-    typedef cub::BlockReduce<int4, kBlock> Reduce;
+    typedef cub::BlockReduce<longlong4, kBlock> Reduce;
     __shared__ typename Reduce::TempStorage tmp;
-    int4 mine = make_int4(n_edges, n_loads, moves ? 1 : 0, moves);
-    int4 tot = Reduce(tmp).Reduce(mine, [](const int4 &x, const int4 &y) {
-        return make_int4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
+    longlong4 mine = make_longlong4(t_edges, t_loads, t_changed, t_moves);
+    longlong4 tot = Reduce(tmp).Reduce(mine, [](const longlong4 &x, const longlong4 &y) {
+        return make_longlong4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
     });
     if (threadIdx.x == 0) {
         if (tot.x) atomicAdd(&stats[0], (unsigned long long)tot.x);
@@ -286,6 +292,16 @@ __global__ void k_materialize(int32_t v0, int32_t count, int32_t d, const int32_
     }
 }
 
+int switch_grid()
+{
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_switch, kBlock, 0);
+    int b = (sms > 0 ? sms : 1) * (per_sm > 0 ? per_sm : 1) * 4;
+    return b > 0 ? b : 1;
+}
+
 }  // namespace
 
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player, const int32_t *off,
@@ -294,9 +310,13 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
                    const int32_t *gmask, uint8_t *dirty, uint32_t *err)
 {
     if (np <= 0) return;
+    static int blocks = 0;   // resident blocks on the device (same device for the process's solvers)
+    if (blocks == 0) blocks = switch_grid();
+    unsigned g = grid_for(np);
+    g = g < (unsigned)blocks ? g : (unsigned)blocks;
     count_launch();
-    k_switch<<<grid_for(np), kBlock, 0, s>>>(np, plist, player, off, tgt, strat, st, key, node, stats, game_of,
-                                             gcount, gmask, dirty, err);
+    k_switch<<<g, kBlock, 0, s>>>(np, plist, player, off, tgt, strat, st, key, node, stats, game_of, gcount, gmask,
+                                  dirty, err);
 }
 
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state, unsigned long long *gcount)
