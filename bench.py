@@ -179,27 +179,35 @@ def traffic_per_launch(kernel, n):
 
 
 def phase_bytes(phase, n, m, nsub, counters, calls, n_even, n_odd, iters, brs):
-    """Algorithmic bytes per call of a timed phase (roofline)."""
+    """Algorithmic bytes per call of a timed phase: every array element the
+    phase must touch, once, at its size (the per-unit figures are in the
+    design notes)."""
     L = 2 * n + 2
     if phase == "switch":
+        # per vertex of the player: plist, strategy, offsets, key of the current
+        # choice (4 B each); per compared edge: target id and its key (8 B);
+        # per walk step: parent and priority (8 B); per changed vertex: the
+        # strategy write and two dirty flags (6 B)
         sw_calls = max(1, counters["switches"])
         player_vertices = brs * n_odd + iters * n_even
-        total = (n * sw_calls + 12 * player_vertices + 12 * counters["sw_edges"] + 8 * counters["sw_loads"]
-                 + 4 * counters["sw_changed"])
+        total = (16 * player_vertices + 8 * counters["sw_edges"] + 8 * counters["sw_loads"]
+                 + 6 * counters["sw_changed"])
         return total / sw_calls
     if phase == "sublist":
-        return 4 * L + 8 * n + 12 * nsub
+        return 4 * L + 8 * n + 8 * nsub          # successor per node, (sublist, prefix) per vertex, reduced list
     if phase == "tour":
-        return 4 * L + 25 * n + 12 * nsub
+        return 14 * n                             # dirty flags, vloc reset, sink-list scan (strategy, solved)
     if phase == "broadcast":
-        return 37 * n
+        # broadcast: vloc, solved, strategy, priority in; status, PathNode out (37 B);
+        # root-path summaries: status and PathNode in, summary and key out (32 B)
+        return 69 * n
     if phase == "reduced":
         rounds = (nsub - 1).bit_length() + 1
         return 24 * nsub * rounds
     return None
 
 
-KERNEL_OF_PHASE = {"switch": "k_switch", "sublist": "k_walk_sublists", "tour": "k_tour_link",
+KERNEL_OF_PHASE = {"switch": "k_switch", "sublist": "k_walk_sublists", "tour": "k_tour_relink",
                    "broadcast": "k_broadcast_depth", "reduced": "k_rank_reduced", "cycles": "k_cycles"}
 
 

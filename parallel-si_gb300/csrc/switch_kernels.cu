@@ -151,11 +151,11 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
     // its own counters fit 32 bits.
     int32_t t_edges = 0, t_loads = 0, t_changed = 0, t_moves = 0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < np; i += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t v = plist[i];
+        const int32_t v = __ldcs(&plist[i]);   // one-use streams are evict-first: L2 keeps the keys
         if (gmask && !gmask[game_of[v]]) continue;
         int32_t cur = strat[v];
         int32_t kc = (cur >= 0) ? key[cur] : 0;
-        const int32_t e0 = off[v], e1 = off[v + 1];
+        const int32_t e0 = __ldcs(&off[v]), e1 = __ldcs(&off[v + 1]);
         t_edges += e1 - e0;
         int32_t moves = 0;
         // Fast pass: successors in batches of kBatch -- all ids, then all
@@ -169,7 +169,7 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
             const int32_t cnt = min(kBatch, e1 - eb);
             int32_t us[kBatch], ks[kBatch];
 #pragma unroll
-            for (int j = 0; j < kBatch; j++) us[j] = (j < cnt) ? tgt[eb + j] : 0;
+            for (int j = 0; j < kBatch; j++) us[j] = (j < cnt) ? __ldcs(&tgt[eb + j]) : 0;
 #pragma unroll
             for (int j = 0; j < kBatch; j++) ks[j] = (j < cnt) ? key[us[j]] : 0;
 #pragma unroll
