@@ -187,6 +187,37 @@ int psi_batch_solve(psi_batch *b, int32_t *iter_counts, int32_t *br_counts);
 int psi_batch_get_strategy(psi_batch *b, int32_t game, int32_t *out);
 int psi_batch_get_winning(psi_batch *b, int32_t game, int32_t player, int32_t *out, int64_t cap, int64_t *count);
 
+/* ------------------------------------------------------ solution certificate
+ * Checks a solution independently of how it was computed (no counterpart in
+ * the reference).  strategy[n]: each vertex's successor (-1 = the sink, Even
+ * only), as psi_get_strategy returns it; infinite[n]: +1 where Even wins, any
+ * other value where Odd wins, as psi_get_infinite returns it.  The solution is
+ * correct iff every strategy entry is a successor (or the sink for Even), the
+ * winner's strategy stays in its region and the loser cannot leave it
+ * (closure and trap), and every cycle inside Even's region under Even's
+ * strategy has an even top priority (inside Odd's region under Odd's
+ * strategy: odd).  The first two checks take O(n+m) on several threads; the
+ * cycle check decomposes strongly connected components and may need up to
+ * O(n*m) edge visits on adversarial games: work_budget bounds them (<= 0:
+ * unbounded), past it the status is PSI_CHECK_INCOMPLETE (the other checks
+ * passed).  report->vertex is the lowest offending vertex found. */
+enum {
+    PSI_CHECK_OK = 0,
+    PSI_CHECK_BAD_STRATEGY = 1,  /* an entry is not a successor of its vertex */
+    PSI_CHECK_NOT_CLOSED = 2,    /* a winner's strategy leaves the winner's region */
+    PSI_CHECK_NOT_TRAP = 3,      /* a loser's vertex has an edge out of the winner's region */
+    PSI_CHECK_BAD_CYCLE = 4,     /* a cycle of the wrong parity inside a region */
+    PSI_CHECK_INCOMPLETE = 5     /* the cycle check ran out of work_budget */
+};
+typedef struct {
+    int32_t status;       /* PSI_CHECK_* */
+    int32_t reserved;
+    int64_t vertex;       /* offending vertex, or -1 */
+    int64_t edge_visits;  /* work of the cycle check */
+} psi_check_report;
+int psi_check_solution(const psi_game *g, const int32_t *strategy, const int32_t *infinite, int64_t work_budget,
+                       psi_check_report *report);
+
 /* ---------------------------------------------------------------- serving
  * Continuous batching: games are submitted at any time and solved together in
  * one resident arena of vertex and edge ranges on the device.  Each

@@ -8,6 +8,7 @@
 #include <string>
 #include <vector>
 
+#include "check.h"
 #include "game.h"
 #include "kernels.h"
 #include "psi.h"
@@ -466,6 +467,22 @@ int psi_batch_get_winning(psi_batch *b, int32_t game, int32_t player, int32_t *o
         }
     }
     if (count) *count = k;
+    return PSI_OK;
+    PSI_GUARD_END
+}
+
+int psi_check_solution(const psi_game *g, const int32_t *strategy, const int32_t *infinite, int64_t work_budget,
+                       psi_check_report *report)
+{
+    if (!g || !strategy || !infinite || !report) return psi::fail(PSI_ERR_INVALID, "null argument");
+    PSI_GUARD_BEGIN
+    psi::CheckReport r;
+    int rc = psi::check_solution(psi::view_of(g->g), strategy, infinite, work_budget, &r);
+    if (rc) return rc;
+    report->status = r.status;
+    report->reserved = 0;
+    report->vertex = r.vertex;
+    report->edge_visits = r.edge_visits;
     return PSI_OK;
     PSI_GUARD_END
 }

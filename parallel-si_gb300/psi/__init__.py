@@ -21,7 +21,7 @@ def launch_count() -> int:
     """Kernel launches issued by the native library in this process."""
     return int(lib.psi_launch_count())
 
-__all__ = ["Game", "GPUList", "Batch", "Server", "PsiError", "Options", "solve_si", "batch_sizes", "shard_games", "default_options", "version"]
+__all__ = ["Game", "GPUList", "Batch", "Server", "PsiError", "Options", "solve_si", "batch_sizes", "shard_games", "check_solution", "default_options", "version"]
 
 
 def version() -> str:
@@ -281,6 +281,24 @@ def batch_sizes(count: int, n_lo: int, n_hi: int, seed: int = 1) -> np.ndarray:
     out = np.empty(count, np.int32)
     check(lib.psi_generate_batch_sizes(count, n_lo, n_hi, C.c_uint64(seed), ptr(out)))
     return out
+
+
+CHECK_STATUS = {0: "ok", 1: "bad strategy", 2: "not closed", 3: "not a trap", 4: "bad cycle", 5: "incomplete"}
+
+
+def check_solution(game: "Game", strategy, infinite, work_budget: int = 0) -> dict:
+    """Certificate check of a solution (psi_check_solution): strategy entries,
+    closure and trap of both regions, cycle parities inside them.  Returns
+    {"status": name, "code": PSI_CHECK_*, "vertex": v or -1, "edge_visits": k}."""
+    from ._lib import CheckReport
+    st = np.ascontiguousarray(strategy, dtype=np.int32)
+    inf = np.ascontiguousarray(infinite, dtype=np.int32)
+    if len(st) != game.n or len(inf) != game.n:
+        raise ValueError("strategy and infinite need one entry per vertex")
+    r = CheckReport()
+    check(lib.psi_check_solution(game._h, ptr(st), ptr(inf), int(work_budget), C.byref(r)))
+    return {"status": CHECK_STATUS.get(r.status, str(r.status)), "code": r.status, "vertex": r.vertex,
+            "edge_visits": r.edge_visits}
 
 
 def shard_games(footprints, world: int):

@@ -34,6 +34,10 @@ class PsiError(RuntimeError):
         self.message = message
 
 
+class CheckReport(C.Structure):
+    _fields_ = [("status", C.c_int32), ("reserved", C.c_int32), ("vertex", C.c_int64), ("edge_visits", C.c_int64)]
+
+
 class Options(C.Structure):
     _fields_ = [
         ("device", C.c_int32),
@@ -103,6 +107,7 @@ _SIGS = {
     "psi_batch_solve": ([_vp, _vp, _vp], C.c_int),
     "psi_batch_get_strategy": ([_vp, C.c_int32, _vp], C.c_int),
     "psi_batch_get_winning": ([_vp, C.c_int32, C.c_int32, _vp, C.c_int64, _i64p], C.c_int),
+    "psi_check_solution": ([_vp, _vp, _vp, C.c_int64, C.POINTER(CheckReport)], C.c_int),
     "psi_server_create": ([C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Options), _pp], C.c_int),
     "psi_server_destroy": ([_vp], None),
     "psi_server_submit": ([_vp, _vp, _i64p], C.c_int),
