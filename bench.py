@@ -50,7 +50,9 @@ def workload_config(n, m=None, seed=1):
                     f"uniform in [0,n), out-degree uniform in [{DEG_LO},{DEG_HI}], distinct non-self successors",
         "n": n,
         "seed": seed,
-        "step": "one full solve_si (init_strat to convergence), game resident in HBM",
+        "step": "one full solve_si (init_strat to convergence) through psi_solve, game resident in HBM",
+        "solve_loop": "one CUDA graph per solve (device-side loop control); per-phase times for the roofline "
+                      "from the same kernels in the host-driven loop",
         "l2": "inputs larger than L2 (game CSR + solver state ~1.3 GB at n=2^24), no flush",
         "parallelism": "replicas: one independent game per GPU",
     }
@@ -273,7 +275,9 @@ def run_gb300(args, rank, world, local):
     owner, _, _, _ = game.csr()
     n_odd = int(owner.sum())
     n_even = game.n - n_odd
-    solver = psi.GPUList(game, device=local, sublist_len=args.sublist_len)
+    # the product path: psi_solve with default options (the whole solve_si
+    # loop as one CUDA graph, device-side loop control)
+    solver = psi.GPUList(game, device=local, sublist_len=args.sublist_len, graph=int(not args.host_loop))
 
     for _ in range(args.warmup):
         solver.solve()
@@ -294,8 +298,23 @@ def run_gb300(args, rank, world, local):
     dist.barrier()
     ms_max = dist.max(ms)
     iters_all = dist.sum(iters)
-    phases = solver.phase_times()
-    counters = solver.counters()
+
+    # Per-kernel device times for the roofline: a graph records no per-phase
+    # events, so the same kernels are timed once more through the host-driven
+    # loop (psi_options.graph = 0), each phase bracketed by CUDA events on the
+    # solver stream, in a second timed region of K solves.
+    if args.host_loop:
+        phase_solver = solver
+    else:
+        phase_solver = psi.GPUList(game, device=local, sublist_len=args.sublist_len, graph=0)
+        phase_solver.solve()
+        phase_solver.reset_times()
+        for _ in range(args.steps):
+            phase_solver.solve()
+    phases = phase_solver.phase_times()
+    counters = phase_solver.counters()
+    if phase_solver is not solver:
+        phase_solver.close()
     nsub = (2 * game.n + 1 + args.sublist_len - 1) // args.sublist_len + 1
 
     # roofline of the dominant kernel-level phase
@@ -528,6 +547,8 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--sublist-len", type=int, default=64)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--host-loop", action="store_true",
+                    help="time the host-driven solve loop instead of the default one-graph solve")
     ap.add_argument("--workload", choices=("single", "batch", "serve"), default="single",
                     help="single: the 2^24 game (headline); batch: many mixed-size games solved together; "
                          "serve: the same kind of games arriving at a continuous-batching server")

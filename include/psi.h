@@ -88,7 +88,11 @@ typedef struct {
     int32_t sublist_len;     /* Helman-JaJa node stride between sublist heads (default 64,
                                 the reference's gpu_list_ranking.cu:19) */
     int32_t timing;          /* 1: record per-phase CUDA-event times (default 1) */
-    int32_t reserved[4];
+    int32_t graph;           /* 1 (default): psi_solve runs the whole solve_si loop as one CUDA
+                                graph (device-side loop control, no host synchronisation per
+                                step; same results; records no per-phase times); 0: the
+                                host-driven loop */
+    int32_t reserved[3];
 } psi_options;
 
 void psi_options_default(psi_options *opt);

@@ -172,6 +172,7 @@ void psi_options_default(psi_options *opt)
     opt->valuation_mode = PSI_VAL_PATH;
     opt->sublist_len = 64;
     opt->timing = 1;
+    opt->graph = 1;
 }
 
 int psi_solver_create(const psi_game *g, const psi_options *opt, psi_solver **out)
@@ -286,7 +287,8 @@ int psi_solve(psi_solver *s, int32_t reset, int32_t *iter_count, int32_t *br_cou
     if (!iter_count || !br_count) return psi::fail(PSI_ERR_INVALID, "null output");
     *iter_count = 0;
     *br_count = 0;
-    PSI_SOLVER_CALL(s->s->solve(reset, iter_count, br_count, max_evals));
+    PSI_SOLVER_CALL(s->s->use_graph() ? s->s->solve_graph(reset, iter_count, br_count, max_evals)
+                                      : s->s->solve(reset, iter_count, br_count, max_evals));
 }
 
 int psi_solver_times(psi_solver *s, double *eval_ms, double *switch_ms, int64_t *evals, int64_t *switches)

@@ -98,23 +98,29 @@ __global__ void k_init_strat(int32_t n, const int8_t *__restrict__ owner, const 
 }
 
 __global__ void k_reset_odd(int32_t n, const int8_t *__restrict__ owner, const int32_t *__restrict__ off,
-                            const int32_t *__restrict__ tgt, int32_t *__restrict__ strat)
+                            const int32_t *__restrict__ tgt, int32_t *__restrict__ strat,
+                            const int32_t *__restrict__ gate)
 {
-    int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= n) return;
-    if (owner[v] == 1) strat[v] = tgt[off[v]];
+    if (gate && !*gate) return;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        if (owner[v] == 1) strat[v] = tgt[off[v]];
 }
 
 // Up node of v points at its own down node; the down node of a vertex that no
 // parent links (solved, or child of a solved vertex) points back at its up
 // node.  The sink's down node ends the list.
-__global__ void k_tour_init(int32_t n, int32_t *__restrict__ succ, int2 *__restrict__ vloc)
+__global__ void k_tour_init(int32_t n, int32_t *__restrict__ succ, int2 *__restrict__ vloc,
+                            uint8_t *__restrict__ dirty, const int32_t *__restrict__ gate)
 {
-    int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i > n) return;
-    succ[2 * (int64_t)i + 1] = 2 * i;
-    succ[2 * (int64_t)i] = (i == n) ? TOUR_END : 2 * i + 1;
-    if (i < n) vloc[i] = make_int2(-1, 0);
+    if (gate && !*gate) return;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += (int64_t)gridDim.x * blockDim.x) {
+        succ[2 * i + 1] = (int32_t)(2 * i);
+        succ[2 * i] = (i == n) ? TOUR_END : (int32_t)(2 * i + 1);
+        if (i < n) {
+            vloc[i] = make_int2(-1, 0);
+            dirty[i] = 0;   // a full build leaves nothing to relink
+        }
+    }
 }
 
 // Thread p: (a) if p is a live child of the sink, append it to the sink list;
@@ -128,23 +134,26 @@ __global__ void k_tour_init(int32_t n, int32_t *__restrict__ succ, int2 *__restr
 __global__ void k_tour_link(int32_t n, const int32_t *__restrict__ strat, const uint8_t *__restrict__ solved,
                             const int32_t *__restrict__ rev_off, const int32_t *__restrict__ rev_src,
                             int32_t *__restrict__ succ, int32_t *__restrict__ sinklist,
-                            int32_t *__restrict__ sinkcount)
+                            int32_t *__restrict__ sinkcount, const int32_t *__restrict__ gate)
 {
-    int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    bool live = p < n && !solved[p];
-    bool to_sink = live && strat[p] < 0;
-    block_append(to_sink, p, sinklist, sinkcount);
-    if (!live) return;
-    int32_t prev = -1;
-    int32_t e1 = rev_off[p + 1];
-    for (int32_t e = rev_off[p]; e < e1; e++) {
-        int32_t u = rev_src[e];
-        if (strat[u] != p) continue;
-        if (prev < 0) succ[2 * (int64_t)p + 1] = 2 * u + 1;
-        else succ[2 * (int64_t)prev] = 2 * u + 1;
-        prev = u;
+    if (gate && !*gate) return;
+    // grid-stride with block-uniform passes (block_append needs every thread)
+    for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < n; b0 += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t p = (int32_t)(b0 + threadIdx.x);
+        const bool live = p < n && !solved[p];
+        block_append(live && strat[p] < 0, p, sinklist, sinkcount);
+        if (!live) continue;
+        int32_t prev = -1;
+        const int32_t e1 = rev_off[p + 1];
+        for (int32_t e = rev_off[p]; e < e1; e++) {
+            int32_t u = rev_src[e];
+            if (strat[u] != p) continue;
+            if (prev < 0) succ[2 * (int64_t)p + 1] = 2 * u + 1;
+            else succ[2 * (int64_t)prev] = 2 * u + 1;
+            prev = u;
+        }
+        if (prev >= 0) succ[2 * (int64_t)prev] = 2 * p;
     }
-    if (prev >= 0) succ[2 * (int64_t)prev] = 2 * p;
 }
 
 // Incremental tour maintenance.  Between evaluations the tour lists persist
@@ -158,19 +167,23 @@ __global__ void k_tour_link(int32_t n, const int32_t *__restrict__ strat, const 
 // are still exact.  The dirty parents are compacted first (k_dirty_list, which
 // also clears the flags), so the relinking threads are all busy.
 __global__ void k_dirty_list(int32_t n, uint8_t *__restrict__ dirty, int32_t *__restrict__ list,
-                             int32_t *__restrict__ count)
+                             int32_t *__restrict__ count, const int32_t *__restrict__ gate)
 {
-    int32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-    bool take = p < n && dirty[p];
-    if (take) dirty[p] = 0;
-    block_append(take, p, list, count);
+    if (gate && !*gate) return;
+    for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < n; b0 += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t p = (int32_t)(b0 + threadIdx.x);
+        const bool take = p < n && dirty[p];
+        if (take) dirty[p] = 0;
+        block_append(take, p, list, count);
+    }
 }
 
 __global__ void k_tour_relink(const int32_t *__restrict__ list, const int32_t *__restrict__ count,
                               const int32_t *__restrict__ strat, const uint8_t *__restrict__ solved,
                               const int32_t *__restrict__ rev_off, const int32_t *__restrict__ rev_src,
-                              int32_t *__restrict__ succ)
+                              int32_t *__restrict__ succ, const int32_t *__restrict__ gate)
 {
+    if (gate && !*gate) return;
     const int32_t k = *count;
     for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k; i += gridDim.x * blockDim.x) {
         const int32_t p = list[i];
@@ -195,17 +208,22 @@ __global__ void k_tour_relink(const int32_t *__restrict__ list, const int32_t *_
 
 // The sink's live children (the full build collects them in k_tour_link).
 __global__ void k_sink_list(int32_t n, const int32_t *__restrict__ strat, const uint8_t *__restrict__ solved,
-                            int32_t *__restrict__ sinklist, int32_t *__restrict__ sinkcount)
+                            int32_t *__restrict__ sinklist, int32_t *__restrict__ sinkcount,
+                            const int32_t *__restrict__ gate)
 {
-    int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    bool take = v < n && strat[v] < 0 && !solved[v];
-    block_append(take, v, sinklist, sinkcount);
+    if (gate && !*gate) return;
+    for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < n; b0 += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t v = (int32_t)(b0 + threadIdx.x);
+        block_append(v < n && strat[v] < 0 && !solved[v], v, sinklist, sinkcount);
+    }
 }
 
 // sink up -> up(c0) ... down(c0) -> up(c1) ... down(c_last) -> sink down
 __global__ void k_sink_chain(int32_t n, const int32_t *__restrict__ sinklist,
-                             const int32_t *__restrict__ sinkcount, int32_t *__restrict__ succ)
+                             const int32_t *__restrict__ sinkcount, int32_t *__restrict__ succ,
+                             const int32_t *__restrict__ gate)
 {
+    if (gate && !*gate) return;
     int32_t k = *sinkcount;
     if (k == 0 && blockIdx.x == 0 && threadIdx.x == 0) succ[2 * (int64_t)n + 1] = 2 * n;
     for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k; i += gridDim.x * blockDim.x) {
@@ -480,8 +498,9 @@ __global__ void __launch_bounds__(kBlock) k_cycles(const int32_t *__restrict__ u
 __global__ void k_mark_solved(const int32_t *__restrict__ ucount, const int32_t *__restrict__ ulist,
                               int32_t player, const int32_t *__restrict__ st, uint8_t *__restrict__ solved,
                               uint8_t *__restrict__ dirty, const int32_t *__restrict__ game_of,
-                              const int32_t *__restrict__ gmask)
+                              const int32_t *__restrict__ gmask, const int32_t *__restrict__ gate)
 {
+    if (gate && !*gate) return;
     int32_t nu = *ucount;
     int32_t target = (player == 0) ? ST_POS_INF : ST_NEG_INF;
     for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nu; i += gridDim.x * blockDim.x) {
@@ -495,6 +514,23 @@ __global__ void k_mark_solved(const int32_t *__restrict__ ucount, const int32_t 
             dirty[u] = 1;
         }
     }
+}
+
+// Grid for the grid-stride kernels: enough blocks to fill the device a few
+// times over, not one block per 256 items (a kernel whose gate is closed then
+// costs a small launch).
+unsigned capped_grid(int64_t items)
+{
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    unsigned g = grid_for(items);
+    unsigned cap = 16u * (unsigned)sms;
+    return g < cap ? g : cap;
 }
 
 int device_blocks(const void *kernel, int block)
@@ -517,6 +553,8 @@ static std::atomic<long long> g_launches{0};
 
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+void add_launches(long long k) { g_launches.fetch_add(k, std::memory_order_relaxed); }
+
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 void launch_init_strat(cudaStream_t s, int32_t n, const int8_t *owner, const int32_t *off,
@@ -526,43 +564,45 @@ void launch_init_strat(cudaStream_t s, int32_t n, const int8_t *owner, const int
     k_init_strat<<<grid_for(n), kBlock, 0, s>>>(n, owner, off, tgt, strat, st);
 }
 
-void launch_reset_odd(cudaStream_t s, int32_t n, const int8_t *owner, const int32_t *off,
-                      const int32_t *tgt, int32_t *strat)
+void launch_reset_odd(cudaStream_t s, int32_t n, const int8_t *owner, const int32_t *off, const int32_t *tgt,
+                      int32_t *strat, const int32_t *gate)
 {
     count_launch();
-    k_reset_odd<<<grid_for(n), kBlock, 0, s>>>(n, owner, off, tgt, strat);
+    k_reset_odd<<<capped_grid(n), kBlock, 0, s>>>(n, owner, off, tgt, strat, gate);
 }
 
 void launch_tour_build(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
                        const int32_t *rev_off, const int32_t *rev_src, int32_t *succ, int2 *vloc,
-                       int32_t *sinklist, int32_t *sinkcount)
+                       int32_t *sinklist, int32_t *sinkcount, uint8_t *dirty, const int32_t *gate)
 {
     count_launch();
-    k_tour_init<<<grid_for((int64_t)n + 1), kBlock, 0, s>>>(n, succ, vloc);
+    k_tour_init<<<capped_grid((int64_t)n + 1), kBlock, 0, s>>>(n, succ, vloc, dirty, gate);
     count_launch();
-    k_tour_link<<<grid_for(n), kBlock, 0, s>>>(n, strat, solved, rev_off, rev_src, succ, sinklist, sinkcount);
+    k_tour_link<<<capped_grid(n), kBlock, 0, s>>>(n, strat, solved, rev_off, rev_src, succ, sinklist, sinkcount,
+                                                  gate);
     count_launch();
     unsigned g = grid_for(n);
-    k_sink_chain<<<g < 1216u ? g : 1216u, kBlock, 0, s>>>(n, sinklist, sinkcount, succ);
+    k_sink_chain<<<g < 1216u ? g : 1216u, kBlock, 0, s>>>(n, sinklist, sinkcount, succ, gate);
 }
 
 int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
                        const int32_t *rev_off, const int32_t *rev_src, uint8_t *dirty, int32_t *succ, int2 *vloc,
-                       int32_t *sinklist, int32_t *sinkcount, int32_t *dlist, int32_t *dcount)
+                       int32_t *sinklist, int32_t *sinkcount, int32_t *dlist, int32_t *dcount,
+                       const int32_t *gate)
 {
     cudaError_t e = cudaMemsetAsync(vloc, 0xff, 8 * (size_t)n, s);   // (-1, -1): on no walked sublist
     if (e == cudaSuccess) e = cudaMemsetAsync(dcount, 0, sizeof(int32_t), s);
     if (e != cudaSuccess) return (int)e;
     count_launch();
-    k_dirty_list<<<grid_for(n), kBlock, 0, s>>>(n, dirty, dlist, dcount);
+    k_dirty_list<<<capped_grid(n), kBlock, 0, s>>>(n, dirty, dlist, dcount, gate);
     count_launch();
     unsigned g = grid_for(n);
     g = g < 1216u ? g : 1216u;
-    k_tour_relink<<<g, kBlock, 0, s>>>(dlist, dcount, strat, solved, rev_off, rev_src, succ);
+    k_tour_relink<<<g, kBlock, 0, s>>>(dlist, dcount, strat, solved, rev_off, rev_src, succ, gate);
     count_launch();
-    k_sink_list<<<grid_for(n), kBlock, 0, s>>>(n, strat, solved, sinklist, sinkcount);
+    k_sink_list<<<capped_grid(n), kBlock, 0, s>>>(n, strat, solved, sinklist, sinkcount, gate);
     count_launch();
-    k_sink_chain<<<g, kBlock, 0, s>>>(n, sinklist, sinkcount, succ);
+    k_sink_chain<<<g, kBlock, 0, s>>>(n, sinklist, sinkcount, succ, gate);
     return 0;
 }
 
@@ -632,10 +672,10 @@ int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, c
 
 void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, int32_t player,
                         const int32_t *st, uint8_t *solved, uint8_t *dirty, const int32_t *game_of,
-                        const int32_t *gmask)
+                        const int32_t *gmask, const int32_t *gate)
 {
     count_launch();
-    k_mark_solved<<<608, kBlock, 0, s>>>(ucount, ulist, player, st, solved, dirty, game_of, gmask);
+    k_mark_solved<<<608, kBlock, 0, s>>>(ucount, ulist, player, st, solved, dirty, game_of, gmask, gate);
 }
 
 }  // namespace psi

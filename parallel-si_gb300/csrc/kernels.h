@@ -10,8 +10,13 @@ namespace psi {
 
 struct PathNode;   // device_common.cuh
 
+// Launchers taking `gate` (a device word, nullptr = always) enqueue kernels
+// that return at once while *gate == 0: the graph-driven solve loop enqueues
+// every kernel of a step and lets the device decide which ones work.
+
 // Process-wide count of kernel launches issued by this library.
 void count_launch();
+void add_launches(long long k);
 long long launch_count();
 
 // ---- one-time game set-up: distinct in-neighbours of every vertex in
@@ -33,7 +38,7 @@ int select_winning(cudaStream_t s, int32_t n, int32_t player, const int32_t *st,
 void launch_init_strat(cudaStream_t s, int32_t n, const int8_t *owner, const int32_t *off,
                        const int32_t *tgt, int32_t *strat, int32_t *st);
 void launch_reset_odd(cudaStream_t s, int32_t n, const int8_t *owner, const int32_t *off,
-                      const int32_t *tgt, int32_t *strat);
+                      const int32_t *tgt, int32_t *strat, const int32_t *gate = nullptr);
 
 // ---- evaluation (gpu_list_ranking.cu:52-277)
 // Euler tour of the sink tree, built from scratch.  rev_off/rev_src: distinct
@@ -41,14 +46,15 @@ void launch_reset_odd(cudaStream_t s, int32_t n, const int8_t *owner, const int3
 // n entries.
 void launch_tour_build(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
                        const int32_t *rev_off, const int32_t *rev_src, int32_t *succ, int2 *vloc,
-                       int32_t *sinklist, int32_t *sinkcount);
+                       int32_t *sinklist, int32_t *sinkcount, uint8_t *dirty, const int32_t *gate = nullptr);
 // The same tour brought up to date from the previous one: only the parents
 // flagged in dirty (cleared here; dlist: n entries of scratch, dcount: one
 // counter) are relinked and the sink's list is rebuilt.  Returns a
 // cudaError_t value.
 int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
                        const int32_t *rev_off, const int32_t *rev_src, uint8_t *dirty, int32_t *succ, int2 *vloc,
-                       int32_t *sinklist, int32_t *sinkcount, int32_t *dlist, int32_t *dcount);
+                       int32_t *sinklist, int32_t *sinkcount, int32_t *dlist, int32_t *dcount,
+                       const int32_t *gate = nullptr);
 // Sublist walks; heads are the nodes j*stride (j < nsub-1) and the list start.
 void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, int32_t stride, const int32_t *succ,
                           int2 *vloc, int2 *red, uint32_t *err);
@@ -75,7 +81,7 @@ int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, c
 // Newly solved vertices are flagged in dirty (their children leave the tour).
 void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, int32_t player,
                         const int32_t *st, uint8_t *solved, uint8_t *dirty, const int32_t *game_of = nullptr,
-                        const int32_t *gmask = nullptr);
+                        const int32_t *gmask = nullptr, const int32_t *gate = nullptr);
 
 // ---- all-switches (gpu_parity.cu:191-317, cpu_parity.cpp:154-263)
 // Switches the np vertices listed in plist (all owned by `player`).
@@ -86,7 +92,8 @@ void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ul
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player,
                    const int32_t *off, const int32_t *tgt, int32_t *strat, const int32_t *st,
                    const int32_t *key, const PathNode *node, unsigned long long *stats, const int32_t *game_of,
-                   unsigned long long *gcount, const int32_t *gmask, uint8_t *dirty, uint32_t *err);
+                   unsigned long long *gcount, const int32_t *gmask, uint8_t *dirty, uint32_t *err,
+                   const int32_t *gate = nullptr);
 // ---- batches: per-game accounting of solve_si (state[g] = brs, iters,
 // odd_done, done; gcount[g] = strict improvements of the last switch step)
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state,

@@ -54,6 +54,7 @@ int Solver::create(const CsrView &g, const psi_options &opt, Solver **out)
     s->device_ = opt.device;
     s->timing_ = opt.timing != 0;
     s->stride_ = opt.sublist_len;
+    s->use_graph_ = opt.graph != 0;
     rc = s->alloc_arrays(g.n, g.m);
     if (!rc) rc = s->upload_game(g);
     if (rc) {
@@ -139,6 +140,7 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
         {(void **)&jA_, 8 * (size_t)cap_n},
         {(void **)&jB_, 8 * (size_t)cap_n},
         {(void **)&dw_, sizeof(Words)},
+        {(void **)&ctl_, sizeof(GraphCtl)},
     };
     for (const auto &a : arrays) {
         cudaError_t e = cudaMalloc(a.ptr, a.bytes ? a.bytes : 16);
@@ -184,6 +186,8 @@ Solver::~Solver()
 {
     cudaSetDevice(device_);
     if (stream_) cudaStreamSynchronize(stream_);
+    if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+    if (graph_) cudaGraphDestroy(graph_);
     for (void *p : allocs_) cudaFree(p);
     if (hw_) cudaFreeHost(hw_);
     for (auto &p : ph_) {
@@ -300,8 +304,8 @@ int Solver::compute_valuation()
                                     &dw_->sinkcount, reinterpret_cast<int32_t *>(jA_), &dw_->cnt[0]);
         if (te) return fail(PSI_ERR_CUDA, std::string("tour update: ") + cudaGetErrorString((cudaError_t)te));
     } else {
-        PSI_CUDA_TRY(cudaMemsetAsync(dirty_, 0, (size_t)n_, stream_));
-        launch_tour_build(stream_, n_, strat_, solved_, rev_off_, rev_src_, succ_, vloc_, ulist_, &dw_->sinkcount);
+        launch_tour_build(stream_, n_, strat_, solved_, rev_off_, rev_src_, succ_, vloc_, ulist_, &dw_->sinkcount,
+                          dirty_);
     }
     phase_end(PH_TOUR);
     // 2. Helman-JaJa sublists, then the reduced list ranked on the device

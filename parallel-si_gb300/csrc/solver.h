@@ -28,6 +28,16 @@ struct SolverTimes {
     int64_t unreached = 0, jump_rounds = 0;
 };
 
+// Control words of the graph-driven solve loop (solver_graph.cu), on the device.
+struct GraphCtl {
+    enum { kRunning = 0, kConverged = 1, kEvalCap = 2, kRunaway = 3 };
+    int32_t full = 0;    // gate: the next evaluation builds the tour from scratch
+    int32_t incr = 0;    // gate: the next evaluation updates the previous tour
+    int32_t even = 0;    // gate: Even's mark_solved and switch run in this step
+    int32_t reset = 0;   // gate: Odd's strategy is reset before the next evaluation
+    int32_t brs = 0, iters = 0, stop = kRunning, max_evals = 0;
+};
+
 class Solver {
 public:
     static int create(const CsrView &g, const psi_options &opt, Solver **out);
@@ -58,6 +68,9 @@ public:
     int get_depth(int32_t *out);
     int get_valuation(int32_t v0, int32_t count, int32_t *out);
     int solve(int32_t reset, int32_t *iters, int32_t *brs, int64_t max_evals);
+    // The same loop as one CUDA graph launch (solver_graph.cu).
+    int solve_graph(int32_t reset, int32_t *iters, int32_t *brs, int64_t max_evals);
+    bool use_graph() const { return use_graph_; }
 
     int32_t n() const { return n_; }
     int64_t m() const { return m_; }
@@ -99,6 +112,8 @@ private:
     int init_arena(int32_t slots);
     void set_extent(int32_t n);
     int sync_and_check(const char *what);
+    int enqueue_step(cudaGraphConditionalHandle loop, bool reset);
+    int build_graph(bool reset);
     int get_range(const int32_t *src, int64_t v0, int64_t count, int32_t *out);
     int set_device();
 
@@ -154,6 +169,12 @@ private:
         int32_t cnt[3];             // active-list counters of the cycle kernel
     };
     Words *dw_ = nullptr, *hw_ = nullptr;
+    // graph-driven solve loop
+    bool use_graph_ = false, graph_reset_ = false;
+    GraphCtl *ctl_ = nullptr;
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t graph_exec_ = nullptr;
+    long long graph_step_launches_ = 0;   // kernels per loop pass (for the launch counter)
     std::vector<void *> allocs_;
 };
 

@@ -1,0 +1,174 @@
+// solver_graph.cu -- solve_si (main.cpp:20-55) as one CUDA graph.
+//
+// The host-driven loop (Solver::solve) synchronises after every evaluation
+// and every switch step to read the switch count that decides what comes
+// next.  Here the decision moves to the device: one SI step -- an optional
+// reset of Odd's strategy, an evaluation, mark_solved(Odd) and Odd's switch,
+// then mark_solved(Even) and Even's switch -- is captured once as the body of
+// a conditional "while" node, and small control kernels read the switch
+// counts and set gate words (which kernels of the next pass do work) and,
+// when the loop is over, the node's condition.  A whole solve is one graph
+// launch and one synchronisation.  The kernels are the same as the host
+// loop's; gated ones return at once when their gate word is 0.
+#include <string>
+
+#include "device_common.cuh"
+#include "kernels.h"
+#include "psi_internal.h"
+#include "solver.h"
+
+namespace psi {
+
+namespace {
+
+// after an evaluation: the tour is valid for updates, one more evaluation
+__global__ void k_ctl_evaluated(GraphCtl *c)
+{
+    c->full = 0;
+    c->incr = 1;
+    c->reset = 0;
+    c->brs++;
+}
+
+// after Odd's switch: Even moves in this step iff Odd made no strict improvement
+__global__ void k_ctl_odd(GraphCtl *c, const unsigned long long *sw) { c->even = (sw[3] == 0) ? 1 : 0; }
+
+// after Even's (gated) switch: iteration count, termination, reset, caps
+__global__ void k_ctl_even(GraphCtl *c, const unsigned long long *sw, cudaGraphConditionalHandle loop,
+                           int32_t reset_variant, int32_t guard)
+{
+    bool go = true;
+    if (c->even) {
+        c->iters++;
+        if (sw[3] == 0) {
+            c->stop = GraphCtl::kConverged;
+            go = false;
+        } else if (reset_variant) {   // main.cpp:25-26: Odd starts the next iteration afresh
+            c->reset = 1;
+            c->full = 1;              // many Odd strategies change: rebuild the tour
+            c->incr = 0;
+        }
+    }
+    if (go && c->max_evals > 0 && c->brs >= c->max_evals) {
+        c->stop = GraphCtl::kEvalCap;
+        go = false;
+    }
+    if (go && c->brs >= guard) {
+        c->stop = GraphCtl::kRunaway;
+        go = false;
+    }
+    if (!go) cudaGraphSetConditional(loop, 0);
+}
+
+// A solve that needs this many evaluations is treated as a fault (the loop
+// runs on the device and must end by itself).
+constexpr int32_t kEvalGuard = 1 << 20;
+
+}  // namespace
+
+// One SI step on the stream, no synchronisation (captured into the loop body).
+int Solver::enqueue_step(cudaGraphConditionalHandle loop, bool reset)
+{
+    launch_reset_odd(stream_, n_, owner_, off_, tgt_, strat_, &ctl_->reset);
+    // evaluation (as compute_valuation, with both tour paths gated)
+    PSI_CUDA_TRY(cudaMemsetAsync(&dw_->ucount, 0, 2 * sizeof(int32_t), stream_));   // ucount, sinkcount
+    launch_tour_build(stream_, n_, strat_, solved_, rev_off_, rev_src_, succ_, vloc_, ulist_, &dw_->sinkcount, dirty_,
+                      &ctl_->full);
+    int ce = launch_tour_update(stream_, n_, strat_, solved_, rev_off_, rev_src_, dirty_, succ_, vloc_, ulist_,
+                                &dw_->sinkcount, reinterpret_cast<int32_t *>(jA_), &dw_->cnt[0], &ctl_->incr);
+    if (ce) return fail(PSI_ERR_CUDA, std::string("tour update: ") + cudaGetErrorString((cudaError_t)ce));
+    launch_walk_sublists(stream_, nsub_, n_, L_, stride_, succ_, vloc_, redA_, &dw_->err);
+    const int2 *fin = nullptr;
+    ce = launch_rank_reduced(stream_, nsub_, redA_, redB_, redC_, &fin);
+    if (ce) return fail(PSI_ERR_CUDA, std::string("reduced-list kernel: ") + cudaGetErrorString((cudaError_t)ce));
+    launch_broadcast_depth(stream_, n_, vloc_, fin, strat_, pri_, solved_, st_, node_, ulist_, &dw_->ucount);
+    launch_rootinfo(stream_, n_, st_, node_, key_, &dw_->err);
+    int32_t *la = reinterpret_cast<int32_t *>(vloc_), *lb = la + n_;
+    ce = launch_cycles(stream_, &dw_->ucount, ulist_, strat_, pri_, solved_, st_, key_, jA_, jB_, la, lb, dw_->cnt,
+                       &dw_->err);
+    if (ce) return fail(PSI_ERR_CUDA, std::string("cycle kernel: ") + cudaGetErrorString((cudaError_t)ce));
+    count_launch();
+    k_ctl_evaluated<<<1, 1, 0, stream_>>>(ctl_);
+    // Odd: mark_solved(1), switch(1)
+    launch_mark_solved(stream_, &dw_->ucount, ulist_, 1, st_, solved_, dirty_);
+    PSI_CUDA_TRY(cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_));
+    launch_switch(stream_, np_ - np0_, plist_ + np0_, 1, off_, tgt_, strat_, st_, key_, node_, dw_->sw, nullptr,
+                  nullptr, nullptr, dirty_, &dw_->err);
+    count_launch();
+    k_ctl_odd<<<1, 1, 0, stream_>>>(ctl_, dw_->sw);
+    // Even, when Odd made no strict improvement: mark_solved(0), switch(0)
+    launch_mark_solved(stream_, &dw_->ucount, ulist_, 0, st_, solved_, dirty_, nullptr, nullptr, &ctl_->even);
+    PSI_CUDA_TRY(cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_));
+    launch_switch(stream_, np0_, plist_, 0, off_, tgt_, strat_, st_, key_, node_, dw_->sw, nullptr, nullptr, nullptr,
+                  dirty_, &dw_->err, &ctl_->even);
+    count_launch();
+    k_ctl_even<<<1, 1, 0, stream_>>>(ctl_, dw_->sw, loop, reset ? 1 : 0, kEvalGuard);
+    PSI_CUDA_TRY(cudaGetLastError());
+    return PSI_OK;
+}
+
+int Solver::build_graph(bool reset)
+{
+    if (graph_exec_) {
+        cudaGraphExecDestroy(graph_exec_);
+        graph_exec_ = nullptr;
+    }
+    if (graph_) {
+        cudaGraphDestroy(graph_);
+        graph_ = nullptr;
+    }
+    PSI_CUDA_TRY(cudaGraphCreate(&graph_, 0));
+    cudaGraphConditionalHandle loop;
+    PSI_CUDA_TRY(cudaGraphConditionalHandleCreate(&loop, graph_, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = loop;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    PSI_CUDA_TRY(cudaGraphAddNode(&node, graph_, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    PSI_CUDA_TRY(cudaStreamBeginCaptureToGraph(stream_, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const long long before = launch_count();
+    int rc = enqueue_step(loop, reset);
+    graph_step_launches_ = launch_count() - before;
+    cudaGraph_t captured = nullptr;
+    cudaError_t e = cudaStreamEndCapture(stream_, &captured);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(PSI_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    PSI_CUDA_TRY(cudaGraphInstantiate(&graph_exec_, graph_, 0));
+    graph_reset_ = reset;
+    return PSI_OK;
+}
+
+// solve_si as one graph launch; the same results and counts as solve().
+int Solver::solve_graph(int32_t reset, int32_t *iters, int32_t *brs, int64_t max_evals)
+{
+    int rc = init_strat();
+    if (rc) return rc;
+    if (!graph_exec_ || graph_reset_ != (reset != 0)) {
+        rc = build_graph(reset != 0);
+        if (rc) return rc;
+    }
+    GraphCtl init;
+    init.full = 1;   // init_strat: the first evaluation builds the tour
+    init.max_evals = max_evals > 0 && max_evals < INT32_MAX ? (int32_t)max_evals : 0;
+    PSI_CUDA_TRY(cudaMemcpyAsync(ctl_, &init, sizeof init, cudaMemcpyHostToDevice, stream_));
+    PSI_CUDA_TRY(cudaGraphLaunch(graph_exec_, stream_));
+    GraphCtl out;
+    PSI_CUDA_TRY(cudaMemcpyAsync(&out, ctl_, sizeof out, cudaMemcpyDeviceToHost, stream_));
+    rc = sync_and_check("solve (graph)");
+    if (rc) return rc;
+    *iters = out.iters;
+    *brs = out.brs;
+    add_launches(graph_step_launches_ * out.brs);   // every pass launches each kernel of the body once
+    times_.evals += out.brs;
+    times_.switches += out.brs + out.iters;
+    val_ready_ = true;
+    tour_valid_ = true;
+    if (out.stop == GraphCtl::kEvalCap) return fail(PSI_ERR_LIMIT, "evaluation cap reached");
+    if (out.stop != GraphCtl::kConverged) return fail(PSI_ERR_LIMIT, "graph solve loop stopped by its guard");
+    return PSI_OK;
+}
+
+}  // namespace psi

@@ -143,8 +143,10 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
                                                    const int32_t *__restrict__ game_of,
                                                    unsigned long long *__restrict__ gcount,
                                                    const int32_t *__restrict__ gmask,
-                                                   uint8_t *__restrict__ dirty, uint32_t *__restrict__ err)
+                                                   uint8_t *__restrict__ dirty, uint32_t *__restrict__ err,
+                                                   const int32_t *__restrict__ gate)
 {
+    if (gate && !*gate) return;
     // Grid-stride over plist with a bounded grid: the work counters are
     // reduced once per block (a few thousand atomics per launch instead of a
     // set per 256 vertices).  A thread sees a few dozen vertices at most, so
@@ -307,7 +309,7 @@ int switch_grid()
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player, const int32_t *off,
                    const int32_t *tgt, int32_t *strat, const int32_t *st, const int32_t *key, const PathNode *node,
                    unsigned long long *stats, const int32_t *game_of, unsigned long long *gcount,
-                   const int32_t *gmask, uint8_t *dirty, uint32_t *err)
+                   const int32_t *gmask, uint8_t *dirty, uint32_t *err, const int32_t *gate)
 {
     if (np <= 0) return;
     static int blocks = 0;   // resident blocks on the device (same device for the process's solvers)
@@ -316,7 +318,7 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
     g = g < (unsigned)blocks ? g : (unsigned)blocks;
     count_launch();
     k_switch<<<g, kBlock, 0, s>>>(np, plist, player, off, tgt, strat, st, key, node, stats, game_of, gcount, gmask,
-                                  dirty, err);
+                                  dirty, err, gate);
 }
 
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state, unsigned long long *gcount)

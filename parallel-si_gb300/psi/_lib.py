@@ -44,7 +44,8 @@ class Options(C.Structure):
         ("valuation_mode", C.c_int32),
         ("sublist_len", C.c_int32),
         ("timing", C.c_int32),
-        ("reserved", C.c_int32 * 4),
+        ("graph", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
 
 

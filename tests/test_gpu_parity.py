@@ -86,3 +86,37 @@ def test_gpu_solver_from_host_csr_matches_game_handle():
         assert np.array_equal(a.get_winning(p), b.get_winning(p))
     a.close()
     b.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fam,n,seed,reset", [("c1", 10000, 81, False), ("c2", 200000, 82, False),
+                                              ("c3", 50000, 83, False), ("smallpri", 30000, 84, False),
+                                              ("c2", 40000, 85, True), ("ring10", 10, 0, False)])
+def test_gpu_graph_solve_matches_host_loop(fam, n, seed, reset):
+    """psi_solve as one CUDA graph (device-side loop control) gives the host
+    loop's counts, strategies and regions."""
+    from games import ring10
+    g = ring10() if fam == "ring10" else make(fam, n, seed)
+    a = psi.GPUList(g, graph=0)
+    b = psi.GPUList(g, graph=1)
+    assert a.solve(reset=reset) == b.solve(reset=reset)
+    assert np.array_equal(a.get_strategy(), b.get_strategy())
+    assert np.array_equal(a.get_infinite(), b.get_infinite())
+    # the graph is reused by the next solve, and rebuilt when the variant changes
+    assert b.solve(reset=reset) == a.solve(reset=reset)
+    assert b.solve(reset=not reset) == a.solve(reset=not reset)
+    assert np.array_equal(a.get_strategy(), b.get_strategy())
+    a.close()
+    b.close()
+
+
+@pytest.mark.gpu
+def test_gpu_graph_solve_evaluation_cap():
+    g = make("c2", 50000, 86)
+    s = psi.GPUList(g, graph=1)
+    it, br = s.solve()
+    with pytest.raises(psi.PsiError) as e:
+        s.solve(max_evals=br - 1)
+    assert e.value.code == 8   # PSI_ERR_LIMIT
+    assert s.solve() == (it, br)
+    s.close()
