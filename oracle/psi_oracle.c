@@ -51,25 +51,26 @@ static int *row(const oracle_t *o, int v) { return o->vals + (int64_t)v * rowsz(
 oracle_t *oracle_create(int n, const int *owner, const int *priority,
                         const int *offsets, const int *targets)
 {
-    if (n <= 0) return NULL;
+    if (n < 0) return NULL;                       /* n = 0: the empty game (game.cpp:56 with no lines) */
     oracle_t *o = (oracle_t *)calloc(1, sizeof(oracle_t));
     if (!o) return NULL;
+    const int n1 = n > 0 ? n : 1;                 /* every array gets at least one slot */
     o->n = n;
     o->m = offsets[n];
     int mp = 0;                                   /* game.cpp:18-31: max_pri >= 0 */
     for (int v = 0; v < n; v++)
         if (priority[v] > mp) mp = priority[v];
     o->max_pri = mp;
-    o->owner = (int *)malloc(sizeof(int) * n);
-    o->priority = (int *)malloc(sizeof(int) * n);
+    o->owner = (int *)malloc(sizeof(int) * n1);
+    o->priority = (int *)malloc(sizeof(int) * n1);
     o->offsets = (int *)malloc(sizeof(int) * (n + 1));
     o->targets = (int *)malloc(sizeof(int) * (o->m > 0 ? o->m : 1));
-    o->strat = (int *)calloc(n, sizeof(int));
-    o->infinite = (int *)calloc(n, sizeof(int));
-    o->solved = (int *)calloc(n, sizeof(int));
-    o->done = (int *)calloc(n, sizeof(int));
-    o->stack = (int *)malloc(sizeof(int) * n);
-    o->vals = (int *)calloc((size_t)n * (size_t)rowsz(o), sizeof(int));
+    o->strat = (int *)calloc(n1, sizeof(int));
+    o->infinite = (int *)calloc(n1, sizeof(int));
+    o->solved = (int *)calloc(n1, sizeof(int));
+    o->done = (int *)calloc(n1, sizeof(int));
+    o->stack = (int *)malloc(sizeof(int) * n1);
+    o->vals = (int *)calloc((size_t)n1 * (size_t)rowsz(o), sizeof(int));
     o->zero_val = (int *)calloc((size_t)rowsz(o), sizeof(int));
     if (!o->owner || !o->priority || !o->offsets || !o->targets || !o->strat ||
         !o->infinite || !o->solved || !o->done || !o->stack || !o->vals || !o->zero_val) {

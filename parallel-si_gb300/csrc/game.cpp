@@ -247,8 +247,9 @@ std::pair<int64_t, int> first_bad_vertex(int64_t lo, int64_t hi, const int32_t *
 int validate_csr(int32_t n, const int32_t *owner, const int32_t *priority, const int32_t *offsets,
                  const int32_t *targets)
 {
-    if (n <= 0) return fail(PSI_ERR_INVALID, "game has no vertices");
+    if (n < 0) return fail(PSI_ERR_INVALID, "negative vertex count");
     if (offsets[0] != 0) return fail(PSI_ERR_INVALID, "offsets[0] must be 0");
+    if (n == 0) return PSI_OK;   // the empty game (offsets = {0})
     // vertex checks per chunk; the lowest failing vertex decides the message
     std::mutex mu;
     std::pair<int64_t, int> worst{-1, 0};

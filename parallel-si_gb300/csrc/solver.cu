@@ -46,7 +46,7 @@ int check_options(const psi_options &opt)
 int Solver::create(const CsrView &g, const psi_options &opt, Solver **out)
 {
     *out = nullptr;
-    if (g.n <= 0) return fail(PSI_ERR_INVALID, "game has no vertices");
+    if (g.n < 0) return fail(PSI_ERR_INVALID, "negative vertex count");   // n = 0: the empty game
     if (2 * (int64_t)g.n + 2 > INT32_MAX) return fail(PSI_ERR_TOO_LARGE, "n too large for int32 tour ids");
     int rc = check_options(opt);
     if (rc) return rc;
