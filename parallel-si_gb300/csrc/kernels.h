@@ -14,6 +14,11 @@ struct PathNode;   // device_common.cuh
 // that return at once while *gate == 0: the graph-driven solve loop enqueues
 // every kernel of a step and lets the device decide which ones work.
 
+// Stream-ordered allocation from the library's memory pool on the current
+// device (pool.cu); release with cudaFreeAsync on a stream.  Freed blocks
+// stay cached in the pool for later allocations of the process.
+cudaError_t device_alloc(void **p, size_t bytes, cudaStream_t s);
+
 // Process-wide count of kernel launches issued by this library.
 void count_launch();
 void add_launches(long long k);

@@ -92,11 +92,11 @@ int build_reverse_csr(cudaStream_t s, int32_t n, int64_t m, const int32_t *off, 
     e = cub::DeviceScan::ExclusiveSum(nullptr, tmp_scan, (int32_t *)nullptr, (int32_t *)nullptr, n + 1, s);
     if (e) return e;
     size_t tmp_bytes = std::max(tmp_sort, std::max(tmp_uniq, tmp_scan));
-    if ((e = cudaMallocAsync((void **)&k0, 8 * (size_t)m, s))) goto out;
-    if ((e = cudaMallocAsync((void **)&k1, 8 * (size_t)m, s))) goto out;
-    if ((e = cudaMallocAsync((void **)&nuniq, sizeof(int32_t), s))) goto out;
-    if ((e = cudaMallocAsync((void **)&deg, 4 * ((size_t)n + 1), s))) goto out;
-    if ((e = cudaMallocAsync(&tmp, tmp_bytes, s))) goto out;
+    if ((e = device_alloc((void **)&k0, 8 * (size_t)m, s))) goto out;
+    if ((e = device_alloc((void **)&k1, 8 * (size_t)m, s))) goto out;
+    if ((e = device_alloc((void **)&nuniq, sizeof(int32_t), s))) goto out;
+    if ((e = device_alloc((void **)&deg, 4 * ((size_t)n + 1), s))) goto out;
+    if ((e = device_alloc(&tmp, tmp_bytes, s))) goto out;
     count_launch();
     k_edge_keys<<<grid_for(n), kBlock, 0, s>>>(n, off, tgt, k0);
     {
@@ -140,7 +140,7 @@ int partition_players(cudaStream_t s, int32_t n, const int8_t *owner, int32_t *p
     cudaError_t e = cub::DevicePartition::If(nullptr, bytes, ids, plist, n_even, n, even, s);
     if (e) return e;
     void *tmp = nullptr;
-    if ((e = cudaMallocAsync(&tmp, bytes, s))) return e;
+    if ((e = device_alloc(&tmp, bytes, s))) return e;
     e = cub::DevicePartition::If(tmp, bytes, ids, plist, n_even, n, even, s);
     cudaFreeAsync(tmp, s);
     return e;
@@ -154,7 +154,7 @@ int select_winning(cudaStream_t s, int32_t n, int32_t player, const int32_t *st,
     cudaError_t e = cub::DeviceSelect::If(nullptr, bytes, ids, out, count, n, won, s);
     if (e) return e;
     void *tmp = nullptr;
-    if ((e = cudaMallocAsync(&tmp, bytes, s))) return e;
+    if ((e = device_alloc(&tmp, bytes, s))) return e;
     e = cub::DeviceSelect::If(tmp, bytes, ids, out, count, n, won, s);
     cudaFreeAsync(tmp, s);
     return e;

@@ -143,8 +143,8 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
         {(void **)&ctl_, sizeof(GraphCtl)},
     };
     for (const auto &a : arrays) {
-        cudaError_t e = cudaMalloc(a.ptr, a.bytes ? a.bytes : 16);
-        if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        cudaError_t e = device_alloc(a.ptr, a.bytes, stream_);
+        if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
         allocs_.push_back(*a.ptr);
     }
     PSI_CUDA_TRY(cudaMallocHost((void **)&hw_, sizeof(Words)));
@@ -188,7 +188,8 @@ Solver::~Solver()
     if (stream_) cudaStreamSynchronize(stream_);
     if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
     if (graph_) cudaGraphDestroy(graph_);
-    for (void *p : allocs_) cudaFree(p);
+    for (void *p : allocs_) cudaFreeAsync(p, stream_);   // back to the library's pool
+    if (stream_) cudaStreamSynchronize(stream_);
     if (hw_) cudaFreeHost(hw_);
     for (auto &p : ph_) {
         if (p.a) cudaEventDestroy(p.a);
@@ -504,7 +505,7 @@ int Solver::get_valuation(int32_t v0, int32_t count, int32_t *out)
     int rc = set_device();
     if (rc) return rc;
     int32_t *rows = nullptr;
-    cudaError_t e = cudaMallocAsync((void **)&rows, (size_t)bytes, stream_);
+    cudaError_t e = device_alloc((void **)&rows, (size_t)bytes, stream_);
     if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, "valuation export buffer");
     launch_materialize(stream_, v0, count, (int32_t)d, st_, node_, rows, &dw_->err);
     PSI_CUDA_TRY(cudaMemcpyAsync(out, rows, (size_t)bytes, cudaMemcpyDeviceToHost, stream_));
@@ -576,8 +577,8 @@ int Solver::enable_batch(const std::vector<int64_t> &base)
     } arrays[] = {{(void **)&game_of_, 4 * (size_t)n_}, {(void **)&gstate_, sizeof(int4) * (size_t)g},
                   {(void **)&gcount_, sizeof(unsigned long long) * (size_t)g}};
     for (const auto &a : arrays) {
-        cudaError_t e = cudaMalloc(a.ptr, a.bytes);
-        if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        cudaError_t e = device_alloc(a.ptr, a.bytes, stream_);
+        if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
         allocs_.push_back(*a.ptr);
     }
     PSI_CUDA_TRY(cudaMemcpyAsync(game_of_, game_of.data(), 4 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
@@ -646,8 +647,8 @@ int Solver::init_arena(int32_t slots)
                   {(void **)&gcount_, sizeof(unsigned long long) * (size_t)slots},
                   {(void **)&gmask_, 4 * (size_t)slots}};
     for (const auto &a : arrays) {
-        cudaError_t e = cudaMalloc(a.ptr, a.bytes);
-        if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        cudaError_t e = device_alloc(a.ptr, a.bytes, stream_);
+        if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
         allocs_.push_back(*a.ptr);
     }
     games_ = slots;
@@ -703,7 +704,7 @@ int Solver::arena_add(const std::vector<const HostGame *> &gs, const std::vector
     cudaError_t e = cudaSuccess;
     int64_t mr = 0;
     int ce = 0;
-    for (int i = 0; i < 7 && e == cudaSuccess; i++) e = cudaMallocAsync((void **)bufs[i], sizes[i], stream_);
+    for (int i = 0; i < 7 && e == cudaSuccess; i++) e = device_alloc((void **)bufs[i], sizes[i], stream_);
     for (int i = 0; i < 5 && e == cudaSuccess; i++)
         e = cudaMemcpyAsync(*bufs[i], src[i], sizes[i], cudaMemcpyHostToDevice, stream_);
     if (e == cudaSuccess) ce = build_reverse_csr(stream_, (int32_t)n, m, u_off, u_tgt, u_roff, u_rsrc, &mr);
