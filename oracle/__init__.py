@@ -17,9 +17,12 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "libpsi_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libpsi_ref.so")
+# Where the build recipe and the fixture test read the reference's sources
+# (absent on machines that only run the prebuilt libraries).
+REF_DIR = os.environ.get("REF_DIR", "/root/reference")
 
 
-def build(ref_dir: str = "/root/reference") -> None:
+def build(ref_dir: str = REF_DIR) -> None:
     """Compile the oracle (and the reference driver when ref_dir exists)."""
     env = dict(os.environ, REF_DIR=ref_dir)
     subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True, env=env)
