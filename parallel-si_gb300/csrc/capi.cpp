@@ -199,14 +199,17 @@ int psi_solver_create_csr(int32_t n, const int32_t *owner, const int32_t *priori
     if (!out || !owner || !priority || !offsets || !targets) return psi::fail(PSI_ERR_INVALID, "null argument");
     *out = nullptr;
     PSI_GUARD_BEGIN
-    psi::CsrView v;
-    int rc = psi::make_view(n, owner, priority, offsets, targets, v);
-    if (rc) return rc;
+    // the shape is checked here; the per-vertex and per-edge checks of
+    // validate_csr run on the device right after the upload
+    if (n < 0) return psi::fail(PSI_ERR_INVALID, "negative vertex count");
+    if (offsets[0] != 0) return psi::fail(PSI_ERR_INVALID, "offsets[0] must be 0");
+    if (offsets[n] < 0) return psi::fail(PSI_ERR_INVALID, "offsets[n] is negative");
+    psi::CsrView v{n, offsets[n], 0, owner, priority, offsets, targets};
     psi_options o;
     psi_options_default(&o);
     if (opt) o = *opt;
     psi::Solver *s = nullptr;
-    rc = psi::Solver::create(v, o, &s);
+    int rc = psi::Solver::create(v, o, &s, /*validate=*/true);
     if (rc) return rc;
     psi_solver *h = new psi_solver();
     h->s = s;

@@ -30,6 +30,14 @@ long long launch_count();
 int build_reverse_csr(cudaStream_t s, int32_t n, int64_t m, const int32_t *off, const int32_t *tgt,
                       int32_t *rev_off, int32_t *rev_src, int64_t *rev_m);
 
+// Validation of an uploaded game (validate_csr's checks on the device):
+// *bad_vertex = the lowest failing vertex or -1, *bad_check = its check (1
+// player, 2 priority, 3 no successor), *bad_edge = 1 if a successor lies
+// outside [0, n), *max_pri = the largest priority.  Synchronous; returns a
+// cudaError_t value.
+int validate_game(cudaStream_t s, int32_t n, int64_t m, const int32_t *owner, const int32_t *pri,
+                  const int32_t *off, const int32_t *tgt, int64_t *bad_vertex, int32_t *bad_check,
+                  int32_t *bad_edge, int32_t *max_pri);
 // Owner int32 -> int8 on the device (the upload sends the caller's int32 array).
 void launch_narrow_owner(cudaStream_t s, int32_t n, const int32_t *in, int8_t *out);
 // plist = Even's vertices in increasing order, then Odd's (in decreasing

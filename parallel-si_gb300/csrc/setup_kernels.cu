@@ -3,6 +3,7 @@
 // that the tour build scans to link each parent's children without atomics,
 // the owner narrowing and player lists built at upload, and the winning-set
 // selection read back at the end of a solve.
+#include <cub/block/block_reduce.cuh>
 #include <cub/device/device_partition.cuh>
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
@@ -22,25 +23,54 @@ inline unsigned grid_for(int64_t items, int block = kBlock)
     return (unsigned)(g < 1 ? 1 : g);
 }
 
-// key = (target << 32) | source for every edge
-__global__ void k_edge_keys(int32_t n, const int32_t *__restrict__ off, const int32_t *__restrict__ tgt,
-                            unsigned long long *__restrict__ keys)
+// (target, source) of every edge, in CSR order: sources non-decreasing, so a
+// stable sort by target leaves each target's sources in increasing order.
+__global__ void k_edge_pairs(int32_t n, const int32_t *__restrict__ off, const int32_t *__restrict__ tgt,
+                             uint32_t *__restrict__ keys, int32_t *__restrict__ vals)
 {
-    int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= n) return;
-    for (int32_t e = off[v]; e < off[v + 1]; e++)
-        keys[e] = ((unsigned long long)(uint32_t)tgt[e] << 32) | (uint32_t)v;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
+        for (int32_t e = off[v]; e < off[v + 1]; e++) {
+            keys[e] = (uint32_t)tgt[e];
+            vals[e] = (int32_t)v;
+        }
 }
 
-__global__ void k_rev_count(const unsigned long long *__restrict__ keys, const int32_t *__restrict__ nkeys,
-                            int32_t *__restrict__ deg, int32_t *__restrict__ src)
+// Keep the first of each run of equal (target, source) pairs; count the kept
+// sources per target.
+__global__ void k_rev_unique(int64_t m, const uint32_t *__restrict__ keys, const int32_t *__restrict__ vals,
+                             uint8_t *__restrict__ keep, int32_t *__restrict__ deg)
 {
-    int32_t k = *nkeys;
-    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k; i += gridDim.x * blockDim.x) {
-        unsigned long long key = keys[i];
-        atomicAdd(&deg[(int32_t)(key >> 32)], 1);
-        src[i] = (int32_t)(uint32_t)(key & 0xffffffffull);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t k = keys[i];
+        const bool first = i == 0 || k != keys[i - 1] || vals[i] != vals[i - 1];
+        keep[i] = first ? 1 : 0;
+        if (first) atomicAdd(&deg[k], 1);
     }
+}
+
+// Checks an uploaded CSR game as validate_csr does on the host: the lowest
+// failing vertex and its check (1 player not 0/1, 2 negative priority, 3 no
+// successor) as min(4 v + check) in *bad_vertex, any successor outside
+// [0, n) in *bad_edge, and the largest priority in *max_pri.
+__global__ void k_validate(int32_t n, int64_t m, const int32_t *__restrict__ owner, const int32_t *__restrict__ pri,
+                           const int32_t *__restrict__ off, const int32_t *__restrict__ tgt,
+                           unsigned long long *__restrict__ bad_vertex, int32_t *__restrict__ bad_edge,
+                           int32_t *__restrict__ max_pri)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int32_t top = 0;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+        const int32_t o = owner[v], p = pri[v];
+        const int check = (o != 0 && o != 1) ? 1 : (p < 0 ? 2 : (off[v + 1] <= off[v] ? 3 : 0));
+        if (check) atomicMin(bad_vertex, (unsigned long long)v * 4 + check);
+        top = max(top, p);
+    }
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += stride)
+        if ((uint32_t)tgt[e] >= (uint32_t)n) *bad_edge = 1;
+    typedef cub::BlockReduce<int32_t, kBlock> Reduce;
+    __shared__ typename Reduce::TempStorage tmp;
+    const int32_t block_top = Reduce(tmp).Reduce(top, [](int32_t x, int32_t y) { return max(x, y); });
+    if (threadIdx.x == 0) atomicMax(max_pri, block_top);
 }
 
 __global__ void k_narrow_owner(int32_t n, const int32_t *__restrict__ in, int8_t *__restrict__ out)
@@ -77,38 +107,46 @@ int build_reverse_csr(cudaStream_t s, int32_t n, int64_t m, const int32_t *off, 
 {
     *rev_m = 0;
     if (m <= 0) return cudaMemsetAsync(rev_off, 0, 4 * ((size_t)n + 1), s);
-    unsigned long long *k0 = nullptr, *k1 = nullptr;
-    int32_t *nuniq = nullptr, *deg = nullptr;
+    uint32_t *k0 = nullptr, *k1 = nullptr;
+    int32_t *v0 = nullptr, *v1 = nullptr, *nuniq = nullptr, *deg = nullptr;
+    uint8_t *keep = nullptr;
     void *tmp = nullptr;
-    size_t tmp_sort = 0, tmp_uniq = 0, tmp_scan = 0;
-    const int end_bit = 32 + bits_for(n);
+    size_t tmp_sort = 0, tmp_sel = 0, tmp_scan = 0;
+    const int end_bit = bits_for(n);   // targets < n
     cudaError_t e = cudaSuccess;
-    cub::DoubleBuffer<unsigned long long> db(nullptr, nullptr);
-    e = cub::DeviceRadixSort::SortKeys(nullptr, tmp_sort, db, (int)m, 0, end_bit, s);
-    if (e) return e;
-    e = cub::DeviceSelect::Unique(nullptr, tmp_uniq, (unsigned long long *)nullptr, (unsigned long long *)nullptr,
-                                  (int32_t *)nullptr, (int)m, s);
+    {
+        cub::DoubleBuffer<uint32_t> dk(nullptr, nullptr);
+        cub::DoubleBuffer<int32_t> dv(nullptr, nullptr);
+        e = cub::DeviceRadixSort::SortPairs(nullptr, tmp_sort, dk, dv, (int)m, 0, end_bit, s);
+        if (e) return e;
+    }
+    e = cub::DeviceSelect::Flagged(nullptr, tmp_sel, (int32_t *)nullptr, (uint8_t *)nullptr, (int32_t *)nullptr,
+                                   (int32_t *)nullptr, (int)m, s);
     if (e) return e;
     e = cub::DeviceScan::ExclusiveSum(nullptr, tmp_scan, (int32_t *)nullptr, (int32_t *)nullptr, n + 1, s);
     if (e) return e;
-    size_t tmp_bytes = std::max(tmp_sort, std::max(tmp_uniq, tmp_scan));
-    if ((e = device_alloc((void **)&k0, 8 * (size_t)m, s))) goto out;
-    if ((e = device_alloc((void **)&k1, 8 * (size_t)m, s))) goto out;
+    size_t tmp_bytes = std::max(tmp_sort, std::max(tmp_sel, tmp_scan));
+    if ((e = device_alloc((void **)&k0, 4 * (size_t)m, s))) goto out;
+    if ((e = device_alloc((void **)&k1, 4 * (size_t)m, s))) goto out;
+    if ((e = device_alloc((void **)&v0, 4 * (size_t)m, s))) goto out;
+    if ((e = device_alloc((void **)&v1, 4 * (size_t)m, s))) goto out;
+    if ((e = device_alloc((void **)&keep, (size_t)m, s))) goto out;
     if ((e = device_alloc((void **)&nuniq, sizeof(int32_t), s))) goto out;
     if ((e = device_alloc((void **)&deg, 4 * ((size_t)n + 1), s))) goto out;
     if ((e = device_alloc(&tmp, tmp_bytes, s))) goto out;
     count_launch();
-    k_edge_keys<<<grid_for(n), kBlock, 0, s>>>(n, off, tgt, k0);
+    k_edge_pairs<<<grid_for(n), kBlock, 0, s>>>(n, off, tgt, k0, v0);
     {
-        cub::DoubleBuffer<unsigned long long> keys(k0, k1);
+        // stable by target: each target's sources stay in increasing order
+        cub::DoubleBuffer<uint32_t> keys(k0, k1);
+        cub::DoubleBuffer<int32_t> vals(v0, v1);
         size_t t = tmp_bytes;
-        if ((e = cub::DeviceRadixSort::SortKeys(tmp, t, keys, (int)m, 0, end_bit, s))) goto out;
-        unsigned long long *sorted = keys.Current(), *spare = keys.Alternate();
-        t = tmp_bytes;
-        if ((e = cub::DeviceSelect::Unique(tmp, t, sorted, spare, nuniq, (int)m, s))) goto out;
+        if ((e = cub::DeviceRadixSort::SortPairs(tmp, t, keys, vals, (int)m, 0, end_bit, s))) goto out;
         if ((e = cudaMemsetAsync(deg, 0, 4 * ((size_t)n + 1), s))) goto out;
         count_launch();
-        k_rev_count<<<1216, kBlock, 0, s>>>(spare, nuniq, deg, rev_src);
+        k_rev_unique<<<1216, kBlock, 0, s>>>(m, keys.Current(), vals.Current(), keep, deg);
+        t = tmp_bytes;
+        if ((e = cub::DeviceSelect::Flagged(tmp, t, vals.Current(), keep, rev_src, nuniq, (int)m, s))) goto out;
         t = tmp_bytes;
         if ((e = cub::DeviceScan::ExclusiveSum(tmp, t, deg, rev_off, n + 1, s))) goto out;
         int32_t h = 0;
@@ -117,12 +155,47 @@ int build_reverse_csr(cudaStream_t s, int32_t n, int64_t m, const int32_t *off, 
         *rev_m = h;
     }
 out:
-    if (k0) cudaFreeAsync(k0, s);
-    if (k1) cudaFreeAsync(k1, s);
-    if (nuniq) cudaFreeAsync(nuniq, s);
-    if (deg) cudaFreeAsync(deg, s);
-    if (tmp) cudaFreeAsync(tmp, s);
+    for (void *p : {(void *)k0, (void *)k1, (void *)v0, (void *)v1, (void *)keep, (void *)nuniq, (void *)deg, tmp})
+        if (p) cudaFreeAsync(p, s);
     return (int)e;
+}
+
+int validate_game(cudaStream_t s, int32_t n, int64_t m, const int32_t *owner, const int32_t *pri,
+                  const int32_t *off, const int32_t *tgt, int64_t *bad_vertex, int32_t *bad_check,
+                  int32_t *bad_edge, int32_t *max_pri)
+{
+    *bad_vertex = -1;
+    *bad_check = 0;
+    *bad_edge = 0;
+    *max_pri = 0;
+    if (n <= 0) return 0;
+    struct Out {
+        unsigned long long bad_vertex;
+        int32_t bad_edge, max_pri;
+    };
+    Out *d = nullptr;
+    cudaError_t e = device_alloc((void **)&d, sizeof(Out), s);
+    if (e) return e;
+    Out init = {~0ull, 0, 0};
+    Out h = init;
+    e = cudaMemcpyAsync(d, &init, sizeof init, cudaMemcpyHostToDevice, s);
+    if (!e) {
+        count_launch();
+        unsigned g = grid_for(std::max<int64_t>(n, m));
+        g = g < 2432u ? g : 2432u;
+        k_validate<<<g, kBlock, 0, s>>>(n, m, owner, pri, off, tgt, &d->bad_vertex, &d->bad_edge, &d->max_pri);
+        e = cudaMemcpyAsync(&h, d, sizeof h, cudaMemcpyDeviceToHost, s);
+    }
+    if (!e) e = cudaStreamSynchronize(s);
+    cudaFreeAsync(d, s);
+    if (e) return e;
+    if (h.bad_vertex != ~0ull) {
+        *bad_vertex = (int64_t)(h.bad_vertex / 4);
+        *bad_check = (int32_t)(h.bad_vertex % 4);
+    }
+    *bad_edge = h.bad_edge;
+    *max_pri = h.max_pri;
+    return 0;
 }
 
 void launch_narrow_owner(cudaStream_t s, int32_t n, const int32_t *in, int8_t *out)

@@ -43,7 +43,7 @@ int check_options(const psi_options &opt)
 
 }  // namespace
 
-int Solver::create(const CsrView &g, const psi_options &opt, Solver **out)
+int Solver::create(const CsrView &g, const psi_options &opt, Solver **out, bool validate)
 {
     *out = nullptr;
     if (g.n < 0) return fail(PSI_ERR_INVALID, "negative vertex count");   // n = 0: the empty game
@@ -56,7 +56,7 @@ int Solver::create(const CsrView &g, const psi_options &opt, Solver **out)
     s->stride_ = opt.sublist_len;
     s->use_graph_ = opt.graph != 0;
     rc = s->alloc_arrays(g.n, g.m);
-    if (!rc) rc = s->upload_game(g);
+    if (!rc) rc = s->upload_game(g, validate);
     if (rc) {
         delete s;
         return rc;
@@ -157,7 +157,7 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
 // owner array goes up as the caller's int32 (into st_, free until the first
 // evaluation) and is narrowed on the device; the player lists are an ordered
 // partition on the device.
-int Solver::upload_game(const CsrView &g)
+int Solver::upload_game(const CsrView &g, bool validate)
 {
     set_extent(g.n);
     m_ = g.m;
@@ -167,6 +167,20 @@ int Solver::upload_game(const CsrView &g)
     PSI_CUDA_TRY(cudaMemcpyAsync(pri_, g.priority, 4 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
     PSI_CUDA_TRY(cudaMemcpyAsync(off_, g.offsets, 4 * ((size_t)n_ + 1), cudaMemcpyHostToDevice, stream_));
     if (m_) PSI_CUDA_TRY(cudaMemcpyAsync(tgt_, g.targets, 4 * (size_t)m_, cudaMemcpyHostToDevice, stream_));
+    if (validate) {
+        int64_t bad_v = -1;
+        int32_t check = 0, bad_e = 0, top = 0;
+        int ve = validate_game(stream_, n_, m_, st_, pri_, off_, tgt_, &bad_v, &check, &bad_e, &top);
+        if (ve) return fail(PSI_ERR_CUDA, std::string("validation: ") + cudaGetErrorString((cudaError_t)ve));
+        if (bad_v >= 0) {
+            std::string v = std::to_string(bad_v);
+            if (check == 1) return fail(PSI_ERR_INVALID, "invalid player at vertex " + v);
+            if (check == 2) return fail(PSI_ERR_INVALID, "negative priority at vertex " + v);
+            return fail(PSI_ERR_INVALID, "vertex " + v + " has no successor");
+        }
+        if (bad_e) return fail(PSI_ERR_INVALID, "successor out of range");
+        max_pri_ = top;
+    }
     launch_narrow_owner(stream_, n_, st_, owner_);
     int ce = partition_players(stream_, n_, owner_, plist_, &dw_->sinkcount);
     if (ce) return fail(PSI_ERR_CUDA, std::string("player lists: ") + cudaGetErrorString((cudaError_t)ce));

@@ -40,7 +40,9 @@ struct GraphCtl {
 
 class Solver {
 public:
-    static int create(const CsrView &g, const psi_options &opt, Solver **out);
+    // validate: run validate_csr's checks on the device after the upload (the
+    // view's max_pri is then ignored and computed there).
+    static int create(const CsrView &g, const psi_options &opt, Solver **out, bool validate = false);
     // An empty arena for served games (serve.cpp): up to max_vertices vertex
     // slots (each game takes n+1), max_edges edges, `slots` games at a time.
     static int create_arena(int64_t max_vertices, int64_t max_edges, int32_t slots, const psi_options &opt,
@@ -108,7 +110,7 @@ public:
 private:
     Solver() = default;
     int alloc_arrays(int64_t cap_n, int64_t cap_m);
-    int upload_game(const CsrView &g);
+    int upload_game(const CsrView &g, bool validate);
     int init_arena(int32_t slots);
     void set_extent(int32_t n);
     int sync_and_check(const char *what);

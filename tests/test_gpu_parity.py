@@ -120,3 +120,35 @@ def test_gpu_graph_solve_evaluation_cap():
     assert e.value.code == 8   # PSI_ERR_LIMIT
     assert s.solve() == (it, br)
     s.close()
+
+
+@pytest.mark.gpu
+def test_gpu_solver_from_host_csr_validates_like_the_host():
+    """The device-side checks of psi_solver_create_csr report what the host
+    validator (psi_game_from_csr) reports."""
+    g = make("c2", 5000, 91)
+    ow, pr, off, tg = [np.ascontiguousarray(a, dtype=np.int32) for a in g.csr()]
+
+    def both(o, p, f, t):
+        msgs = []
+        for make_it in (lambda: psi.Game.from_csr(o, p, f, t), lambda: psi.GPUList.from_csr(o, p, f, t)):
+            with pytest.raises(psi.PsiError) as e:
+                make_it()
+            assert e.value.code == 1   # PSI_ERR_INVALID
+            msgs.append(e.value.message)
+        assert msgs[0] == msgs[1], msgs
+        return msgs[0]
+
+    bad = tg.copy(); bad[17] = 5000
+    assert "successor" in both(ow, pr, off, bad)
+    bad = tg.copy(); bad[3] = -2
+    assert "successor" in both(ow, pr, off, bad)
+    bad = pr.copy(); bad[4321] = -1; bad[4000] = -7
+    assert both(ow, bad, off, tg) == "negative priority at vertex 4000"
+    bad = ow.copy(); bad[77] = 2
+    assert both(bad, pr, off, tg) == "invalid player at vertex 77"
+    bad = off.copy(); bad[1234] = bad[1235]   # vertex 1234 loses its successors
+    assert both(ow, pr, bad, tg) == "vertex 1234 has no successor"
+    s = psi.GPUList.from_csr(ow, pr, off, tg)
+    assert s.max_pri == int(pr.max())
+    s.close()
