@@ -101,10 +101,12 @@ void psi_options_default(psi_options *opt);
  * gpu_list_ranking.cu:14-36): uploads the game and allocates the solver's
  * device state.  The game may be freed afterwards. */
 int psi_solver_create(const psi_game *g, const psi_options *opt, psi_solver **out);
-/* The same from a CSR in caller memory, validated as psi_game_from_csr
- * validates, uploaded straight from the caller's arrays (no host copy; the
- * arrays may be freed afterwards): GPUGame + GPUList construction from an
- * in-memory game without the intermediate psi_game. */
+/* The same from a CSR in caller memory, uploaded straight from the caller's
+ * arrays (no host copy; the arrays may be freed afterwards) and validated
+ * with psi_game_from_csr's checks and messages -- the shape of offsets on
+ * the host, the per-vertex and per-edge checks on the device after the
+ * upload: GPUGame + GPUList construction from an in-memory game without the
+ * intermediate psi_game. */
 int psi_solver_create_csr(int32_t n, const int32_t *owner, const int32_t *priority, const int32_t *offsets,
                           const int32_t *targets, const psi_options *opt, psi_solver **out);
 void psi_solver_destroy(psi_solver *s);
