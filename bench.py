@@ -330,6 +330,10 @@ def run_gb300(args, rank, world, local):
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                     "traffic": traffic, "kernel": KERNEL_OF_PHASE[dom], "peak_source": peak_kind,
                     "algorithmic_bytes_per_launch": bpc, "ms_per_launch": dom_ms / dom_calls}
+        if traffic:
+            # what HBM actually moved per second (random 32-byte sectors count whole)
+            roofline["traffic_GBps"] = traffic / (dom_ms / dom_calls / 1e3) / 1e9
+            roofline["traffic_frac"] = roofline["traffic_GBps"] / peak
     lr = {}
     for p in ("sublist", "tour", "broadcast"):
         pm, pc = phases[p]
