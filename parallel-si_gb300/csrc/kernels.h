@@ -121,8 +121,17 @@ void launch_arena_place(cudaStream_t s, int32_t nu, int32_t k_games, const int32
                         const int32_t *u_off, const int32_t *u_tgt, const int32_t *u_roff, const int32_t *u_rsrc,
                         int8_t *owner, int32_t *pri, int32_t *off, int32_t *tgt, int32_t *rev_off, int32_t *rev_src,
                         int32_t *strat, int32_t *st, uint8_t *solved, int32_t *game_of, int4 *gstate,
-                        unsigned long long *gcount);
-void launch_arena_clear(cudaStream_t s, int32_t vb, int32_t count, uint8_t *solved, int32_t *game_of, int32_t *st);
+                        unsigned long long *gcount, int32_t *succ, uint8_t *dirty);
+// Games copied as they are into a union (game k at vertices ub[k], edges
+// ue[k]): offsets and targets shifted to union numbering; u_off[nu] = ue[K].
+void launch_union_fixup(cudaStream_t s, int32_t nu, int64_t mu, int32_t k_games, const int32_t *ub, const int32_t *ue,
+                        int32_t *u_off, int32_t *u_tgt);
+// Tour upkeep of the arena: every slot an isolated pair; the sink's nodes
+// following the vertex count from old_n to new_n.
+void launch_isolate_pairs(cudaStream_t s, int64_t count, int32_t *succ);
+void launch_move_extent(cudaStream_t s, int32_t old_n, int32_t new_n, int32_t *succ);
+void launch_arena_clear(cudaStream_t s, int32_t vb, int32_t count, uint8_t *solved, int32_t *game_of, int32_t *st,
+                        int32_t *succ, uint8_t *dirty);
 // Appends the vertices of `player` that belong to a game to plist (*count += k).
 void launch_build_plist(cudaStream_t s, int32_t n, int32_t player, const int8_t *owner, const int32_t *game_of,
                         int32_t *plist, int32_t *count);

@@ -121,29 +121,44 @@ public:
         std::vector<int32_t> done, iters, brs;
         rc = solver_->arena_step(reset_, done, iters, brs);
         if (rc) return rc;
+        // retire the finished games together: copy their results out, free
+        // their ranges, then turn the copies into game-local results
+        std::vector<Request *> fin;
+        std::vector<std::vector<int32_t>> status;
         for (size_t i = 0; i < done.size(); i++) {
             Request *r = slot_req_[done[i]];
             if (!r) continue;
             r->iters = iters[i];
             r->brs = brs[i];
             r->strategy.resize(r->game.n);
-            r->infinite.resize(r->game.n);
-            rc = solver_->get_strategy_range(r->vb, r->game.n, r->strategy.data());
-            if (!rc) rc = solver_->get_infinite_range(r->vb, r->game.n, r->infinite.data());
+            status.emplace_back(r->game.n);
+            rc = solver_->arena_fetch((int32_t)r->vb, r->game.n, r->strategy.data(), status.back().data());
             if (rc) return rc;
+            fin.push_back(r);
+        }
+        if (fin.empty()) return PSI_OK;
+        std::vector<int32_t> vbs, counts, slots;
+        for (Request *r : fin) {
+            const int64_t count = (int64_t)r->game.n + 1;
+            ends_.erase(ends_.find(r->vb + count));
+            vbs.push_back((int32_t)r->vb);
+            counts.push_back((int32_t)count);
+            slots.push_back(r->slot);
+        }
+        rc = solver_->arena_remove(vbs, counts, slots, (int32_t)extent());
+        if (rc) return rc;
+        for (size_t i = 0; i < fin.size(); i++) {
+            Request *r = fin[i];
             for (int32_t &t : r->strategy)
                 if (t >= 0) t -= (int32_t)r->vb;
-            rc = release(r);
-            if (rc) return rc;
+            r->infinite.resize(r->game.n);
+            for (int32_t v = 0; v < r->game.n; v++) r->infinite[v] = status_infinite(status[i][v]);
+            release(r);
             r->state = 2;
             last_finished_.push_back(r->ticket);
             (*finished)++;
         }
-        if (!done.empty()) {
-            rc = solver_->arena_rebuild_lists();
-            if (rc) return rc;
-        }
-        return PSI_OK;
+        return solver_->arena_rebuild_lists();
     }
 
     int status(int64_t ticket, int32_t *state, int32_t *iters, int32_t *brs)
@@ -226,21 +241,18 @@ private:
         return PSI_OK;
     }
 
-    int release(Request *r)
+    // Host bookkeeping of a retired request (its device range is already inert).
+    void release(Request *r)
     {
-        int64_t count = (int64_t)r->game.n + 1;
-        ends_.erase(ends_.find(r->vb + count));
+        const int64_t count = (int64_t)r->game.n + 1;
         vranges_.give(r->vb, count);
         eranges_.give(r->eb, r->game.m);
-        int rc = solver_->arena_remove((int32_t)r->vb, (int32_t)count, r->slot, (int32_t)extent());
-        if (rc) return rc;
         slot_req_[r->slot] = nullptr;
         free_slots_.push_back(r->slot);
         resident_--;
         used_v_ -= count;
         used_e_ -= r->game.m;
         r->game = HostGame();   // the input is no longer needed
-        return PSI_OK;
     }
 
     int64_t extent() const { return ends_.empty() ? 0 : *ends_.rbegin(); }

@@ -35,7 +35,8 @@ __global__ void k_arena_place(int32_t nu, int32_t k_games, const int32_t *__rest
                               int32_t *__restrict__ rev_off, int32_t *__restrict__ rev_src,
                               int32_t *__restrict__ strat, int32_t *__restrict__ st, uint8_t *__restrict__ solved,
                               int32_t *__restrict__ game_of, int4 *__restrict__ gstate,
-                              unsigned long long *__restrict__ gcount)
+                              unsigned long long *__restrict__ gcount, int32_t *__restrict__ succ,
+                              uint8_t *__restrict__ dirty)
 {
     int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nu) return;
@@ -60,6 +61,11 @@ __global__ void k_arena_place(int32_t nu, int32_t k_games, const int32_t *__rest
     st[a] = 0;
     solved[a] = 0;
     game_of[a] = slot[k];
+    // tour: an isolated pair until the next evaluation relinks a (a dirty
+    // parent) and its parent links it
+    succ[2 * (int64_t)a] = 2 * a + 1;
+    succ[2 * (int64_t)a + 1] = 2 * a;
+    dirty[a] = 1;
     if (i == u0) {
         gstate[slot[k]] = make_int4(0, 0, 1, 0);
         gcount[slot[k]] = 0;
@@ -74,20 +80,81 @@ __global__ void k_arena_place(int32_t nu, int32_t k_games, const int32_t *__rest
         st[z] = 0;
         solved[z] = 1;
         game_of[z] = -1;
+        succ[2 * (int64_t)z] = 2 * z + 1;
+        succ[2 * (int64_t)z + 1] = 2 * z;
+        dirty[z] = 0;
     }
 }
 
-// A removed game's range becomes inert: solved, in no game, and with no
-// finite depth left behind (the root-path summary pass visits every vertex
-// with a finite depth).
+// Union staging: each admitted game was copied as it is (its own offsets and
+// vertex ids) to its place in the union; shift offsets by the game's first
+// edge and targets by its first vertex.  ub/ue: first vertex / edge of game k
+// in the union (K+1 entries each).
+__global__ void k_union_fixup(int32_t nu, int64_t mu, int32_t k_games, const int32_t *__restrict__ ub,
+                              const int32_t *__restrict__ ue, int32_t *__restrict__ u_off,
+                              int32_t *__restrict__ u_tgt)
+{
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nu; i += stride) {
+        int32_t lo = 0, hi = k_games;   // largest k with ub[k] <= i
+        while (hi - lo > 1) {
+            int32_t mid = (lo + hi) >> 1;
+            if (ub[mid] <= i) lo = mid;
+            else hi = mid;
+        }
+        u_off[i] += ue[lo];
+    }
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < mu; e += stride) {
+        int32_t lo = 0, hi = k_games;   // largest k with ue[k] <= e
+        while (hi - lo > 1) {
+            int32_t mid = (lo + hi) >> 1;
+            if (ue[mid] <= e) lo = mid;
+            else hi = mid;
+        }
+        u_tgt[e] += ub[lo];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) u_off[nu] = ue[k_games];
+}
+
+// Every slot of a new arena starts as an isolated tour pair.
+__global__ void k_isolate_pairs(int64_t count, int32_t *__restrict__ succ)
+{
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < count; v += (int64_t)gridDim.x * blockDim.x) {
+        succ[2 * v] = (int32_t)(2 * v + 1);
+        succ[2 * v + 1] = (int32_t)(2 * v);
+    }
+}
+
+// The arena's vertex count moved from old_n to new_n: the sink's two nodes
+// are 2n and 2n+1, so vertex old_n gets an isolated pair back (placement may
+// overwrite it next) and the new sink's down node ends the list.
+__global__ void k_move_extent(int32_t old_n, int32_t new_n, int32_t *__restrict__ succ)
+{
+    if (old_n < new_n) {
+        succ[2 * (int64_t)old_n] = 2 * old_n + 1;
+        succ[2 * (int64_t)old_n + 1] = 2 * old_n;
+    }
+    succ[2 * (int64_t)new_n] = TOUR_END;
+    succ[2 * (int64_t)new_n + 1] = 2 * new_n;
+}
+
+// A removed game's range becomes inert: solved, in no game, with no finite
+// depth left behind (the root-path summary pass visits every vertex with a
+// finite depth), and out of the tour.
 __global__ void k_arena_clear(int32_t vb, int32_t count, uint8_t *__restrict__ solved, int32_t *__restrict__ game_of,
-                              int32_t *__restrict__ st)
+                              int32_t *__restrict__ st, int32_t *__restrict__ succ, uint8_t *__restrict__ dirty)
 {
     int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
-    solved[vb + i] = 1;
-    game_of[vb + i] = -1;
-    st[vb + i] = 0;
+    const int32_t v = vb + i;
+    solved[v] = 1;
+    game_of[v] = -1;
+    st[v] = 0;
+    dirty[v] = 0;
+    // the whole game leaves at once (games never link to each other), so its
+    // pairs can be isolated without touching anyone else's list
+    succ[2 * (int64_t)v] = 2 * v + 1;
+    succ[2 * (int64_t)v + 1] = 2 * v;
 }
 
 // Vertices of `player` that belong to a game, appended in any order (the
@@ -179,20 +246,45 @@ void launch_arena_place(cudaStream_t s, int32_t nu, int32_t k_games, const int32
                         const int32_t *u_off, const int32_t *u_tgt, const int32_t *u_roff, const int32_t *u_rsrc,
                         int8_t *owner, int32_t *pri, int32_t *off, int32_t *tgt, int32_t *rev_off, int32_t *rev_src,
                         int32_t *strat, int32_t *st, uint8_t *solved, int32_t *game_of, int4 *gstate,
-                        unsigned long long *gcount)
+                        unsigned long long *gcount, int32_t *succ, uint8_t *dirty)
 {
     if (nu <= 0) return;
     count_launch();
     k_arena_place<<<grid_for(nu), kBlock, 0, s>>>(nu, k_games, ub, vb, eb, slot, u_owner, u_pri, u_off, u_tgt, u_roff,
                                                   u_rsrc, owner, pri, off, tgt, rev_off, rev_src, strat, st, solved,
-                                                  game_of, gstate, gcount);
+                                                  game_of, gstate, gcount, succ, dirty);
 }
 
-void launch_arena_clear(cudaStream_t s, int32_t vb, int32_t count, uint8_t *solved, int32_t *game_of, int32_t *st)
+void launch_union_fixup(cudaStream_t s, int32_t nu, int64_t mu, int32_t k_games, const int32_t *ub, const int32_t *ue,
+                        int32_t *u_off, int32_t *u_tgt)
+{
+    count_launch();
+    unsigned g = grid_for(nu > mu ? nu : mu);
+    g = g < 2432u ? g : 2432u;
+    k_union_fixup<<<g, kBlock, 0, s>>>(nu, mu, k_games, ub, ue, u_off, u_tgt);
+}
+
+void launch_isolate_pairs(cudaStream_t s, int64_t count, int32_t *succ)
 {
     if (count <= 0) return;
     count_launch();
-    k_arena_clear<<<grid_for(count), kBlock, 0, s>>>(vb, count, solved, game_of, st);
+    unsigned g = grid_for(count);
+    g = g < 2432u ? g : 2432u;
+    k_isolate_pairs<<<g, kBlock, 0, s>>>(count, succ);
+}
+
+void launch_move_extent(cudaStream_t s, int32_t old_n, int32_t new_n, int32_t *succ)
+{
+    count_launch();
+    k_move_extent<<<1, 1, 0, s>>>(old_n, new_n, succ);
+}
+
+void launch_arena_clear(cudaStream_t s, int32_t vb, int32_t count, uint8_t *solved, int32_t *game_of, int32_t *st,
+                        int32_t *succ, uint8_t *dirty)
+{
+    if (count <= 0) return;
+    count_launch();
+    k_arena_clear<<<grid_for(count), kBlock, 0, s>>>(vb, count, solved, game_of, st, succ, dirty);
 }
 
 void launch_build_plist(cudaStream_t s, int32_t n, int32_t player, const int8_t *owner, const int32_t *game_of,

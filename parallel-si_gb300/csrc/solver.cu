@@ -670,6 +670,8 @@ int Solver::init_arena(int32_t slots)
     PSI_CUDA_TRY(cudaMemsetAsync(solved_, 1, (size_t)cap_n_, stream_));          // every slot inert
     PSI_CUDA_TRY(cudaMemsetAsync(game_of_, 0xff, 4 * (size_t)cap_n_, stream_));   // -1: in no game
     PSI_CUDA_TRY(cudaMemsetAsync(st_, 0, 4 * (size_t)cap_n_, stream_));            // no finite depths
+    launch_isolate_pairs(stream_, cap_n_ + 1, succ_);                              // no slot in the tour
+    launch_move_extent(stream_, 0, 0, succ_);
     PSI_CUDA_TRY(cudaMemsetAsync(gstate_, 0, sizeof(int4) * (size_t)slots, stream_));
     PSI_CUDA_TRY(cudaMemsetAsync(gcount_, 0, sizeof(unsigned long long) * (size_t)slots, stream_));
     PSI_CUDA_TRY(cudaMemsetAsync(gmask_, 0, 4 * (size_t)slots, stream_));
@@ -678,8 +680,11 @@ int Solver::init_arena(int32_t slots)
     return PSI_OK;
 }
 
-// Places the games admitted in one step: one packed upload of their union,
-// one reverse-CSR build over it and one placement launch.
+// Places the games admitted in one step: each game's arrays are copied as
+// they are into a device staging union (no host packing), shifted to union
+// numbering on the device, given one reverse-CSR build and placed by one
+// launch.  The tour stays valid: placed vertices start as isolated pairs and
+// dirty parents, which the next evaluation relinks.
 int Solver::arena_add(const std::vector<const HostGame *> &gs, const std::vector<int32_t> &vb,
                       const std::vector<int32_t> &eb, const std::vector<int32_t> &slot, int32_t extent)
 {
@@ -688,71 +693,104 @@ int Solver::arena_add(const std::vector<const HostGame *> &gs, const std::vector
     if (K == 0) return PSI_OK;
     if ((int32_t)vb.size() != K || (int32_t)eb.size() != K || (int32_t)slot.size() != K || extent > cap_n_)
         return fail(PSI_ERR_INVALID, "arena placement lists disagree");
+    int64_t n = 0, m = 0;
+    int32_t top = 0;
+    // per-game table: ub[K+1], ue[K+1], vb[K], eb[K], slot[K]
+    std::vector<int32_t> table(5 * (size_t)K + 2);
+    int32_t *ub = table.data(), *ue = ub + K + 1;
     for (int32_t k = 0; k < K; k++) {
         const HostGame &g = *gs[k];
-        if (slot[k] < 0 || slot[k] >= games_ || vb[k] < 0 || eb[k] < 0 || (int64_t)vb[k] + g.n + 1 > extent ||
-            (int64_t)eb[k] + g.m > cap_m_)
+        if (g.n <= 0 || slot[k] < 0 || slot[k] >= games_ || vb[k] < 0 || eb[k] < 0 ||
+            (int64_t)vb[k] + g.n + 1 > extent || (int64_t)eb[k] + g.m > cap_m_)
             return fail(PSI_ERR_INVALID, "arena placement out of range");
+        ub[k] = (int32_t)n;
+        ue[k] = (int32_t)m;
+        n += g.n;
+        m += g.m;
+        top = g.max_pri > top ? g.max_pri : top;
+        table[2 * (size_t)K + 2 + k] = vb[k];
+        table[3 * (size_t)K + 2 + k] = eb[k];
+        table[4 * (size_t)K + 2 + k] = slot[k];
     }
-    HostGame u;
-    std::vector<int64_t> base;
-    int rc = pack_games(gs, u, base);
+    if (2 * n + 2 > INT32_MAX || m > INT32_MAX) return fail(PSI_ERR_TOO_LARGE, "admission too large for int32 ids");
+    ub[K] = (int32_t)n;
+    ue[K] = (int32_t)m;
+    int rc = set_device();
     if (rc) return rc;
-    rc = set_device();
-    if (rc) return rc;
-    // per-game table: ub[K+1], vb[K], eb[K], slot[K]
-    std::vector<int32_t> table(4 * (size_t)K + 1);
-    for (int32_t k = 0; k <= K; k++) table[k] = (int32_t)base[k];
-    for (int32_t k = 0; k < K; k++) {
-        table[K + 1 + k] = vb[k];
-        table[2 * K + 1 + k] = eb[k];
-        table[3 * K + 1 + k] = slot[k];
-    }
-    const int64_t n = u.n, m = u.m;
     int32_t *d_tab = nullptr, *u_owner = nullptr, *u_pri = nullptr, *u_off = nullptr, *u_tgt = nullptr,
             *u_roff = nullptr, *u_rsrc = nullptr;
     int32_t **bufs[] = {&d_tab, &u_owner, &u_pri, &u_off, &u_tgt, &u_roff, &u_rsrc};
     const size_t sizes[] = {4 * table.size(),   4 * (size_t)n,       4 * (size_t)n,      4 * ((size_t)n + 1),
                             4 * (size_t)m,      4 * ((size_t)n + 1), 4 * (size_t)m};
-    const void *src[] = {table.data(), u.owner.data(), u.priority.data(), u.offsets.data(), u.targets.data()};
     cudaError_t e = cudaSuccess;
     int64_t mr = 0;
     int ce = 0;
     for (int i = 0; i < 7 && e == cudaSuccess; i++) e = device_alloc((void **)bufs[i], sizes[i], stream_);
-    for (int i = 0; i < 5 && e == cudaSuccess; i++)
-        e = cudaMemcpyAsync(*bufs[i], src[i], sizes[i], cudaMemcpyHostToDevice, stream_);
-    if (e == cudaSuccess) ce = build_reverse_csr(stream_, (int32_t)n, m, u_off, u_tgt, u_roff, u_rsrc, &mr);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_tab, table.data(), sizes[0], cudaMemcpyHostToDevice, stream_);
+    for (int32_t k = 0; k < K && e == cudaSuccess; k++) {
+        const HostGame &g = *gs[k];
+        const size_t nb = 4 * (size_t)g.n;
+        e = cudaMemcpyAsync(u_owner + ub[k], g.owner.data(), nb, cudaMemcpyHostToDevice, stream_);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(u_pri + ub[k], g.priority.data(), nb, cudaMemcpyHostToDevice, stream_);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(u_off + ub[k], g.offsets.data(), nb, cudaMemcpyHostToDevice, stream_);
+        if (e == cudaSuccess && g.m)
+            e = cudaMemcpyAsync(u_tgt + ue[k], g.targets.data(), 4 * (size_t)g.m, cudaMemcpyHostToDevice, stream_);
+    }
+    if (e == cudaSuccess) {
+        launch_union_fixup(stream_, (int32_t)n, m, K, d_tab, d_tab + K + 1, u_off, u_tgt);
+        ce = build_reverse_csr(stream_, (int32_t)n, m, u_off, u_tgt, u_roff, u_rsrc, &mr);
+    }
     if (e == cudaSuccess && !ce) {
         e = cudaMemsetAsync(&dw_->ucount, 0, sizeof(int32_t), stream_);   // the unreached list is stale
-        launch_arena_place(stream_, (int32_t)n, K, d_tab, d_tab + K + 1, d_tab + 2 * K + 1, d_tab + 3 * K + 1,
-                           u_owner, u_pri, u_off, u_tgt, u_roff, u_rsrc, owner_, pri_, off_, tgt_, rev_off_, rev_src_,
-                           strat_, st_, solved_, game_of_, gstate_, gcount_);
+        if (extent != n_) launch_move_extent(stream_, n_, extent, succ_);
+        const int32_t *vbd = d_tab + 2 * K + 2, *ebd = d_tab + 3 * K + 2, *sld = d_tab + 4 * K + 2;
+        launch_arena_place(stream_, (int32_t)n, K, d_tab, vbd, ebd, sld, u_owner, u_pri, u_off, u_tgt, u_roff, u_rsrc,
+                           owner_, pri_, off_, tgt_, rev_off_, rev_src_, strat_, st_, solved_, game_of_, gstate_,
+                           gcount_, succ_, dirty_);
         if (e == cudaSuccess) e = cudaGetLastError();
-        if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
     }
     for (int i = 0; i < 7; i++)
         if (*bufs[i]) cudaFreeAsync(*bufs[i], stream_);
     if (ce) return fail(PSI_ERR_CUDA, std::string("reverse CSR: ") + cudaGetErrorString((cudaError_t)ce));
     if (e != cudaSuccess) return fail(PSI_ERR_CUDA, std::string("arena_add: ") + cudaGetErrorString(e));
-    if (u.max_pri > max_pri_) max_pri_ = u.max_pri;
+    if (top > max_pri_) max_pri_ = top;
     set_extent(extent);
-    tour_valid_ = false;
     return sync_and_check("arena_add");
 }
 
-int Solver::arena_remove(int32_t vb, int32_t count, int32_t slot, int32_t extent)
+// Retires games: their ranges become inert and leave the tour (one
+// synchronisation for all of them).
+int Solver::arena_remove(const std::vector<int32_t> &vb, const std::vector<int32_t> &count,
+                         const std::vector<int32_t> &slot, int32_t extent)
 {
     if (!arena_) return fail(PSI_ERR_STATE, "not an arena");
-    if (slot < 0 || slot >= games_ || vb < 0 || (int64_t)vb + count > cap_n_)
-        return fail(PSI_ERR_INVALID, "arena range out of range");
+    const size_t K = vb.size();
+    if (count.size() != K || slot.size() != K || extent > cap_n_) return fail(PSI_ERR_INVALID, "arena lists disagree");
+    for (size_t k = 0; k < K; k++)
+        if (slot[k] < 0 || slot[k] >= games_ || vb[k] < 0 || count[k] < 0 || (int64_t)vb[k] + count[k] > cap_n_)
+            return fail(PSI_ERR_INVALID, "arena range out of range");
     int rc = set_device();
     if (rc) return rc;
-    launch_arena_clear(stream_, vb, count, solved_, game_of_, st_);
-    PSI_CUDA_TRY(cudaMemsetAsync(gstate_ + slot, 0, sizeof(int4), stream_));
+    for (size_t k = 0; k < K; k++) {
+        launch_arena_clear(stream_, vb[k], count[k], solved_, game_of_, st_, succ_, dirty_);
+        PSI_CUDA_TRY(cudaMemsetAsync(gstate_ + slot[k], 0, sizeof(int4), stream_));
+    }
     PSI_CUDA_TRY(cudaMemsetAsync(&dw_->ucount, 0, sizeof(int32_t), stream_));
+    if (extent != n_) launch_move_extent(stream_, n_, extent, succ_);
     set_extent(extent);
-    tour_valid_ = false;
     return sync_and_check("arena_remove");
+}
+
+// Copies a game's strategy and status words out (no synchronisation; the
+// host buffers are complete after the next synchronising call).
+int Solver::arena_fetch(int32_t vb, int32_t count, int32_t *strategy, int32_t *status)
+{
+    if (vb < 0 || count < 0 || (int64_t)vb + count > n_) return fail(PSI_ERR_INVALID, "arena range out of range");
+    if (count == 0) return PSI_OK;
+    PSI_CUDA_TRY(cudaMemcpyAsync(strategy, strat_ + vb, 4 * (size_t)count, cudaMemcpyDeviceToHost, stream_));
+    PSI_CUDA_TRY(cudaMemcpyAsync(status, st_ + vb, 4 * (size_t)count, cudaMemcpyDeviceToHost, stream_));
+    return PSI_OK;
 }
 
 // Player lists of the vertices that belong to games (Even's first).

@@ -28,6 +28,10 @@ struct SolverTimes {
     int64_t unreached = 0, jump_rounds = 0;
 };
 
+// Status word -> +1 / -1 / 0 as CPUParity's infinite[] (device_common.cuh:
+// -2 = +inf, -1 = -inf, depth >= 1 = finite).
+inline int32_t status_infinite(int32_t st) { return st == -2 ? 1 : (st == -1 ? -1 : 0); }
+
 // Control words of the graph-driven solve loop (solver_graph.cu), on the device.
 struct GraphCtl {
     enum { kRunning = 0, kConverged = 1, kEvalCap = 2, kRunaway = 3 };
@@ -99,7 +103,9 @@ public:
     // places several games at once (game k at vb[k], eb[k] in slot[k]).
     int arena_add(const std::vector<const HostGame *> &gs, const std::vector<int32_t> &vb,
                   const std::vector<int32_t> &eb, const std::vector<int32_t> &slot, int32_t extent);
-    int arena_remove(int32_t vb, int32_t count, int32_t slot, int32_t extent);
+    int arena_remove(const std::vector<int32_t> &vb, const std::vector<int32_t> &count,
+                     const std::vector<int32_t> &slot, int32_t extent);
+    int arena_fetch(int32_t vb, int32_t count, int32_t *strategy, int32_t *status);
     int arena_rebuild_lists();
     // One solve_si step of every resident game (its reset variant when `reset`);
     // `done` receives the slots that finished in this step with their
