@@ -8,6 +8,9 @@
 //   psi::GPUList        ~ GPUList(Game&, GPUGame&) (gpu_list_ranking.h:11-41):
 //                          the GPU solver; constructing it uploads the game
 //   psi::solve_si       ~ solve_si (main.cpp:20-55, gpumain.cpp:18-53)
+// and, without counterparts in the reference: psi::Batch (many games solved
+// together), psi::Server (continuous batching) and psi::check_solution (a
+// certificate check of a result).
 // Failures become psi::Error exceptions carrying the C ABI status and message
 // (the reference exits on CUDA errors, gpu_util.cpp:10-17, and throws
 // const char* on parse errors, game.cpp:68-105).
@@ -17,6 +20,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "psi.h"
@@ -191,6 +195,103 @@ public:
 private:
     psi_solver *s_ = nullptr;
     int32_t n_ = 0;
+};
+
+// Certificate check of a solution (psi_check_solution): PSI_CHECK_OK or the
+// failed check; *vertex receives the offending vertex, if any.
+inline int check_solution(const Game &g, const std::vector<int32_t> &strategy, const std::vector<int32_t> &infinite,
+                          int64_t *vertex = nullptr, int64_t work_budget = 0)
+{
+    psi_check_report r;
+    check(psi_check_solution(g.handle(), strategy.data(), infinite.data(), work_budget, &r));
+    if (vertex) *vertex = r.vertex;
+    return r.status;
+}
+
+// Many games solved together (psi_batch_*); each ends with its solo results.
+class Batch {
+public:
+    explicit Batch(const std::vector<const Game *> &games, const psi_options *opt = nullptr)
+    {
+        std::vector<const psi_game *> hs;
+        for (const Game *g : games) {
+            hs.push_back(g->handle());
+            sizes_.push_back(g->get_n_vertices());
+        }
+        check(psi_batch_create(hs.data(), (int32_t)hs.size(), opt, &b_));
+    }
+    Batch(const Batch &) = delete;
+    Batch &operator=(const Batch &) = delete;
+    ~Batch() { psi_batch_destroy(b_); }
+    // (iteration, evaluation) counts per game
+    void solve(std::vector<int32_t> &iters, std::vector<int32_t> &brs)
+    {
+        iters.assign(sizes_.size(), 0);
+        brs.assign(sizes_.size(), 0);
+        check(psi_batch_solve(b_, iters.data(), brs.data()));
+    }
+    std::vector<int32_t> get_strategy(int32_t game)
+    {
+        std::vector<int32_t> s((size_t)sizes_.at(game));
+        check(psi_batch_get_strategy(b_, game, s.data()));
+        return s;
+    }
+
+private:
+    psi_batch *b_ = nullptr;
+    std::vector<int32_t> sizes_;
+};
+
+// Continuous-batching server (psi_server_*): submit at any time, step, take.
+class Server {
+public:
+    Server(int64_t max_vertices, int64_t max_edges, int32_t max_games, bool reset = false,
+           const psi_options *opt = nullptr)
+    {
+        check(psi_server_create(max_vertices, max_edges, max_games, reset ? 1 : 0, opt, &s_));
+    }
+    Server(const Server &) = delete;
+    Server &operator=(const Server &) = delete;
+    ~Server() { psi_server_destroy(s_); }
+    int64_t submit(const Game &g)
+    {
+        int64_t t = 0;
+        check(psi_server_submit(s_, g.handle(), &t));
+        sizes_.push_back({t, g.get_n_vertices()});
+        return t;
+    }
+    int32_t step()
+    {
+        int32_t k = 0;
+        check(psi_server_step(s_, &k));
+        return k;
+    }
+    bool finished(int64_t ticket, int32_t *iters = nullptr, int32_t *brs = nullptr)
+    {
+        int32_t state = 0;
+        check(psi_server_status(s_, ticket, &state, iters, brs));
+        return state == PSI_REQ_FINISHED;
+    }
+    // strategy and infinity flags of a finished request, in its own vertex ids
+    void take(int64_t ticket, std::vector<int32_t> &strategy, std::vector<int32_t> &infinite)
+    {
+        int32_t n = 0;
+        for (const auto &p : sizes_)
+            if (p.first == ticket) n = p.second;
+        strategy.assign((size_t)n, 0);
+        infinite.assign((size_t)n, 0);
+        check(psi_server_take(s_, ticket, strategy.data(), infinite.data()));
+    }
+    bool idle()
+    {
+        int32_t resident = 0, queued = 0;
+        check(psi_server_info(s_, &resident, &queued, nullptr, nullptr));
+        return resident == 0 && queued == 0;
+    }
+
+private:
+    psi_server *s_ = nullptr;
+    std::vector<std::pair<int64_t, int32_t>> sizes_;
 };
 
 // The reference driver loop (main.cpp:20-55) over any StrategyImprovement.

@@ -3,6 +3,8 @@
 // written against include/psi_si.hpp.  Built and run by tests/test_cpp_driver.py.
 //   drop_in_driver parse <game.gm>   -> "n m max_pri" (no GPU needed)
 //   drop_in_driver solve <game.gm>   -> "time iters brs" then the W0 size
+//   drop_in_driver serve <game.gm>   -> the same game through Batch and Server:
+//                                       "iters brs" of each and the certificate status
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -22,6 +24,21 @@ int main(int argc, char **argv)
         g.parse_pgsolver(argv[2]);
         if (std::strcmp(argv[1], "parse") == 0) {
             std::printf("%d %lld %d\n", g.get_n_vertices(), (long long)g.get_n_edges(), g.get_max_pri());
+            return 0;
+        }
+        if (std::strcmp(argv[1], "serve") == 0) {
+            std::vector<const psi::Game *> one{&g};
+            psi::Batch b(one);
+            std::vector<int32_t> bi, bb;
+            b.solve(bi, bb);
+            psi::Server srv(2 * (int64_t)g.get_n_vertices() + 2, 2 * g.get_n_edges() + 2, 4);
+            int64_t t = srv.submit(g);
+            while (!srv.idle()) srv.step();
+            int32_t si_ = 0, sb = 0;
+            srv.finished(t, &si_, &sb);
+            std::vector<int32_t> strat, inf;
+            srv.take(t, strat, inf);
+            std::printf("%d %d\n%d %d\n%d\n", bi[0], bb[0], si_, sb, psi::check_solution(g, strat, inf));
             return 0;
         }
         psi::GPUList si(g);

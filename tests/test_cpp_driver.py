@@ -51,3 +51,16 @@ def test_cpp_driver_solves_like_the_oracle(driver, tmp_path):
     o = oracle.Oracle(*g.csr())
     assert (int(iters), int(brs)) == o.solve()
     assert int(w0) == o.get_winning(0).size
+
+
+@pytest.mark.gpu
+def test_cpp_batch_server_and_check(driver, tmp_path):
+    g = make("c4", 3000, 17)
+    o = oracle.Oracle(*g.csr())
+    it_br = o.solve()
+    o.close()
+    out = subprocess.run([driver, "serve", write_game(tmp_path, g)], capture_output=True, text=True, check=True)
+    lines = out.stdout.split("\n")
+    assert tuple(map(int, lines[0].split())) == it_br    # batch
+    assert tuple(map(int, lines[1].split())) == it_br    # server
+    assert int(lines[2]) == 0                            # PSI_CHECK_OK
