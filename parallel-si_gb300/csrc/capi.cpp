@@ -381,25 +381,17 @@ int psi_batch_create(const psi_game *const *games, int32_t count, const psi_opti
         if (!games[k]) return psi::fail(PSI_ERR_INVALID, "null game in batch");
         gs.push_back(&games[k]->g);
     }
-    psi::HostGame u;
     std::vector<int64_t> base;
-    int rc = psi::pack_games(gs, u, base);
-    if (rc) return rc;
     psi_options o;
     psi_options_default(&o);
     if (opt) o = *opt;
     psi::Solver *s = nullptr;
-    rc = psi::Solver::create(psi::view_of(u), o, &s);
+    int rc = psi::Solver::create_union(gs, o, &s, &base);
     if (rc) return rc;
-    rc = s->enable_batch(base);
-    if (rc) {
-        delete s;
-        return rc;
-    }
     psi_batch *b = new psi_batch();
     b->s = s;
     b->base = std::move(base);
-    b->m = u.m;
+    b->m = s->m();
     *out = b;
     return PSI_OK;
     PSI_GUARD_END

@@ -364,42 +364,4 @@ int generate_longpath(int32_t n, int32_t pri_hi, uint64_t seed, HostGame &g)
     return PSI_OK;
 }
 
-// Disjoint union of games: game k's vertices become [base[k], base[k+1]) and
-// its successor ids are shifted by base[k].
-int pack_games(const std::vector<const HostGame *> &games, HostGame &out, std::vector<int64_t> &base)
-{
-    out = HostGame();
-    base.assign(1, 0);
-    int64_t n = 0, m = 0;
-    int32_t mp = 0;
-    for (const HostGame *g : games) {
-        if (!g || g->n <= 0) return fail(PSI_ERR_INVALID, "empty game in batch");
-        n += g->n;
-        m += g->m;
-        mp = g->max_pri > mp ? g->max_pri : mp;
-        base.push_back(n);
-    }
-    if (2 * n + 2 > INT32_MAX) return fail(PSI_ERR_TOO_LARGE, "batch has too many vertices for int32 tour ids");
-    if (m > INT32_MAX) return fail(PSI_ERR_TOO_LARGE, "batch has more than 2^31-1 edges");
-    out.n = (int32_t)n;
-    out.m = m;
-    out.max_pri = mp;
-    out.owner.reserve(n);
-    out.priority.reserve(n);
-    out.offsets.reserve(n + 1);
-    out.targets.reserve(m);
-    int32_t eoff = 0;
-    for (size_t k = 0; k < games.size(); k++) {
-        const HostGame &g = *games[k];
-        int32_t vb = (int32_t)base[k];
-        out.owner.insert(out.owner.end(), g.owner.begin(), g.owner.end());
-        out.priority.insert(out.priority.end(), g.priority.begin(), g.priority.end());
-        for (int32_t v = 0; v < g.n; v++) out.offsets.push_back(eoff + g.offsets[v]);
-        for (int64_t e = 0; e < g.m; e++) out.targets.push_back(vb + g.targets[e]);
-        eoff += (int32_t)g.m;
-    }
-    out.offsets.push_back(eoff);
-    return PSI_OK;
-}
-
 }  // namespace psi

@@ -75,7 +75,6 @@ int make_game(int32_t n, const int32_t *owner, const int32_t *priority, const in
               const int32_t *targets, HostGame &g);
 int generate_random(int32_t n, int32_t deg_lo, int32_t deg_hi, int32_t pri_hi, uint64_t seed, HostGame &g);
 int generate_longpath(int32_t n, int32_t pri_hi, uint64_t seed, HostGame &g);
-int pack_games(const std::vector<const HostGame *> &games, HostGame &out, std::vector<int64_t> &base);
 
 }  // namespace psi
 

@@ -123,9 +123,10 @@ void launch_arena_place(cudaStream_t s, int32_t nu, int32_t k_games, const int32
                         int32_t *strat, int32_t *st, uint8_t *solved, int32_t *game_of, int4 *gstate,
                         unsigned long long *gcount, int32_t *succ, uint8_t *dirty);
 // Games copied as they are into a union (game k at vertices ub[k], edges
-// ue[k]): offsets and targets shifted to union numbering; u_off[nu] = ue[K].
+// ue[k]): offsets and targets shifted to union numbering, u_off[nu] = ue[K],
+// and game_of[v] = v's game when game_of != nullptr.
 void launch_union_fixup(cudaStream_t s, int32_t nu, int64_t mu, int32_t k_games, const int32_t *ub, const int32_t *ue,
-                        int32_t *u_off, int32_t *u_tgt);
+                        int32_t *u_off, int32_t *u_tgt, int32_t *game_of = nullptr);
 // Tour upkeep of the arena: every slot an isolated pair; the sink's nodes
 // following the vertex count from old_n to new_n.
 void launch_isolate_pairs(cudaStream_t s, int64_t count, int32_t *succ);

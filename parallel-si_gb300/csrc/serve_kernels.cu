@@ -86,13 +86,13 @@ __global__ void k_arena_place(int32_t nu, int32_t k_games, const int32_t *__rest
     }
 }
 
-// Union staging: each admitted game was copied as it is (its own offsets and
-// vertex ids) to its place in the union; shift offsets by the game's first
-// edge and targets by its first vertex.  ub/ue: first vertex / edge of game k
-// in the union (K+1 entries each).
+// Union staging: each game was copied as it is (its own offsets and vertex
+// ids) to its place in the union; shift offsets by the game's first edge and
+// targets by its first vertex, and (game_of != nullptr) record each vertex's
+// game.  ub/ue: first vertex / edge of game k in the union (K+1 entries each).
 __global__ void k_union_fixup(int32_t nu, int64_t mu, int32_t k_games, const int32_t *__restrict__ ub,
                               const int32_t *__restrict__ ue, int32_t *__restrict__ u_off,
-                              int32_t *__restrict__ u_tgt)
+                              int32_t *__restrict__ u_tgt, int32_t *__restrict__ game_of)
 {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nu; i += stride) {
@@ -103,6 +103,7 @@ __global__ void k_union_fixup(int32_t nu, int64_t mu, int32_t k_games, const int
             else hi = mid;
         }
         u_off[i] += ue[lo];
+        if (game_of) game_of[i] = lo;
     }
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < mu; e += stride) {
         int32_t lo = 0, hi = k_games;   // largest k with ue[k] <= e
@@ -256,12 +257,12 @@ void launch_arena_place(cudaStream_t s, int32_t nu, int32_t k_games, const int32
 }
 
 void launch_union_fixup(cudaStream_t s, int32_t nu, int64_t mu, int32_t k_games, const int32_t *ub, const int32_t *ue,
-                        int32_t *u_off, int32_t *u_tgt)
+                        int32_t *u_off, int32_t *u_tgt, int32_t *game_of)
 {
     count_launch();
     unsigned g = grid_for(nu > mu ? nu : mu);
     g = g < 2432u ? g : 2432u;
-    k_union_fixup<<<g, kBlock, 0, s>>>(nu, mu, k_games, ub, ue, u_off, u_tgt);
+    k_union_fixup<<<g, kBlock, 0, s>>>(nu, mu, k_games, ub, ue, u_off, u_tgt, game_of);
 }
 
 void launch_isolate_pairs(cudaStream_t s, int64_t count, int32_t *succ)

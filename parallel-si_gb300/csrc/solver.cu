@@ -88,6 +88,89 @@ int Solver::create_arena(int64_t max_vertices, int64_t max_edges, int32_t slots,
     return PSI_OK;
 }
 
+// Many games as one disjoint union (a batch): each game's arrays are copied
+// as they are to their place in the device union and shifted there (no host
+// packing); base receives the first vertex of every game (K+1 entries).
+int Solver::create_union(const std::vector<const HostGame *> &gs, const psi_options &opt, Solver **out,
+                         std::vector<int64_t> *base)
+{
+    *out = nullptr;
+    const int32_t K = (int32_t)gs.size();
+    if (K < 1) return fail(PSI_ERR_INVALID, "empty batch");
+    std::vector<int32_t> table(2 * (size_t)K + 2);
+    int32_t *ub = table.data(), *ue = ub + K + 1;
+    int64_t n = 0, m = 0;
+    int32_t top = 0;
+    base->assign(1, 0);
+    for (int32_t k = 0; k < K; k++) {
+        const HostGame *g = gs[k];
+        if (!g || g->n <= 0) return fail(PSI_ERR_INVALID, "empty game in batch");
+        ub[k] = (int32_t)n;
+        ue[k] = (int32_t)m;
+        n += g->n;
+        m += g->m;
+        top = g->max_pri > top ? g->max_pri : top;
+        base->push_back(n);
+        if (2 * n + 2 > INT32_MAX) return fail(PSI_ERR_TOO_LARGE, "batch has too many vertices for int32 tour ids");
+        if (m > INT32_MAX) return fail(PSI_ERR_TOO_LARGE, "batch has more than 2^31-1 edges");
+    }
+    ub[K] = (int32_t)n;
+    ue[K] = (int32_t)m;
+    int rc = check_options(opt);
+    if (rc) return rc;
+    Solver *s = new Solver();
+    s->device_ = opt.device;
+    s->timing_ = opt.timing != 0;
+    s->stride_ = opt.sublist_len;
+    s->use_graph_ = opt.graph != 0;
+    rc = s->alloc_arrays(n, m);
+    if (!rc) rc = s->upload_union(gs, table, base->back());
+    if (rc) {
+        delete s;
+        return rc;
+    }
+    s->max_pri_ = top;
+    *out = s;
+    return PSI_OK;
+}
+
+int Solver::upload_union(const std::vector<const HostGame *> &gs, const std::vector<int32_t> &table, int64_t n)
+{
+    const int32_t K = (int32_t)gs.size();
+    const int32_t *ub = table.data(), *ue = ub + K + 1;
+    set_extent((int32_t)n);
+    m_ = ue[K];
+    np_ = n_;
+    const struct {
+        void **ptr;
+        size_t bytes;
+    } arrays[] = {{(void **)&game_of_, 4 * (size_t)n_}, {(void **)&gstate_, sizeof(int4) * (size_t)K},
+                  {(void **)&gcount_, sizeof(unsigned long long) * (size_t)K}};
+    for (const auto &a : arrays) {
+        cudaError_t e = device_alloc(a.ptr, a.bytes, stream_);
+        if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
+        allocs_.push_back(*a.ptr);
+    }
+    int32_t *d_tab = nullptr;
+    PSI_CUDA_TRY(device_alloc((void **)&d_tab, 4 * table.size(), stream_));
+    PSI_CUDA_TRY(cudaMemcpyAsync(d_tab, table.data(), 4 * table.size(), cudaMemcpyHostToDevice, stream_));
+    for (int32_t k = 0; k < K; k++) {
+        const HostGame &g = *gs[k];
+        const size_t nb = 4 * (size_t)g.n;
+        PSI_CUDA_TRY(cudaMemcpyAsync(st_ + ub[k], g.owner.data(), nb, cudaMemcpyHostToDevice, stream_));
+        PSI_CUDA_TRY(cudaMemcpyAsync(pri_ + ub[k], g.priority.data(), nb, cudaMemcpyHostToDevice, stream_));
+        PSI_CUDA_TRY(cudaMemcpyAsync(off_ + ub[k], g.offsets.data(), nb, cudaMemcpyHostToDevice, stream_));
+        if (g.m)
+            PSI_CUDA_TRY(cudaMemcpyAsync(tgt_ + ue[k], g.targets.data(), 4 * (size_t)g.m, cudaMemcpyHostToDevice,
+                                         stream_));
+    }
+    launch_union_fixup(stream_, n_, m_, K, d_tab, d_tab + K + 1, off_, tgt_, game_of_);
+    PSI_CUDA_TRY(cudaMemsetAsync(gcount_, 0, 8 * (size_t)K, stream_));
+    cudaFreeAsync(d_tab, stream_);
+    games_ = K;
+    return finish_upload();
+}
+
 // Vertex count the kernels process: the tour has 2n+2 nodes, the sublist
 // heads follow from the stride.
 void Solver::set_extent(int32_t n)
@@ -181,6 +264,13 @@ int Solver::upload_game(const CsrView &g, bool validate)
         if (bad_e) return fail(PSI_ERR_INVALID, "successor out of range");
         max_pri_ = top;
     }
+    return finish_upload();
+}
+
+// Common tail of an upload: the owner array (uploaded as int32 into st_)
+// narrowed, the player lists, fresh SI state and the reverse CSR.
+int Solver::finish_upload()
+{
     launch_narrow_owner(stream_, n_, st_, owner_);
     int ce = partition_players(stream_, n_, owner_, plist_, &dw_->sinkcount);
     if (ce) return fail(PSI_ERR_CUDA, std::string("player lists: ") + cudaGetErrorString((cudaError_t)ce));
@@ -570,35 +660,6 @@ int Solver::solve(int32_t reset, int32_t *iters, int32_t *brs, int64_t max_evals
     }
     *iters = it;
     *brs = br;
-    return PSI_OK;
-}
-
-int Solver::enable_batch(const std::vector<int64_t> &base)
-{
-    if (games_) return fail(PSI_ERR_STATE, "batch partition already set");
-    int32_t g = (int32_t)base.size() - 1;
-    if (g < 1 || base[0] != 0 || base[g] != n_) return fail(PSI_ERR_INVALID, "batch partition does not cover the game");
-    int rc = set_device();
-    if (rc) return rc;
-    std::vector<int32_t> game_of(n_);
-    for (int32_t k = 0; k < g; k++) {
-        if (base[k + 1] <= base[k]) return fail(PSI_ERR_INVALID, "empty game in batch");
-        for (int64_t v = base[k]; v < base[k + 1]; v++) game_of[v] = k;
-    }
-    const struct {
-        void **ptr;
-        size_t bytes;
-    } arrays[] = {{(void **)&game_of_, 4 * (size_t)n_}, {(void **)&gstate_, sizeof(int4) * (size_t)g},
-                  {(void **)&gcount_, sizeof(unsigned long long) * (size_t)g}};
-    for (const auto &a : arrays) {
-        cudaError_t e = device_alloc(a.ptr, a.bytes, stream_);
-        if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
-        allocs_.push_back(*a.ptr);
-    }
-    PSI_CUDA_TRY(cudaMemcpyAsync(game_of_, game_of.data(), 4 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
-    PSI_CUDA_TRY(cudaMemsetAsync(gcount_, 0, 8 * (size_t)g, stream_));
-    PSI_CUDA_TRY(cudaStreamSynchronize(stream_));
-    games_ = g;
     return PSI_OK;
 }
 

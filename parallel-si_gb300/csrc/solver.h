@@ -51,6 +51,10 @@ public:
     // slots (each game takes n+1), max_edges edges, `slots` games at a time.
     static int create_arena(int64_t max_vertices, int64_t max_edges, int32_t slots, const psi_options &opt,
                             Solver **out);
+    // A batch: the disjoint union of gs, game k owning vertices
+    // [base[k], base[k+1]) (solve_batch accounts per game).
+    static int create_union(const std::vector<const HostGame *> &gs, const psi_options &opt, Solver **out,
+                            std::vector<int64_t> *base);
     ~Solver();
 
     // The StrategyImprovement interface (si.h:6-16).
@@ -90,10 +94,10 @@ public:
     int timer_begin();
     int timer_end(double *ms);
 
-    // Batches: the solver's game is a disjoint union of games, game g owning
-    // vertices [base[g], base[g+1]).  solve_batch runs solve_si over the union
-    // and returns each game's own iteration and evaluation counts.
-    int enable_batch(const std::vector<int64_t> &base);
+    // Batches (create_union): the solver's game is a disjoint union of games,
+    // game g owning vertices [base[g], base[g+1]).  solve_batch runs solve_si
+    // over the union and returns each game's own iteration and evaluation
+    // counts.
     int solve_batch(int32_t *iters, int32_t *brs);
     int32_t batch_games() const { return games_; }
 
@@ -117,6 +121,8 @@ private:
     Solver() = default;
     int alloc_arrays(int64_t cap_n, int64_t cap_m);
     int upload_game(const CsrView &g, bool validate);
+    int upload_union(const std::vector<const HostGame *> &gs, const std::vector<int32_t> &table, int64_t n);
+    int finish_upload();
     int init_arena(int32_t slots);
     void set_extent(int32_t n);
     int sync_and_check(const char *what);
