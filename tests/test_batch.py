@@ -58,3 +58,33 @@ def test_batch_solve_is_repeatable():
     again = b.solve()
     assert all(np.array_equal(x, y) for x, y in zip(first, again))
     assert all(np.array_equal(s, b.get_strategy(k)) for k, s in enumerate(strats))
+
+
+def test_batch_rejects_empty_and_missing_games_before_device_use():
+    import ctypes as C
+    from psi._lib import lib, PSI_ERR_INVALID
+    good = psi.Game.random(50, 2, 4, 50, 1)
+    empty = psi.Game.parse_text("parity -1;\n")
+    h = C.c_void_p()
+    arr = (C.c_void_p * 2)(good._h.value, empty._h.value)
+    assert lib.psi_batch_create(C.cast(arr, C.c_void_p), 2, None, C.byref(h)) == PSI_ERR_INVALID
+    arr = (C.c_void_p * 2)(good._h.value, None)
+    assert lib.psi_batch_create(C.cast(arr, C.c_void_p), 2, None, C.byref(h)) == PSI_ERR_INVALID
+    assert lib.psi_batch_create(C.cast(arr, C.c_void_p), 0, None, C.byref(h)) == PSI_ERR_INVALID
+
+
+@pytest.mark.gpu
+def test_batch_of_mixed_families_and_tiny_games_matches_oracle():
+    from games import make, ring10
+    games = [psi.Game.from_csr([1], [3], [0, 1], [0]), ring10(), make("c3", 3000, 5), make("smallpri", 2000, 6),
+             psi.Game.from_csr([0], [2], [0, 1], [0]), make("c1", 4000, 7), make("c2", 100, 8)]
+    b = psi.Batch(games)
+    it, br = b.solve()
+    for k, g in enumerate(games):
+        o = oracle.Oracle(*g.csr())
+        assert (it[k], br[k]) == o.solve(), f"game {k}"
+        assert np.array_equal(b.get_strategy(k), o.get_strategy()), f"game {k}"
+        assert np.array_equal(b.get_winning(k, 1), o.get_winning(1)), f"game {k}"
+        o.close()
+    single = psi.Batch([games[2]])
+    assert tuple(single.solve()[0]) == (it[2],)

@@ -120,3 +120,43 @@ def test_serve_rejects_games_that_never_fit():
     srv.drain()
     assert srv.status(t)[0] == psi.Server.FINISHED
     check_against(srv, t, oracle_result(g), "n=999")
+
+
+@pytest.mark.gpu
+def test_serve_stress_random_arrivals_and_sizes():
+    """Many admissions and retirements in a small arena (the vertex count of
+    the arena grows and shrinks, ranges are reused at once, tiny games sit
+    next to large ones); every result equals the game's solo GPU solve."""
+    rng = np.random.default_rng(2024)
+    games = []
+    for i in range(90):
+        r = rng.random()
+        if r < 0.15:
+            games.append(psi.Game.from_csr([int(rng.integers(2))], [int(rng.integers(4))], [0, 1], [0]))
+        elif r < 0.25:
+            games.append(ring10())
+        else:
+            n = int(rng.integers(20, 6000))
+            games.append(make(("c1", "c2", "c3", "c4", "smallpri")[i % 5], n, 500 + i))
+    expected = []
+    for g in games:
+        s = psi.GPUList(g)
+        it_br = s.solve()
+        expected.append((it_br, s.get_strategy(), s.get_infinite()))
+        s.close()
+    srv = psi.Server(max_vertices=24000, max_edges=24000 * 8, max_games=10)
+    pending = list(range(len(games)))
+    open_tickets = {}
+    steps = 0
+    while pending or open_tickets:
+        for _ in range(int(rng.integers(0, 4))):
+            if pending:
+                k = pending.pop(0)
+                open_tickets[srv.submit(games[k])] = k
+        srv.step()
+        steps += 1
+        for t in srv.finished():
+            k = open_tickets.pop(int(t))
+            check_against(srv, int(t), expected[k], f"game {k}")
+        assert steps < 20000
+    assert srv.info() == (0, 0, 0, 0)
