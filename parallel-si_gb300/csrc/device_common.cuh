@@ -4,6 +4,8 @@
 
 #include <climits>
 #include <cstdint>
+
+#include "kernels.h"
 #include <cuda_runtime.h>
 
 namespace psi {
@@ -58,6 +60,22 @@ __host__ __device__ __forceinline__ int32_t finite_key(int32_t m, int32_t c)
 __host__ __device__ __forceinline__ int key_infinite(int32_t k)
 {
     return k == KEY_POS_INF ? 1 : (k == KEY_NEG_INF ? -1 : 0);
+}
+
+// Value signature codes of infinite vertices (finite: (rmax, rcnt), rmax >= 0).
+constexpr int32_t SIG_POS_INF = INT32_MIN + 2;
+constexpr int32_t SIG_NEG_INF = INT32_MIN + 1;
+
+// Records v's new value signature; if it changed, flags v's in-neighbours
+// for their next switch step (kernels.h: ChangeTrack).
+__device__ __forceinline__ void note_signature(const ChangeTrack &t, int32_t v, int2 sig)
+{
+    if (!t.sig) return;
+    const int2 old = t.sig[v];
+    if (old.x == sig.x && old.y == sig.y) return;
+    t.sig[v] = sig;
+    const int32_t e1 = t.rev_off[v + 1];
+    for (int32_t e = t.rev_off[v]; e < e1; e++) t.need[t.rev_src[e]] = 1;
 }
 
 // Tour node ids (an Euler tour of the strategy forest, two nodes per vertex):

@@ -99,11 +99,14 @@ __global__ void k_init_strat(int32_t n, const int8_t *__restrict__ owner, const 
 
 __global__ void k_reset_odd(int32_t n, const int8_t *__restrict__ owner, const int32_t *__restrict__ off,
                             const int32_t *__restrict__ tgt, int32_t *__restrict__ strat,
-                            const int32_t *__restrict__ gate)
+                            const int32_t *__restrict__ gate, uint8_t *__restrict__ need)
 {
     if (gate && !*gate) return;
     for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x)
-        if (owner[v] == 1) strat[v] = tgt[off[v]];
+        if (owner[v] == 1) {
+            strat[v] = tgt[off[v]];
+            if (need) need[v] = 1;   // its choice starts over
+        }
 }
 
 // Up node of v points at its own down node; the down node of a vertex that no
@@ -360,7 +363,7 @@ __device__ __forceinline__ void top1_merge(int32_t &m, int32_t &c, int32_t m2, i
 // usually been done already).  A concurrent reader sees either RM_UNKNOWN or
 // the final pair, which is written as one 8-byte store.
 __global__ void k_rootinfo(int32_t n, const int32_t *__restrict__ st, PathNode *__restrict__ node,
-                           int32_t *__restrict__ key, uint32_t *__restrict__ err)
+                           int32_t *__restrict__ key, uint32_t *__restrict__ err, ChangeTrack track)
 {
     int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= n || st[v] < 1) return;
@@ -382,6 +385,7 @@ __global__ void k_rootinfo(int32_t n, const int32_t *__restrict__ st, PathNode *
     }
     *reinterpret_cast<int2 *>(&node[v].rmax) = make_int2(m, c);
     if (key) key[v] = finite_key(m, c);
+    note_signature(track, v, make_int2(m, c));
 }
 
 // ---- cycle parity of the unreached vertices
@@ -402,7 +406,7 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
                             const int32_t *__restrict__ pri, const uint8_t *__restrict__ solved,
                             int32_t *__restrict__ st, int32_t *__restrict__ key, int2 *__restrict__ ja,
                             int2 *__restrict__ jb, int32_t *__restrict__ la, int32_t *__restrict__ lb,
-                            int32_t *__restrict__ cnt, uint32_t *__restrict__ err)
+                            int32_t *__restrict__ cnt, uint32_t *__restrict__ err, const ChangeTrack &track)
 {
     const int64_t tid = GRID ? (int64_t)blockIdx.x * blockDim.x + threadIdx.x : threadIdx.x;
     const int64_t nth = GRID ? (int64_t)gridDim.x * blockDim.x : blockDim.x;
@@ -470,6 +474,7 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
         int32_t su = solved[t] ? st[t] : ((__ldcg(&in[t]).y % 2 == 0) ? ST_POS_INF : ST_NEG_INF);
         st[u] = su;
         if (key) key[u] = (su == ST_POS_INF) ? KEY_POS_INF : KEY_NEG_INF;
+        note_signature(track, u, make_int2(su == ST_POS_INF ? SIG_POS_INF : SIG_NEG_INF, 0));
     }
 }
 
@@ -481,15 +486,16 @@ __global__ void __launch_bounds__(kBlock) k_cycles(const int32_t *__restrict__ u
                                                    int32_t *__restrict__ key, int2 *__restrict__ ja,
                                                    int2 *__restrict__ jb,
                                                    int32_t *__restrict__ la, int32_t *__restrict__ lb,
-                                                   int32_t *__restrict__ cnt, uint32_t *__restrict__ err)
+                                                   int32_t *__restrict__ cnt, uint32_t *__restrict__ err,
+                                                   ChangeTrack track)
 {
     int32_t nu = *ucount;
     if (nu == 0) return;
     if (nu <= kSmallCycles) {
-        if (blockIdx.x == 0) cycles_body<false>(nu, ulist, strat, pri, solved, st, key, ja, jb, la, lb, cnt, err);
+        if (blockIdx.x == 0) cycles_body<false>(nu, ulist, strat, pri, solved, st, key, ja, jb, la, lb, cnt, err, track);
         return;
     }
-    cycles_body<true>(nu, ulist, strat, pri, solved, st, key, ja, jb, la, lb, cnt, err);
+    cycles_body<true>(nu, ulist, strat, pri, solved, st, key, ja, jb, la, lb, cnt, err, track);
 }
 
 // mark_solved restricted to the last evaluation's unreached vertices: every
@@ -565,10 +571,10 @@ void launch_init_strat(cudaStream_t s, int32_t n, const int8_t *owner, const int
 }
 
 void launch_reset_odd(cudaStream_t s, int32_t n, const int8_t *owner, const int32_t *off, const int32_t *tgt,
-                      int32_t *strat, const int32_t *gate)
+                      int32_t *strat, const int32_t *gate, uint8_t *need)
 {
     count_launch();
-    k_reset_odd<<<capped_grid(n), kBlock, 0, s>>>(n, owner, off, tgt, strat, gate);
+    k_reset_odd<<<capped_grid(n), kBlock, 0, s>>>(n, owner, off, tgt, strat, gate, need);
 }
 
 void launch_tour_build(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
@@ -645,15 +651,16 @@ void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const i
     k_broadcast_depth<<<grid_for(n), kBlock, 0, s>>>(n, vloc, fin, strat, pri, solved, st, node, ulist, ucount);
 }
 
-void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, int32_t *key, uint32_t *err)
+void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, int32_t *key, uint32_t *err,
+                     ChangeTrack track)
 {
     count_launch();
-    k_rootinfo<<<grid_for(n), kBlock, 0, s>>>(n, st, node, key, err);
+    k_rootinfo<<<grid_for(n), kBlock, 0, s>>>(n, st, node, key, err, track);
 }
 
 int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, const int32_t *strat,
                   const int32_t *pri, const uint8_t *solved, int32_t *st, int32_t *key, int2 *ja, int2 *jb,
-                  int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err)
+                  int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err, ChangeTrack track)
 {
     static int blocks = 0, blocks_dev = -1;
     int dev = 0;
@@ -664,7 +671,7 @@ int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, c
     }
     void *args[] = {(void *)&ucount, (void *)&ulist, (void *)&strat, (void *)&pri, (void *)&solved,
                     (void *)&st, (void *)&key, (void *)&ja, (void *)&jb, (void *)&la, (void *)&lb, (void *)&cnt,
-                    (void *)&err};
+                    (void *)&err, (void *)&track};
     count_launch();
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_cycles, dim3(blocks), dim3(kBlock), args, 0, s);
     return e == cudaSuccess ? 0 : (int)e;

@@ -10,6 +10,17 @@ namespace psi {
 
 struct PathNode;   // device_common.cuh
 
+// Change tracking between evaluations and switch steps: sig holds each
+// vertex's value signature from the last evaluation ((rmax, rcnt) if finite,
+// an infinity code if not); when an evaluation changes a vertex's signature,
+// its in-neighbours (rev_off/rev_src) get need = 1, and a switch step examines
+// only its player's vertices with need set.  sig == nullptr: no tracking.
+struct ChangeTrack {
+    int2 *sig = nullptr;
+    uint8_t *need = nullptr;
+    const int32_t *rev_off = nullptr, *rev_src = nullptr;
+};
+
 // Launchers taking `gate` (a device word, nullptr = always) enqueue kernels
 // that return at once while *gate == 0: the graph-driven solve loop enqueues
 // every kernel of a step and lets the device decide which ones work.
@@ -51,7 +62,7 @@ int select_winning(cudaStream_t s, int32_t n, int32_t player, const int32_t *st,
 void launch_init_strat(cudaStream_t s, int32_t n, const int8_t *owner, const int32_t *off,
                        const int32_t *tgt, int32_t *strat, int32_t *st);
 void launch_reset_odd(cudaStream_t s, int32_t n, const int8_t *owner, const int32_t *off,
-                      const int32_t *tgt, int32_t *strat, const int32_t *gate = nullptr);
+                      const int32_t *tgt, int32_t *strat, const int32_t *gate = nullptr, uint8_t *need = nullptr);
 
 // ---- evaluation (gpu_list_ranking.cu:52-277)
 // Euler tour of the sink tree, built from scratch.  rev_off/rev_src: distinct
@@ -81,14 +92,15 @@ void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const i
                             int32_t *st, PathNode *node, int32_t *ulist, int32_t *ucount);
 // Root-path summaries (rmax, rcnt) of every reached vertex, also stored as its
 // comparison key when key != nullptr.
-void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, int32_t *key, uint32_t *err);
+void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, int32_t *key, uint32_t *err,
+                     ChangeTrack track = ChangeTrack());
 // Cycle parity of the *ucount vertices in ulist (cooperative launch), also
 // stored as their comparison keys when key != nullptr.  ja, jb: n entries;
 // la, lb: n entries (active lists); cnt: 3 counters.  Returns a cudaError_t
 // value.
 int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, const int32_t *strat,
                   const int32_t *pri, const uint8_t *solved, int32_t *st, int32_t *key, int2 *ja, int2 *jb,
-                  int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err);
+                  int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err, ChangeTrack track = ChangeTrack());
 // mark_solved over the last evaluation's unreached vertices (cpu_parity.cpp:265-274);
 // with game_of/gmask only for games whose mask is set (nullptr: all).
 // Newly solved vertices are flagged in dirty (their children leave the tour).
@@ -101,12 +113,17 @@ void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ul
 // stats[0..3] += compared edges, walk loads, changed vertices, strict
 // improvements; with game_of (batches) also gcount[game] += improvements,
 // and with gmask only vertices of games whose mask is set switch.  The old and
-// the new successor of every changed vertex are flagged in dirty.
+// the new successor of every changed vertex are flagged in dirty.  With need
+// (and list: n entries, list_count: one counter) only the vertices of plist
+// whose need flag is set are examined (ChangeTrack); examined vertices get
+// need = 0, or 1 when a tie at their best successor leaves their choice to a
+// walk that a later evaluation may decide differently.
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player,
                    const int32_t *off, const int32_t *tgt, int32_t *strat, const int32_t *st,
                    const int32_t *key, const PathNode *node, unsigned long long *stats, const int32_t *game_of,
                    unsigned long long *gcount, const int32_t *gmask, uint8_t *dirty, uint32_t *err,
-                   const int32_t *gate = nullptr);
+                   const int32_t *gate = nullptr, uint8_t *need = nullptr, int32_t *list = nullptr,
+                   int32_t *list_count = nullptr);
 // ---- batches: per-game accounting of solve_si (state[g] = brs, iters,
 // odd_done, done; gcount[g] = strict improvements of the last switch step)
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state,
@@ -121,7 +138,7 @@ void launch_arena_place(cudaStream_t s, int32_t nu, int32_t k_games, const int32
                         const int32_t *u_off, const int32_t *u_tgt, const int32_t *u_roff, const int32_t *u_rsrc,
                         int8_t *owner, int32_t *pri, int32_t *off, int32_t *tgt, int32_t *rev_off, int32_t *rev_src,
                         int32_t *strat, int32_t *st, uint8_t *solved, int32_t *game_of, int4 *gstate,
-                        unsigned long long *gcount, int32_t *succ, uint8_t *dirty);
+                        unsigned long long *gcount, int32_t *succ, uint8_t *dirty, int2 *sig, uint8_t *need);
 // Games copied as they are into a union (game k at vertices ub[k], edges
 // ue[k]): offsets and targets shifted to union numbering, u_off[nu] = ue[K],
 // and game_of[v] = v's game when game_of != nullptr.
@@ -144,7 +161,7 @@ void launch_serve_account(cudaStream_t s, int32_t slots, int32_t event, int4 *st
 // switched go back to their first successor.
 void launch_serve_reset_odd(cudaStream_t s, int32_t np, const int32_t *plist, const int32_t *game_of,
                             const int32_t *gmask, const unsigned long long *gcount, const int32_t *off,
-                            const int32_t *tgt, int32_t *strat, uint8_t *dirty);
+                            const int32_t *tgt, int32_t *strat, uint8_t *dirty, uint8_t *need);
 
 // ---- dense valuation rows for export (the reference's ArrayVal layout)
 void launch_materialize(cudaStream_t s, int32_t v0, int32_t count, int32_t d, const int32_t *st,

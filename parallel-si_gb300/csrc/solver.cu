@@ -215,6 +215,8 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
         {(void **)&key_, 4 * (size_t)cap_n},
         {(void **)&succ_, 4 * (size_t)capL},
         {(void **)&dirty_, (size_t)cap_n},
+        {(void **)&sig_, 8 * (size_t)cap_n},
+        {(void **)&need_, (size_t)cap_n},
         {(void **)&ulist_, 4 * (size_t)cap_n},
         {(void **)&vloc_, 8 * (size_t)cap_n},
         {(void **)&redA_, 8 * (size_t)cap_sub},
@@ -276,6 +278,7 @@ int Solver::finish_upload()
     if (ce) return fail(PSI_ERR_CUDA, std::string("player lists: ") + cudaGetErrorString((cudaError_t)ce));
     PSI_CUDA_TRY(cudaMemsetAsync(solved_, 0, n_, stream_));
     PSI_CUDA_TRY(cudaMemsetAsync(st_, 0, 4 * (size_t)n_, stream_));
+    reset_tracking();
     // reverse CSR on the device (distinct in-neighbours, increasing order)
     int64_t rev_m = 0;
     ce = build_reverse_csr(stream_, n_, m_, off_, tgt_, rev_off_, rev_src_, &rev_m);
@@ -369,12 +372,19 @@ int Solver::sync_and_check(const char *what)
     return PSI_OK;
 }
 
+void Solver::reset_tracking()
+{
+    cudaMemsetAsync(need_, 1, (size_t)n_, stream_);
+    cudaMemsetAsync(sig_, 0x80, 8 * (size_t)n_, stream_);   // matches no signature
+}
+
 int Solver::init_strat()
 {
     int rc = set_device();
     if (rc) return rc;
     launch_init_strat(stream_, n_, owner_, off_, tgt_, strat_, st_);
     PSI_CUDA_TRY(cudaMemsetAsync(solved_, 0, n_, stream_));
+    reset_tracking();
     rc = sync_and_check("init_strat");
     if (rc) return rc;
     strat_ready_ = true;
@@ -389,6 +399,7 @@ int Solver::reset_opponent_strategy()
     int rc = set_device();
     if (rc) return rc;
     launch_reset_odd(stream_, n_, owner_, off_, tgt_, strat_);
+    PSI_CUDA_TRY(cudaMemsetAsync(need_, 1, (size_t)n_, stream_));   // Odd's choices start over
     tour_valid_ = false;
     return sync_and_check("reset_opponent_strategy");
 }
@@ -426,14 +437,14 @@ int Solver::compute_valuation()
     //    (ulist held the sink's children until here)
     phase_begin(PH_BROADCAST);
     launch_broadcast_depth(stream_, n_, vloc_, fin, strat_, pri_, solved_, st_, node_, ulist_, &dw_->ucount);
-    launch_rootinfo(stream_, n_, st_, node_, key_, &dw_->err);
+    launch_rootinfo(stream_, n_, st_, node_, key_, &dw_->err, track());
     phase_end(PH_BROADCAST);
     // 4. cycle parity by pointer jumping over the unreached vertices
     phase_begin(PH_CYCLES);
     // the tour's vloc array is free again: it holds the two active lists
     int32_t *la = reinterpret_cast<int32_t *>(vloc_), *lb = la + n_;
     int ce = launch_cycles(stream_, &dw_->ucount, ulist_, strat_, pri_, solved_, st_, key_, jA_, jB_, la, lb,
-                           dw_->cnt, &dw_->err);
+                           dw_->cnt, &dw_->err, track());
     if (ce) return fail(PSI_ERR_CUDA, std::string("cycle kernel launch: ") + cudaGetErrorString((cudaError_t)ce));
     phase_end(PH_CYCLES);
     phase_end(PH_EVAL);
@@ -471,8 +482,9 @@ int Solver::switch_strategy(int32_t player, int64_t *switched)
     phase_begin(PH_SWITCH);
     const int32_t np = (player == 0) ? np0_ : np_ - np0_;
     const int32_t *pl = plist_ + (player == 0 ? 0 : np0_);
+    // jB_ is free until the next cycle pass: it holds the list of vertices to examine
     launch_switch(stream_, np, pl, player, off_, tgt_, strat_, st_, key_, node_, dw_->sw, game_of_, gcount_, gmask_,
-                  dirty_, &dw_->err);
+                  dirty_, &dw_->err, nullptr, need_, reinterpret_cast<int32_t *>(jB_), &dw_->cnt[2]);
     phase_end(PH_SWITCH);
     rc = sync_and_check("switch_strategy");
     if (rc) return rc;
@@ -593,6 +605,7 @@ int Solver::set_strategy(const int32_t *in)
         if (!ok) return fail(PSI_ERR_INVALID, "strategy entry of vertex " + std::to_string(v) + " is not a successor");
     }
     PSI_CUDA_TRY(cudaMemcpyAsync(strat_, in, 4 * (size_t)n_, cudaMemcpyHostToDevice, stream_));
+    reset_tracking();
     PSI_CUDA_TRY(cudaStreamSynchronize(stream_));
     strat_ready_ = true;
     tour_valid_ = false;
@@ -808,7 +821,7 @@ int Solver::arena_add(const std::vector<const HostGame *> &gs, const std::vector
         const int32_t *vbd = d_tab + 2 * K + 2, *ebd = d_tab + 3 * K + 2, *sld = d_tab + 4 * K + 2;
         launch_arena_place(stream_, (int32_t)n, K, d_tab, vbd, ebd, sld, u_owner, u_pri, u_off, u_tgt, u_roff, u_rsrc,
                            owner_, pri_, off_, tgt_, rev_off_, rev_src_, strat_, st_, solved_, game_of_, gstate_,
-                           gcount_, succ_, dirty_);
+                           gcount_, succ_, dirty_, sig_, need_);
         if (e == cudaSuccess) e = cudaGetLastError();
     }
     for (int i = 0; i < 7; i++)
@@ -899,7 +912,7 @@ int Solver::arena_step(bool reset, std::vector<int32_t> &done, std::vector<int32
     if (rc) return rc;
     if (reset)
         launch_serve_reset_odd(stream_, np_ - np0_, plist_ + np0_, game_of_, gmask_, gcount_, off_, tgt_, strat_,
-                               dirty_);
+                               dirty_, need_);
     launch_serve_account(stream_, games_, 2, gstate_, gcount_, gmask_);
     std::vector<int4> st((size_t)games_);
     PSI_CUDA_TRY(cudaMemcpyAsync(st.data(), gstate_, sizeof(int4) * (size_t)games_, cudaMemcpyDeviceToHost, stream_));

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include "game.h"
+#include "kernels.h"
 #include "psi.h"
 
 namespace psi {
@@ -171,6 +172,10 @@ private:
     // evaluation scratch
     int32_t *succ_ = nullptr, *ulist_ = nullptr;
     uint8_t *dirty_ = nullptr;   // parents whose child lists changed since the last evaluation
+    int2 *sig_ = nullptr;        // value signature of the last evaluation (ChangeTrack)
+    uint8_t *need_ = nullptr;    // vertices their owner's next switch step must examine
+    ChangeTrack track() const { return ChangeTrack{sig_, need_, rev_off_, rev_src_}; }
+    void reset_tracking();       // every vertex to be examined, no signature known
     int32_t *rev_off_ = nullptr, *rev_src_ = nullptr;   // distinct in-neighbours (static)
     int2 *vloc_ = nullptr, *redA_ = nullptr, *redB_ = nullptr, *jA_ = nullptr, *jB_ = nullptr;
     int2 *redC_ = nullptr;

@@ -69,7 +69,7 @@ constexpr int32_t kEvalGuard = 1 << 20;
 // One SI step on the stream, no synchronisation (captured into the loop body).
 int Solver::enqueue_step(cudaGraphConditionalHandle loop, bool reset)
 {
-    launch_reset_odd(stream_, n_, owner_, off_, tgt_, strat_, &ctl_->reset);
+    launch_reset_odd(stream_, n_, owner_, off_, tgt_, strat_, &ctl_->reset, need_);
     // evaluation (as compute_valuation, with both tour paths gated)
     PSI_CUDA_TRY(cudaMemsetAsync(&dw_->ucount, 0, 2 * sizeof(int32_t), stream_));   // ucount, sinkcount
     launch_tour_build(stream_, n_, strat_, solved_, rev_off_, rev_src_, succ_, vloc_, ulist_, &dw_->sinkcount, dirty_,
@@ -82,25 +82,26 @@ int Solver::enqueue_step(cudaGraphConditionalHandle loop, bool reset)
     ce = launch_rank_reduced(stream_, nsub_, redA_, redB_, redC_, &fin);
     if (ce) return fail(PSI_ERR_CUDA, std::string("reduced-list kernel: ") + cudaGetErrorString((cudaError_t)ce));
     launch_broadcast_depth(stream_, n_, vloc_, fin, strat_, pri_, solved_, st_, node_, ulist_, &dw_->ucount);
-    launch_rootinfo(stream_, n_, st_, node_, key_, &dw_->err);
+    launch_rootinfo(stream_, n_, st_, node_, key_, &dw_->err, track());
     int32_t *la = reinterpret_cast<int32_t *>(vloc_), *lb = la + n_;
     ce = launch_cycles(stream_, &dw_->ucount, ulist_, strat_, pri_, solved_, st_, key_, jA_, jB_, la, lb, dw_->cnt,
-                       &dw_->err);
+                       &dw_->err, track());
     if (ce) return fail(PSI_ERR_CUDA, std::string("cycle kernel: ") + cudaGetErrorString((cudaError_t)ce));
     count_launch();
     k_ctl_evaluated<<<1, 1, 0, stream_>>>(ctl_);
     // Odd: mark_solved(1), switch(1)
     launch_mark_solved(stream_, &dw_->ucount, ulist_, 1, st_, solved_, dirty_);
     PSI_CUDA_TRY(cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_));
+    int32_t *todo = reinterpret_cast<int32_t *>(jB_);   // free until the next cycle pass
     launch_switch(stream_, np_ - np0_, plist_ + np0_, 1, off_, tgt_, strat_, st_, key_, node_, dw_->sw, nullptr,
-                  nullptr, nullptr, dirty_, &dw_->err);
+                  nullptr, nullptr, dirty_, &dw_->err, nullptr, need_, todo, &dw_->cnt[2]);
     count_launch();
     k_ctl_odd<<<1, 1, 0, stream_>>>(ctl_, dw_->sw);
     // Even, when Odd made no strict improvement: mark_solved(0), switch(0)
     launch_mark_solved(stream_, &dw_->ucount, ulist_, 0, st_, solved_, dirty_, nullptr, nullptr, &ctl_->even);
     PSI_CUDA_TRY(cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_));
     launch_switch(stream_, np0_, plist_, 0, off_, tgt_, strat_, st_, key_, node_, dw_->sw, nullptr, nullptr, nullptr,
-                  dirty_, &dw_->err, &ctl_->even);
+                  dirty_, &dw_->err, &ctl_->even, need_, todo, &dw_->cnt[2]);
     count_launch();
     k_ctl_even<<<1, 1, 0, stream_>>>(ctl_, dw_->sw, loop, reset ? 1 : 0, kEvalGuard);
     PSI_CUDA_TRY(cudaGetLastError());

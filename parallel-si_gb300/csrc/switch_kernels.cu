@@ -134,7 +134,57 @@ __device__ int compare_equal_keys(const PathNode *__restrict__ node, const int32
 // (game_of != nullptr) the strict improvements are also added to
 // gcount[game of the vertex]; with gmask only vertices of games whose mask is
 // set switch.
-__global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__restrict__ plist, int32_t player,
+// The vertices of plist whose need flag is set (and, with gmask, whose game
+// takes this step), appended to list with one atomic per block.
+__global__ void k_need_list(int32_t np, const int32_t *__restrict__ plist, const uint8_t *__restrict__ need,
+                            const int32_t *__restrict__ game_of, const int32_t *__restrict__ gmask,
+                            const int32_t *__restrict__ gate, int32_t *__restrict__ list, int32_t *__restrict__ count)
+{
+    if (gate && !*gate) return;
+    __shared__ int32_t warp_base[kBlock / 32];
+    __shared__ int32_t block_base;
+    for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < np; b0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = b0 + threadIdx.x;
+        int32_t v = -1;
+        bool take = false;
+        if (i < np) {
+            v = plist[i];
+            take = need[v] && (!gmask || gmask[game_of[v]]);
+        }
+        const unsigned mask = __ballot_sync(0xffffffffu, take);
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        if (lane == 0) warp_base[w] = __popc(mask);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int32_t sum = 0;
+            for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
+                int32_t t = warp_base[k];
+                warp_base[k] = sum;
+                sum += t;
+            }
+            block_base = sum ? atomicAdd(count, sum) : 0;
+        }
+        __syncthreads();
+        if (take) list[block_base + warp_base[w] + __popc(mask & ((1u << lane) - 1))] = v;
+        __syncthreads();
+    }
+}
+
+// One thread per vertex of the list (all owned by `player`; the list is plist
+// itself, np entries, or -- with count != nullptr -- the *count vertices
+// k_need_list selected).  Per compared edge the common case is one 4-byte
+// gather (the successor's comparison key) and one integer comparison; equal
+// keys of distinct finite vertices fall back to the exact summaries and,
+// rarely, a walk.  stats[0] += compared edges, stats[1] += parent/priority
+// loads of the walks, stats[2] += vertices whose strategy changed, stats[3]
+// += strict improvements.  For a batch of games (game_of != nullptr) the
+// strict improvements are also added to gcount[game of the vertex]; with
+// gmask only vertices of games whose mask is set switch.  With need, an
+// examined vertex keeps need = 1 only if its best key is shared by two
+// distinct finite vertices (start or successors): its choice then rests on a
+// walk, which depends on more than the signatures tracked between steps.
+__global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__restrict__ plist,
+                                                   const int32_t *__restrict__ count, int32_t player,
                                                    const int32_t *__restrict__ off, const int32_t *__restrict__ tgt,
                                                    int32_t *__restrict__ strat, const int32_t *__restrict__ st,
                                                    const int32_t *__restrict__ key,
@@ -144,10 +194,11 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
                                                    unsigned long long *__restrict__ gcount,
                                                    const int32_t *__restrict__ gmask,
                                                    uint8_t *__restrict__ dirty, uint32_t *__restrict__ err,
-                                                   const int32_t *__restrict__ gate)
+                                                   const int32_t *__restrict__ gate, uint8_t *__restrict__ need)
 {
     if (gate && !*gate) return;
-    // Grid-stride over plist with a bounded grid: the work counters are
+    if (count) np = *count;
+    // Grid-stride over the list with a bounded grid: the work counters are
     // reduced once per block (a few thousand atomics per launch instead of a
     // set per 256 vertices).  A thread sees a few dozen vertices at most, so
     // its own counters fit 32 bits.
@@ -160,6 +211,10 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
         const int32_t e0 = __ldcs(&off[v]), e1 = __ldcs(&off[v + 1]);
         t_edges += e1 - e0;
         int32_t moves = 0;
+        // best key over the start and all successors, and whether a second
+        // distinct vertex attains it (a tie)
+        int32_t ext = kc, ext_v = cur;
+        bool tie = false;
         // Fast pass: successors in batches of kBatch -- all ids, then all
         // keys, before the comparisons (independent gathers in flight per
         // thread).  Equal keys of distinct finite vertices end it; the exact
@@ -178,6 +233,13 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
             for (int j = 0; j < kBatch; j++) {
                 if (j >= cnt) break;
                 const int32_t u = us[j], ku = ks[j];
+                if ((player == 0) ? ku > ext : ku < ext) {
+                    ext = ku;
+                    ext_v = u;
+                    tie = false;
+                } else if (ku == ext && u != ext_v) {
+                    tie = true;
+                }
                 int c;
                 if (ku != kc) {
                     c = ku > kc ? 1 : -1;
@@ -198,8 +260,18 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
             cur = cur0;
             kc = kc0;
             moves = 0;
+            ext = kc0;
+            ext_v = cur0;
+            tie = false;
             for (int32_t e = e0; e < e1; e++) {
                 const int32_t u = tgt[e], ku = key[u];
+                if ((player == 0) ? ku > ext : ku < ext) {
+                    ext = ku;
+                    ext_v = u;
+                    tie = false;
+                } else if (ku == ext && u != ext_v) {
+                    tie = true;
+                }
                 int c;
                 if (ku != kc) c = ku > kc ? 1 : -1;
                 else if (u == cur || key_infinite(ku)) c = 0;
@@ -211,6 +283,7 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
                 }
             }
         }
+        if (need) need[v] = (tie && ext != 0 && !key_infinite(ext)) ? 1 : 0;
         if (moves) {   // strict improvements never return to cur0: cur != cur0
             strat[v] = cur;
             if (cur0 >= 0) dirty[cur0] = 1;
@@ -309,16 +382,26 @@ int switch_grid()
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player, const int32_t *off,
                    const int32_t *tgt, int32_t *strat, const int32_t *st, const int32_t *key, const PathNode *node,
                    unsigned long long *stats, const int32_t *game_of, unsigned long long *gcount,
-                   const int32_t *gmask, uint8_t *dirty, uint32_t *err, const int32_t *gate)
+                   const int32_t *gmask, uint8_t *dirty, uint32_t *err, const int32_t *gate, uint8_t *need,
+                   int32_t *list, int32_t *list_count)
 {
     if (np <= 0) return;
     static int blocks = 0;   // resident blocks on the device (same device for the process's solvers)
     if (blocks == 0) blocks = switch_grid();
     unsigned g = grid_for(np);
     g = g < (unsigned)blocks ? g : (unsigned)blocks;
+    const int32_t *items = plist, *count = nullptr;
+    if (need && list && list_count) {
+        // only the vertices whose need flag is set (ChangeTrack)
+        cudaMemsetAsync(list_count, 0, sizeof(int32_t), s);
+        count_launch();
+        k_need_list<<<g, kBlock, 0, s>>>(np, plist, need, game_of, gmask, gate, list, list_count);
+        items = list;
+        count = list_count;
+    }
     count_launch();
-    k_switch<<<g, kBlock, 0, s>>>(np, plist, player, off, tgt, strat, st, key, node, stats, game_of, gcount, gmask,
-                                  dirty, err, gate);
+    k_switch<<<g, kBlock, 0, s>>>(np, items, count, player, off, tgt, strat, st, key, node, stats, game_of, gcount,
+                                  gmask, dirty, err, gate, need);
 }
 
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state, unsigned long long *gcount)
