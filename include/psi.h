@@ -92,8 +92,20 @@ typedef struct {
                                 graph (device-side loop control, no host synchronisation per
                                 step; same results; records no per-phase times); 0: the
                                 host-driven loop */
-    int32_t reserved[3];
+    int32_t incremental;     /* PSI_INCR_*: whether an evaluation after a switch step that
+                                changed few strategies re-evaluates only the vertices whose
+                                strategy path passes through a changed one (the result is
+                                the same as a full evaluation's) */
+    int32_t reserved[2];
 } psi_options;
+
+/* incremental: PSI_INCR_AUTO (default) patches after steps that changed at
+ * most max(1024, n/1024) strategies, giving up for a full evaluation when
+ * more than max(4096, n/8) vertices or 160 levels of descendants are
+ * affected; PSI_INCR_OFF evaluates in full every time; PSI_INCR_ALWAYS
+ * patches whenever the previous evaluation's state allows it, without the
+ * size limits (n extra entries of device memory per buffer; for tests). */
+enum { PSI_INCR_OFF = 0, PSI_INCR_AUTO = 1, PSI_INCR_ALWAYS = 2 };
 
 void psi_options_default(psi_options *opt);
 
@@ -150,9 +162,11 @@ int psi_solver_times(psi_solver *s, double *eval_ms, double *switch_ms, int64_t 
 int psi_solver_reset_times(psi_solver *s);
 /* Per-phase device times (ms) and call counts, phases in this order:
  * 0 evaluation (whole), 1 switch step, 2 tour build, 3 sublist walk,
- * 4 reduced-list ranking, 5 broadcast, 6 cycle parity. */
+ * 4 reduced-list ranking, 5 broadcast, 6 cycle parity, 7 incremental
+ * evaluation (its kernels; they return at once when the full evaluation
+ * runs, and the full evaluation's when a patch does). */
 enum { PSI_PHASE_EVAL = 0, PSI_PHASE_SWITCH, PSI_PHASE_TOUR, PSI_PHASE_SUBLIST, PSI_PHASE_REDUCED,
-       PSI_PHASE_BROADCAST, PSI_PHASE_CYCLES, PSI_PHASE_COUNT };
+       PSI_PHASE_BROADCAST, PSI_PHASE_CYCLES, PSI_PHASE_PATCH, PSI_PHASE_COUNT };
 int psi_solver_phase_times(psi_solver *s, double *ms, int64_t *calls, int32_t nphases);
 /* The solver's CUDA stream (a cudaStream_t), so callers can order their own
  * work or record events against it. */
@@ -161,8 +175,9 @@ int psi_solver_stream(psi_solver *s, void **stream);
 int psi_solver_unreached(psi_solver *s, int64_t *count);
 /* Work counters since the last reset, in this order: evaluations, switch
  * steps, compared edges, parent/priority loads of the comparison walks,
- * vertices whose strategy changed, unreached vertices (summed over
- * evaluations), pointer-jumping rounds.  Writes min(k, 7) values. */
+ * vertices whose strategy changed, unreached vertices (summed over full
+ * evaluations), pointer-jumping rounds, incremental evaluations (patches),
+ * vertices the patches re-evaluated.  Writes min(k, 9) values. */
 int psi_solver_counters(psi_solver *s, int64_t *out, int32_t k);
 /* Kernel launches issued by this library in this process so far. */
 int64_t psi_launch_count(void);

@@ -173,6 +173,7 @@ void psi_options_default(psi_options *opt)
     opt->sublist_len = 64;
     opt->timing = 1;
     opt->graph = 1;
+    opt->incremental = PSI_INCR_AUTO;
 }
 
 int psi_solver_create(const psi_game *g, const psi_options *opt, psi_solver **out)
@@ -320,7 +321,8 @@ int psi_solver_counters(psi_solver *s, int64_t *out, int32_t k)
 {
     if (!s || !s->s || !out) return psi::fail(PSI_ERR_INVALID, "null argument");
     const psi::SolverTimes &t = s->s->times();
-    const int64_t vals[] = {t.evals, t.switches, t.sw_edges, t.sw_loads, t.sw_changed, t.unreached, t.jump_rounds};
+    const int64_t vals[] = {t.evals,     t.switches,    t.sw_edges, t.sw_loads, t.sw_changed,
+                            t.unreached, t.jump_rounds, t.patches,  t.patched};
     for (int32_t i = 0; i < k && i < (int32_t)(sizeof vals / sizeof vals[0]); i++) out[i] = vals[i];
     return PSI_OK;
 }

@@ -20,6 +20,8 @@ constexpr int32_t ST_NEG_INF = -1;
 constexpr int32_t ST_POS_INF = -2;
 constexpr int32_t ST_UNRESOLVED = INT32_MIN;
 
+constexpr int kBlock = 256;   // threads per block of most kernels
+
 __host__ __device__ __forceinline__ int32_t st_infinite(int32_t st)
 {
     return st == ST_POS_INF ? 1 : (st == ST_NEG_INF ? -1 : 0);
@@ -62,20 +64,92 @@ __host__ __device__ __forceinline__ int key_infinite(int32_t k)
     return k == KEY_POS_INF ? 1 : (k == KEY_NEG_INF ? -1 : 0);
 }
 
-// Value signature codes of infinite vertices (finite: (rmax, rcnt), rmax >= 0).
-constexpr int32_t SIG_POS_INF = INT32_MIN + 2;
-constexpr int32_t SIG_NEG_INF = INT32_MIN + 1;
-
-// Records v's new value signature; if it changed, flags v's in-neighbours
-// for their next switch step (kernels.h: ChangeTrack).
-__device__ __forceinline__ void note_signature(const ChangeTrack &t, int32_t v, int2 sig)
+// Change tracking (kernels.h: ChangeTrack), warp-collective: every lane of a
+// converged warp calls it, and the in-neighbours of each lane's vertex v with
+// `changed` set get need = 1.  The in-edges of the changed lanes are spread
+// over the warp's lanes (their rev_off spans laid end to end), so one round of
+// rev_src loads usually covers them all, instead of one dependent load per
+// in-edge on the changed lanes while the rest of the warp waits.
+__device__ __forceinline__ void flag_in_neighbours(const ChangeTrack &t, bool changed, int32_t v)
 {
-    if (!t.sig) return;
-    const int2 old = t.sig[v];
-    if (old.x == sig.x && old.y == sig.y) return;
-    t.sig[v] = sig;
-    const int32_t e1 = t.rev_off[v + 1];
-    for (int32_t e = t.rev_off[v]; e < e1; e++) t.need[t.rev_src[e]] = 1;
+    if (!t.need || (t.quiet && *t.quiet)) return;
+    constexpr unsigned kAll = 0xffffffffu;
+    const unsigned lanes = __ballot_sync(kAll, changed);
+    if (!lanes) return;
+    const int lane = threadIdx.x & 31;
+    int32_t b = 0, d = 0;
+    if (changed) {
+        b = t.rev_off[v];
+        d = t.rev_off[v + 1] - b;
+    }
+    int32_t incl = d;   // inclusive prefix of d over the lanes
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t x = __shfl_up_sync(kAll, incl, o);
+        if (lane >= o) incl += x;
+    }
+    const int32_t total = __shfl_sync(kAll, incl, 31);   // <= m: distinct vertices' in-edges
+    const int32_t excl = incl - d;
+    for (int64_t j0 = 0; j0 < total; j0 += 32) {
+        const int64_t j = j0 + lane;
+        int64_t e = -1;
+        for (unsigned s = lanes; s; s &= s - 1) {
+            const int l = __ffs(s) - 1;
+            const int32_t el = __shfl_sync(kAll, excl, l), dl = __shfl_sync(kAll, d, l), bl = __shfl_sync(kAll, b, l);
+            if (j >= el && j < (int64_t)el + dl) e = bl + (j - el);
+        }
+        if (e >= 0) t.need[t.rev_src[e]] = 1;
+    }
+}
+
+// (max, count of max) of the union of two priority multisets
+__device__ __forceinline__ void top1_merge(int32_t &m, int32_t &c, int32_t m2, int32_t c2)
+{
+    if (m2 > m) {
+        m = m2;
+        c = c2;
+    } else if (m2 == m) {
+        c += c2;
+    }
+}
+
+// Block-aggregated append: every thread of the block calls it (no early
+// return before); one atomic on the shared counter per block instead of one
+// per warp, which serialises when most warps append (the sink's children,
+// the unreached vertices, the dirty parents).
+__device__ __forceinline__ void block_append(bool flag, int32_t value, int32_t *__restrict__ list,
+                                             int32_t *__restrict__ count)
+{
+    __shared__ int32_t warp_base[kBlock / 32];
+    __shared__ int32_t block_base;
+    const unsigned mask = __ballot_sync(0xffffffffu, flag);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) warp_base[w] = __popc(mask);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int32_t sum = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+            int32_t t = warp_base[i];
+            warp_base[i] = sum;
+            sum += t;
+        }
+        block_base = sum ? atomicAdd(count, sum) : 0;
+    }
+    __syncthreads();
+    if (flag) list[block_base + warp_base[w] + __popc(mask & ((1u << lane) - 1))] = value;
+}
+
+// Warp-aggregated slot reservation: every lane of a converged warp calls it;
+// a lane with flag set gets base + its rank among the flagged lanes, where
+// base = atomicAdd(count, flagged lanes) (one atomic per warp); -1 otherwise.
+__device__ __forceinline__ int32_t warp_reserve(bool flag, int32_t *count, int32_t base_offset = 0)
+{
+    const unsigned m = __ballot_sync(0xffffffffu, flag);
+    if (!m) return -1;
+    const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+    int32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return flag ? base_offset + base + __popc(m & ((1u << lane) - 1)) : -1;
 }
 
 // Tour node ids (an Euler tour of the strategy forest, two nodes per vertex):
@@ -90,7 +164,6 @@ constexpr uint32_t DERR_WALK_CAP = 1u << 1;      // a valuation walk exceeded it
 constexpr uint32_t DERR_PASS_CAP = 1u << 2;      // a comparison exceeded its pass cap
 constexpr uint32_t DERR_BAD_INPUT = 1u << 3;     // malformed strategy (target out of range)
 
-constexpr int kBlock = 256;
 
 __host__ __device__ __forceinline__ int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 

@@ -61,32 +61,6 @@ __device__ __forceinline__ int ceil_log2_dev(int64_t x)
     return r;
 }
 
-// Block-aggregated append: every thread of the block calls it (no early
-// return before); one atomic on the shared counter per block instead of one
-// per warp, which serialises when most warps append (the sink's children,
-// the unreached vertices, the dirty parents).
-__device__ __forceinline__ void block_append(bool flag, int32_t value, int32_t *__restrict__ list,
-                                             int32_t *__restrict__ count)
-{
-    __shared__ int32_t warp_base[kBlock / 32];
-    __shared__ int32_t block_base;
-    const unsigned mask = __ballot_sync(0xffffffffu, flag);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 0) warp_base[w] = __popc(mask);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int32_t sum = 0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
-            int32_t t = warp_base[i];
-            warp_base[i] = sum;
-            sum += t;
-        }
-        block_base = sum ? atomicAdd(count, sum) : 0;
-    }
-    __syncthreads();
-    if (flag) list[block_base + warp_base[w] + __popc(mask & ((1u << lane) - 1))] = value;
-}
-
 __global__ void k_init_strat(int32_t n, const int8_t *__restrict__ owner, const int32_t *__restrict__ off,
                              const int32_t *__restrict__ tgt, int32_t *__restrict__ strat,
                              int32_t *__restrict__ st)
@@ -170,13 +144,14 @@ __global__ void k_tour_link(int32_t n, const int32_t *__restrict__ strat, const 
 // are still exact.  The dirty parents are compacted first (k_dirty_list, which
 // also clears the flags), so the relinking threads are all busy.
 __global__ void k_dirty_list(int32_t n, uint8_t *__restrict__ dirty, int32_t *__restrict__ list,
-                             int32_t *__restrict__ count, const int32_t *__restrict__ gate)
+                             int32_t *__restrict__ count, int2 *__restrict__ vloc, const int32_t *__restrict__ gate)
 {
     if (gate && !*gate) return;
     for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < n; b0 += (int64_t)gridDim.x * blockDim.x) {
         const int32_t p = (int32_t)(b0 + threadIdx.x);
         const bool take = p < n && dirty[p];
         if (take) dirty[p] = 0;
+        if (p < n) vloc[p] = make_int2(-1, -1);   // on no walked sublist until the walk reaches it
         block_append(take, p, list, count);
     }
 }
@@ -258,8 +233,9 @@ __device__ __forceinline__ int32_t head_index(int32_t x, int64_t L, int32_t nsub
 template <bool POW2>
 __global__ void k_walk_sublists(int32_t nsub, int32_t n, int64_t L, int32_t stride,
                                 const int32_t *__restrict__ succ, int2 *__restrict__ vloc,
-                                int2 *__restrict__ red, uint32_t *__restrict__ err)
+                                int2 *__restrict__ red, uint32_t *__restrict__ err, const int32_t *__restrict__ gate)
 {
+    if (gate && !*gate) return;
     int32_t j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nsub) return;
     const int64_t h = (j == nsub - 1) ? L - 1 : (int64_t)j * stride;
@@ -298,8 +274,10 @@ __global__ void k_walk_sublists(int32_t nsub, int32_t n, int64_t L, int32_t stri
 // Round 0 reads red and writes a, then the rounds alternate a -> b -> a ...
 // Reads bypass L1 (each buffer is rewritten by other blocks between reads).
 __global__ void __launch_bounds__(kBlock) k_rank_reduced(int32_t nsub, const int2 *__restrict__ red,
-                                                         int2 *__restrict__ a, int2 *__restrict__ b)
+                                                         int2 *__restrict__ a, int2 *__restrict__ b,
+                                                         const int32_t *__restrict__ gate)
 {
+    if (gate && !*gate) return;   // every block returns: no grid barrier is left waiting
     cg::grid_group g = cg::this_grid();
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nth = (int64_t)gridDim.x * blockDim.x;
@@ -327,32 +305,25 @@ __global__ void k_broadcast_depth(int32_t n, const int2 *__restrict__ vloc, cons
                                   const int32_t *__restrict__ strat, const int32_t *__restrict__ pri,
                                   const uint8_t *__restrict__ solved, int32_t *__restrict__ st,
                                   PathNode *__restrict__ node, int32_t *__restrict__ ulist,
-                                  int32_t *__restrict__ ucount)
+                                  int32_t *__restrict__ ucount, const int32_t *__restrict__ gate)
 {
-    int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    bool unreached = false;
-    if (v < n && !solved[v]) {
-        int2 loc = vloc[v];
-        int2 r = (loc.x >= 0) ? fin[loc.x] : make_int2(0, 0);
-        if (loc.x >= 0 && r.x == TOUR_END) {
-            st[v] = loc.y - r.y;
-            node[v] = PathNode{strat[v], pri[v], RM_UNKNOWN, 0};
-        } else {
-            st[v] = ST_UNRESOLVED;
-            unreached = true;
+    if (gate && !*gate) return;
+    // grid-stride with block-uniform passes (block_append needs every thread)
+    for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < n; b0 += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t v = (int32_t)(b0 + threadIdx.x);
+        bool unreached = false;
+        if (v < n && !solved[v]) {
+            int2 loc = vloc[v];
+            int2 r = (loc.x >= 0) ? fin[loc.x] : make_int2(0, 0);
+            if (loc.x >= 0 && r.x == TOUR_END) {
+                st[v] = loc.y - r.y;
+                node[v] = PathNode{strat[v], pri[v], RM_UNKNOWN, 0};
+            } else {
+                st[v] = ST_UNRESOLVED;
+                unreached = true;
+            }
         }
-    }
-    block_append(unreached, v, ulist, ucount);
-}
-
-// (max, count of max) of the union of two priority multisets
-__device__ __forceinline__ void top1_merge(int32_t &m, int32_t &c, int32_t m2, int32_t c2)
-{
-    if (m2 > m) {
-        m = m2;
-        c = c2;
-    } else if (m2 == m) {
-        c += c2;
+        block_append(unreached, v, ulist, ucount);
     }
 }
 
@@ -361,31 +332,44 @@ __device__ __forceinline__ void top1_merge(int32_t &m, int32_t &c, int32_t m2, i
 // known (or the sink) and stores the summary of its own vertex only; with
 // threads in arbitrary order a walk is short on average (an ancestor has
 // usually been done already).  A concurrent reader sees either RM_UNKNOWN or
-// the final pair, which is written as one 8-byte store.
+// the final pair, which is written as one 8-byte store.  The key is written
+// only where it changed; all threads stay to the end (flag_in_neighbours is
+// warp-collective).
 __global__ void k_rootinfo(int32_t n, const int32_t *__restrict__ st, PathNode *__restrict__ node,
-                           int32_t *__restrict__ key, uint32_t *__restrict__ err, ChangeTrack track)
+                           int32_t *__restrict__ key, uint32_t *__restrict__ err, ChangeTrack track,
+                           const int32_t *__restrict__ gate)
 {
-    int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= n || st[v] < 1) return;
-    PathNode q = node[v];
-    int32_t m = q.pri, c = 1, y = q.parent;
-    int32_t steps = 0;
-    while (y >= 0) {
-        int4 r = *reinterpret_cast<const int4 *>(&node[y]);
-        if (r.z != RM_UNKNOWN) {
-            top1_merge(m, c, r.z, r.w);
-            break;
+    if (gate && !*gate) return;
+    for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < n; b0 += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t v = (int32_t)(b0 + threadIdx.x);
+        bool changed = false;
+        if (v < n && st[v] >= 1) {
+            const int32_t old = key ? key[v] : 0;
+            PathNode q = node[v];
+            int32_t m = q.pri, c = 1, y = q.parent;
+            int32_t steps = 0;
+            while (y >= 0) {
+                int4 r = *reinterpret_cast<const int4 *>(&node[y]);
+                if (r.z != RM_UNKNOWN) {
+                    top1_merge(m, c, r.z, r.w);
+                    break;
+                }
+                top1_merge(m, c, r.y, 1);
+                y = r.x;
+                if (++steps > n) {
+                    atomicOr(err, DERR_WALK_CAP);
+                    break;
+                }
+            }
+            *reinterpret_cast<int2 *>(&node[v].rmax) = make_int2(m, c);
+            const int32_t k = finite_key(m, c);
+            if (key && k != old) {
+                key[v] = k;
+                changed = true;
+            }
         }
-        top1_merge(m, c, r.y, 1);
-        y = r.x;
-        if (++steps > n) {
-            atomicOr(err, DERR_WALK_CAP);
-            break;
-        }
+        flag_in_neighbours(track, changed, v);
     }
-    *reinterpret_cast<int2 *>(&node[v].rmax) = make_int2(m, c);
-    if (key) key[v] = finite_key(m, c);
-    note_signature(track, v, make_int2(m, c));
 }
 
 // ---- cycle parity of the unreached vertices
@@ -468,17 +452,28 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
         in = out;
         out = t;
     }
-    for (int64_t i = tid; i < nu; i += nth) {
-        int32_t u = ulist[i];
-        int32_t t = __ldcg(&in[u]).x;
-        int32_t su = solved[t] ? st[t] : ((__ldcg(&in[t]).y % 2 == 0) ? ST_POS_INF : ST_NEG_INF);
-        st[u] = su;
-        if (key) key[u] = (su == ST_POS_INF) ? KEY_POS_INF : KEY_NEG_INF;
-        note_signature(track, u, make_int2(su == ST_POS_INF ? SIG_POS_INF : SIG_NEG_INF, 0));
+    // block-uniform iterations: flag_in_neighbours is warp-collective
+    for (int64_t b0 = tid - threadIdx.x; b0 < nu; b0 += nth) {
+        const int64_t i = b0 + threadIdx.x;
+        bool changed = false;
+        int32_t u = -1;
+        if (i < nu) {
+            u = ulist[i];
+            int32_t t = __ldcg(&in[u]).x;
+            int32_t su = solved[t] ? st[t] : ((__ldcg(&in[t]).y % 2 == 0) ? ST_POS_INF : ST_NEG_INF);
+            st[u] = su;
+            const int32_t k = (su == ST_POS_INF) ? KEY_POS_INF : KEY_NEG_INF;
+            if (key && key[u] != k) {
+                key[u] = k;
+                changed = true;
+            }
+        }
+        flag_in_neighbours(track, changed, u);
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_cycles(const int32_t *__restrict__ ucount,
+// at most 40 registers: six co-resident blocks per SM for the cooperative launch
+__global__ void __launch_bounds__(kBlock, 6) k_cycles(const int32_t *__restrict__ ucount,
                                                    const int32_t *__restrict__ ulist,
                                                    const int32_t *__restrict__ strat,
                                                    const int32_t *__restrict__ pri,
@@ -487,8 +482,9 @@ __global__ void __launch_bounds__(kBlock) k_cycles(const int32_t *__restrict__ u
                                                    int2 *__restrict__ jb,
                                                    int32_t *__restrict__ la, int32_t *__restrict__ lb,
                                                    int32_t *__restrict__ cnt, uint32_t *__restrict__ err,
-                                                   ChangeTrack track)
+                                                   ChangeTrack track, const int32_t *__restrict__ gate)
 {
+    if (gate && !*gate) return;   // every block returns: no grid barrier is left waiting
     int32_t nu = *ucount;
     if (nu == 0) return;
     if (nu <= kSmallCycles) {
@@ -596,11 +592,10 @@ int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const ui
                        int32_t *sinklist, int32_t *sinkcount, int32_t *dlist, int32_t *dcount,
                        const int32_t *gate)
 {
-    cudaError_t e = cudaMemsetAsync(vloc, 0xff, 8 * (size_t)n, s);   // (-1, -1): on no walked sublist
-    if (e == cudaSuccess) e = cudaMemsetAsync(dcount, 0, sizeof(int32_t), s);
+    cudaError_t e = cudaMemsetAsync(dcount, 0, sizeof(int32_t), s);
     if (e != cudaSuccess) return (int)e;
     count_launch();
-    k_dirty_list<<<capped_grid(n), kBlock, 0, s>>>(n, dirty, dlist, dcount, gate);
+    k_dirty_list<<<capped_grid(n), kBlock, 0, s>>>(n, dirty, dlist, dcount, vloc, gate);
     count_launch();
     unsigned g = grid_for(n);
     g = g < 1216u ? g : 1216u;
@@ -613,16 +608,17 @@ int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const ui
 }
 
 void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, int32_t stride, const int32_t *succ,
-                          int2 *vloc, int2 *red, uint32_t *err)
+                          int2 *vloc, int2 *red, uint32_t *err, const int32_t *gate)
 {
     count_launch();
     if ((stride & (stride - 1)) == 0)
-        k_walk_sublists<true><<<grid_for(nsub, 128), 128, 0, s>>>(nsub, n, L, stride, succ, vloc, red, err);
+        k_walk_sublists<true><<<grid_for(nsub, 128), 128, 0, s>>>(nsub, n, L, stride, succ, vloc, red, err, gate);
     else
-        k_walk_sublists<false><<<grid_for(nsub, 128), 128, 0, s>>>(nsub, n, L, stride, succ, vloc, red, err);
+        k_walk_sublists<false><<<grid_for(nsub, 128), 128, 0, s>>>(nsub, n, L, stride, succ, vloc, red, err, gate);
 }
 
-int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, int2 *b, const int2 **fin)
+int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, int2 *b, const int2 **fin,
+                        const int32_t *gate)
 {
     static int blocks = 0, blocks_dev = -1;
     int dev = 0;
@@ -637,7 +633,7 @@ int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, 
     while (((int64_t)1 << rounds) < nsub) rounds++;
     rounds += 1;
     *fin = (rounds % 2 == 1) ? a : b;
-    void *args[] = {(void *)&nsub, (void *)&red, (void *)&a, (void *)&b};
+    void *args[] = {(void *)&nsub, (void *)&red, (void *)&a, (void *)&b, (void *)&gate};
     count_launch();
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_rank_reduced, dim3(grid), dim3(kBlock), args, 0, s);
     return e == cudaSuccess ? 0 : (int)e;
@@ -645,22 +641,23 @@ int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, 
 
 void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const int2 *fin,
                             const int32_t *strat, const int32_t *pri, const uint8_t *solved,
-                            int32_t *st, PathNode *node, int32_t *ulist, int32_t *ucount)
+                            int32_t *st, PathNode *node, int32_t *ulist, int32_t *ucount, const int32_t *gate)
 {
     count_launch();
-    k_broadcast_depth<<<grid_for(n), kBlock, 0, s>>>(n, vloc, fin, strat, pri, solved, st, node, ulist, ucount);
+    k_broadcast_depth<<<capped_grid(n), kBlock, 0, s>>>(n, vloc, fin, strat, pri, solved, st, node, ulist, ucount,
+                                                        gate);
 }
 
 void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, int32_t *key, uint32_t *err,
-                     ChangeTrack track)
+                     ChangeTrack track, const int32_t *gate)
 {
     count_launch();
-    k_rootinfo<<<grid_for(n), kBlock, 0, s>>>(n, st, node, key, err, track);
+    k_rootinfo<<<capped_grid(n), kBlock, 0, s>>>(n, st, node, key, err, track, gate);
 }
 
 int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, const int32_t *strat,
                   const int32_t *pri, const uint8_t *solved, int32_t *st, int32_t *key, int2 *ja, int2 *jb,
-                  int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err, ChangeTrack track)
+                  int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err, ChangeTrack track, const int32_t *gate)
 {
     static int blocks = 0, blocks_dev = -1;
     int dev = 0;
@@ -671,7 +668,7 @@ int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, c
     }
     void *args[] = {(void *)&ucount, (void *)&ulist, (void *)&strat, (void *)&pri, (void *)&solved,
                     (void *)&st, (void *)&key, (void *)&ja, (void *)&jb, (void *)&la, (void *)&lb, (void *)&cnt,
-                    (void *)&err, (void *)&track};
+                    (void *)&err, (void *)&track, (void *)&gate};
     count_launch();
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_cycles, dim3(blocks), dim3(kBlock), args, 0, s);
     return e == cudaSuccess ? 0 : (int)e;

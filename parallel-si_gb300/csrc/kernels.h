@@ -10,15 +10,43 @@ namespace psi {
 
 struct PathNode;   // device_common.cuh
 
-// Change tracking between evaluations and switch steps: sig holds each
-// vertex's value signature from the last evaluation ((rmax, rcnt) if finite,
-// an infinity code if not); when an evaluation changes a vertex's signature,
-// its in-neighbours (rev_off/rev_src) get need = 1, and a switch step examines
-// only its player's vertices with need set.  sig == nullptr: no tracking.
+// Change tracking between evaluations and switch steps: when an evaluation
+// changes a vertex's comparison key, its in-neighbours (rev_off/rev_src) get
+// need = 1, and a switch step examines only its player's vertices with need
+// set.  The key suffices: a switch decision depends on the order of its
+// successors' keys, except where equal keys tie at the best one, and such a
+// vertex keeps need = 1 (switch_kernels.cu).  need == nullptr: no tracking.
+// quiet (a device word, optional): while nonzero every need flag is already
+// set, and changed keys flag nothing (the first evaluation after a reset).
 struct ChangeTrack {
-    int2 *sig = nullptr;
     uint8_t *need = nullptr;
     const int32_t *rev_off = nullptr, *rev_src = nullptr;
+    const int32_t *quiet = nullptr;
+};
+
+// Device words deciding which kernels of an evaluation do work (their gates;
+// set by the host or by control kernels, patch_kernels.cu).
+struct EvalGates {
+    int32_t full = 0;        // the tour is built from scratch
+    int32_t incr = 0;        // the previous tour is brought up to date
+    int32_t eval = 1;        // the full evaluation's kernels after the tour run
+    int32_t patch = 0;       // this evaluation is a patch (patch_kernels.cu)
+    int32_t try_patch = 0;   // the next evaluation may be a patch: every strategy change since the
+                             // last evaluation went through a switch step that listed it
+    int32_t ccount = 0;      // changed vertices the switch steps listed since the last evaluation
+    int32_t csnap = 0;       // ccount as the current evaluation found it
+    int32_t acount = 0;      // vertices the current patch re-evaluates
+    int32_t lcnt[3] = {0, 0, 0};              // per-level append counters of the patch's search
+    int32_t saved_full = 0, saved_incr = 0;   // tour gates while a patch holds them closed
+    int32_t skip = 0, backoff = 1;            // evaluations not to try a patch after a failed one
+};
+
+// A list of the vertices whose strategy a switch step changes (appended while
+// *count < cap; *count keeps counting past it, so *count <= cap means complete).
+struct ChangeList {
+    int32_t *list = nullptr;
+    int32_t *count = nullptr;
+    int32_t cap = 0;
 };
 
 // Launchers taking `gate` (a device word, nullptr = always) enqueue kernels
@@ -81,26 +109,29 @@ int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const ui
                        const int32_t *gate = nullptr);
 // Sublist walks; heads are the nodes j*stride (j < nsub-1) and the list start.
 void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, int32_t stride, const int32_t *succ,
-                          int2 *vloc, int2 *red, uint32_t *err);
+                          int2 *vloc, int2 *red, uint32_t *err, const int32_t *gate = nullptr);
 // Ranks the reduced list red[0..nsub) (next, weight) by Wyllie pointer jumping
 // (cooperative launch; a, b: nsub entries each).  *fin is set to the buffer
 // that will hold, per item, (TOUR_END if the list start reaches it, else >= 0;
 // inclusive suffix sum).  Returns a cudaError_t value.
-int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, int2 *b, const int2 **fin);
+int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, int2 *b, const int2 **fin,
+                        const int32_t *gate = nullptr);
 void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const int2 *fin,
                             const int32_t *strat, const int32_t *pri, const uint8_t *solved,
-                            int32_t *st, PathNode *node, int32_t *ulist, int32_t *ucount);
+                            int32_t *st, PathNode *node, int32_t *ulist, int32_t *ucount,
+                            const int32_t *gate = nullptr);
 // Root-path summaries (rmax, rcnt) of every reached vertex, also stored as its
 // comparison key when key != nullptr.
 void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, int32_t *key, uint32_t *err,
-                     ChangeTrack track = ChangeTrack());
+                     ChangeTrack track = ChangeTrack(), const int32_t *gate = nullptr);
 // Cycle parity of the *ucount vertices in ulist (cooperative launch), also
 // stored as their comparison keys when key != nullptr.  ja, jb: n entries;
 // la, lb: n entries (active lists); cnt: 3 counters.  Returns a cudaError_t
 // value.
 int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, const int32_t *strat,
                   const int32_t *pri, const uint8_t *solved, int32_t *st, int32_t *key, int2 *ja, int2 *jb,
-                  int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err, ChangeTrack track = ChangeTrack());
+                  int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err, ChangeTrack track = ChangeTrack(),
+                  const int32_t *gate = nullptr);
 // mark_solved over the last evaluation's unreached vertices (cpu_parity.cpp:265-274);
 // with game_of/gmask only for games whose mask is set (nullptr: all).
 // Newly solved vertices are flagged in dirty (their children leave the tour).
@@ -117,13 +148,14 @@ void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ul
 // (and list: n entries, list_count: one counter) only the vertices of plist
 // whose need flag is set are examined (ChangeTrack); examined vertices get
 // need = 0, or 1 when a tie at their best successor leaves their choice to a
-// walk that a later evaluation may decide differently.
+// walk that a later evaluation may decide differently.  With changes.list,
+// every changed vertex is appended to it (ChangeList).
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player,
                    const int32_t *off, const int32_t *tgt, int32_t *strat, const int32_t *st,
                    const int32_t *key, const PathNode *node, unsigned long long *stats, const int32_t *game_of,
                    unsigned long long *gcount, const int32_t *gmask, uint8_t *dirty, uint32_t *err,
                    const int32_t *gate = nullptr, uint8_t *need = nullptr, int32_t *list = nullptr,
-                   int32_t *list_count = nullptr);
+                   int32_t *list_count = nullptr, ChangeList changes = ChangeList());
 // ---- batches: per-game accounting of solve_si (state[g] = brs, iters,
 // odd_done, done; gcount[g] = strict improvements of the last switch step)
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state,
@@ -138,7 +170,7 @@ void launch_arena_place(cudaStream_t s, int32_t nu, int32_t k_games, const int32
                         const int32_t *u_off, const int32_t *u_tgt, const int32_t *u_roff, const int32_t *u_rsrc,
                         int8_t *owner, int32_t *pri, int32_t *off, int32_t *tgt, int32_t *rev_off, int32_t *rev_src,
                         int32_t *strat, int32_t *st, uint8_t *solved, int32_t *game_of, int4 *gstate,
-                        unsigned long long *gcount, int32_t *succ, uint8_t *dirty, int2 *sig, uint8_t *need);
+                        unsigned long long *gcount, int32_t *succ, uint8_t *dirty, uint8_t *need);
 // Games copied as they are into a union (game k at vertices ub[k], edges
 // ue[k]): offsets and targets shifted to union numbering, u_off[nu] = ue[K],
 // and game_of[v] = v's game when game_of != nullptr.
@@ -166,6 +198,35 @@ void launch_serve_reset_odd(cudaStream_t s, int32_t np, const int32_t *plist, co
 // ---- dense valuation rows for export (the reference's ArrayVal layout)
 void launch_materialize(cudaStream_t s, int32_t v0, int32_t count, int32_t d, const int32_t *st,
                         const PathNode *node, int32_t *rows, uint32_t *err);
+
+// ---- incremental evaluation (patch_kernels.cu)
+// Re-evaluates only the vertices whose strategy path passes through a vertex
+// changed since the last evaluation; the result equals a full evaluation's.
+struct PatchArgs {
+    EvalGates *g = nullptr;
+    int32_t *ucount = nullptr, *sinkcount = nullptr;   // reset when the full evaluation runs
+    const int32_t *clist = nullptr;                    // the changed vertices (ChangeList)
+    const int32_t *strat = nullptr, *pri = nullptr, *rev_off = nullptr, *rev_src = nullptr;
+    const uint8_t *solved = nullptr;
+    int32_t *alist = nullptr;   // the vertices re-evaluated (acap entries)
+    int32_t *apos = nullptr;    // per vertex: its position in alist, -1 if none (n entries, -1 between patches)
+    int4 *ja = nullptr, *jb = nullptr;   // pointer-jumping entries (acap each)
+    int32_t acap = 0, ccap = 0, max_levels = 0;
+    int64_t ucap = 0;           // capacity of ulist
+    int32_t *st = nullptr;
+    PathNode *node = nullptr;
+    int32_t *key = nullptr;
+    int32_t *ulist = nullptr;   // unreached list, appended to (mark_solved scans it)
+    unsigned long long *stats = nullptr;   // [0] += 1 per patch, [1] += vertices re-evaluated
+    ChangeTrack track;
+};
+// Sets the gates the host decides before an evaluation (one thread).
+void launch_eval_gates(cudaStream_t s, EvalGates *g, int32_t full, int32_t incr, int32_t try_patch);
+// One thread: decides between a patch and the full evaluation (gates).
+void launch_patch_begin(cudaStream_t s, const PatchArgs &a);
+// Cooperative launches, gated on g->patch; return a cudaError_t value.
+int launch_patch_collect(cudaStream_t s, const PatchArgs &a);
+int launch_patch_values(cudaStream_t s, const PatchArgs &a);
 
 }  // namespace psi
 

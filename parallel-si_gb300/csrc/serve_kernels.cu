@@ -38,7 +38,7 @@ __global__ void k_arena_place(int32_t nu, int32_t k_games, const int32_t *__rest
                               int32_t *__restrict__ strat, int32_t *__restrict__ st, uint8_t *__restrict__ solved,
                               int32_t *__restrict__ game_of, int4 *__restrict__ gstate,
                               unsigned long long *__restrict__ gcount, int32_t *__restrict__ succ,
-                              uint8_t *__restrict__ dirty, int2 *__restrict__ sig, uint8_t *__restrict__ need)
+                              uint8_t *__restrict__ dirty, uint8_t *__restrict__ need)
 {
     int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nu) return;
@@ -68,7 +68,6 @@ __global__ void k_arena_place(int32_t nu, int32_t k_games, const int32_t *__rest
     succ[2 * (int64_t)a] = 2 * a + 1;
     succ[2 * (int64_t)a + 1] = 2 * a;
     dirty[a] = 1;
-    sig[a] = make_int2(INT32_MIN, INT32_MIN);   // no signature yet: the first evaluation flags its in-neighbours
     need[a] = 1;
     if (i == u0) {
         gstate[slot[k]] = make_int4(0, 0, 1, 0);
@@ -253,13 +252,13 @@ void launch_arena_place(cudaStream_t s, int32_t nu, int32_t k_games, const int32
                         const int32_t *u_off, const int32_t *u_tgt, const int32_t *u_roff, const int32_t *u_rsrc,
                         int8_t *owner, int32_t *pri, int32_t *off, int32_t *tgt, int32_t *rev_off, int32_t *rev_src,
                         int32_t *strat, int32_t *st, uint8_t *solved, int32_t *game_of, int4 *gstate,
-                        unsigned long long *gcount, int32_t *succ, uint8_t *dirty, int2 *sig, uint8_t *need)
+                        unsigned long long *gcount, int32_t *succ, uint8_t *dirty, uint8_t *need)
 {
     if (nu <= 0) return;
     count_launch();
     k_arena_place<<<grid_for(nu), kBlock, 0, s>>>(nu, k_games, ub, vb, eb, slot, u_owner, u_pri, u_off, u_tgt, u_roff,
                                                   u_rsrc, owner, pri, off, tgt, rev_off, rev_src, strat, st, solved,
-                                                  game_of, gstate, gcount, succ, dirty, sig, need);
+                                                  game_of, gstate, gcount, succ, dirty, need);
 }
 
 void launch_union_fixup(cudaStream_t s, int32_t nu, int64_t mu, int32_t k_games, const int32_t *ub, const int32_t *ue,

@@ -34,6 +34,8 @@ int check_options(const psi_options &opt)
 {
     if (opt.valuation_mode != PSI_VAL_PATH) return fail(PSI_ERR_INVALID, "unknown valuation_mode");
     if (opt.sublist_len < 2) return fail(PSI_ERR_INVALID, "sublist_len must be >= 2");
+    if (opt.incremental < PSI_INCR_OFF || opt.incremental > PSI_INCR_ALWAYS)
+        return fail(PSI_ERR_INVALID, "unknown incremental mode");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0) return fail(PSI_ERR_NO_DEVICE, "no CUDA device available");
@@ -55,6 +57,7 @@ int Solver::create(const CsrView &g, const psi_options &opt, Solver **out, bool 
     s->timing_ = opt.timing != 0;
     s->stride_ = opt.sublist_len;
     s->use_graph_ = opt.graph != 0;
+    s->incremental_ = opt.incremental;
     rc = s->alloc_arrays(g.n, g.m);
     if (!rc) rc = s->upload_game(g, validate);
     if (rc) {
@@ -78,6 +81,7 @@ int Solver::create_arena(int64_t max_vertices, int64_t max_edges, int32_t slots,
     s->device_ = opt.device;
     s->timing_ = opt.timing != 0;
     s->stride_ = opt.sublist_len;
+    s->incremental_ = PSI_INCR_OFF;   // admissions and retirements change vertices outside any switch step
     rc = s->alloc_arrays(max_vertices, max_edges);
     if (!rc) rc = s->init_arena(slots);
     if (rc) {
@@ -123,6 +127,7 @@ int Solver::create_union(const std::vector<const HostGame *> &gs, const psi_opti
     s->timing_ = opt.timing != 0;
     s->stride_ = opt.sublist_len;
     s->use_graph_ = opt.graph != 0;
+    s->incremental_ = opt.incremental;
     rc = s->alloc_arrays(n, m);
     if (!rc) rc = s->upload_union(gs, table, base->back());
     if (rc) {
@@ -190,6 +195,17 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
     cap_m_ = cap_m;
     const int64_t capL = 2 * cap_n + 2;
     const int64_t cap_sub = ceil_div(capL - 1, stride_) + 1;
+    // incremental evaluation: change-list capacity (larger lists mean a full
+    // evaluation), re-evaluated set capacity, level cap of its search
+    if (incremental_ != PSI_INCR_OFF) {
+        const bool always = incremental_ == PSI_INCR_ALWAYS;
+        const int64_t cc = always ? cap_n : std::max<int64_t>(1024, cap_n >> 10);
+        const int64_t ac = always ? cap_n : std::max<int64_t>(4096, cap_n >> 3);
+        ccap_ = (int32_t)std::max<int64_t>(1, std::min(cc, cap_n));
+        acap_ = (int32_t)std::max<int64_t>(1, std::min(ac, cap_n));
+        max_levels_ = always ? INT32_MAX : 160;
+    }
+    ucap_ = cap_n + acap_;
     PSI_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     for (auto &p : ph_) {
         PSI_CUDA_TRY(cudaEventCreate(&p.a));
@@ -215,9 +231,8 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
         {(void **)&key_, 4 * (size_t)cap_n},
         {(void **)&succ_, 4 * (size_t)capL},
         {(void **)&dirty_, (size_t)cap_n},
-        {(void **)&sig_, 8 * (size_t)cap_n},
         {(void **)&need_, (size_t)cap_n},
-        {(void **)&ulist_, 4 * (size_t)cap_n},
+        {(void **)&ulist_, 4 * (size_t)ucap_},
         {(void **)&vloc_, 8 * (size_t)cap_n},
         {(void **)&redA_, 8 * (size_t)cap_sub},
         {(void **)&redB_, 8 * (size_t)cap_sub},
@@ -232,8 +247,29 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
         if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
         allocs_.push_back(*a.ptr);
     }
+    if (incremental_ != PSI_INCR_OFF) {
+        const struct {
+            void **ptr;
+            size_t bytes;
+        } patch[] = {
+            {(void **)&clist_, 4 * (size_t)ccap_},
+            {(void **)&alist_, 4 * (size_t)acap_},
+            {(void **)&apos_, 4 * (size_t)std::max<int64_t>(1, cap_n)},
+            {(void **)&pj_, 2 * sizeof(int4) * (size_t)acap_},
+        };
+        for (const auto &a : patch) {
+            cudaError_t e = device_alloc(a.ptr, a.bytes, stream_);
+            if (e != cudaSuccess)
+                return fail(PSI_ERR_NOMEM, std::string("device allocation: ") + cudaGetErrorString(e));
+            allocs_.push_back(*a.ptr);
+        }
+        PSI_CUDA_TRY(cudaMemsetAsync(apos_, 0xff, 4 * (size_t)std::max<int64_t>(1, cap_n), stream_));   // -1: in no patch
+    }
     PSI_CUDA_TRY(cudaMallocHost((void **)&hw_, sizeof(Words)));
     PSI_CUDA_TRY(cudaMemsetAsync(dw_, 0, sizeof(Words), stream_));
+    const GraphCtl fresh;
+    // pageable source: staged before the call returns
+    PSI_CUDA_TRY(cudaMemcpyAsync(ctl_, &fresh, sizeof fresh, cudaMemcpyHostToDevice, stream_));
     PSI_CUDA_TRY(cudaMemsetAsync(dirty_, 0, (size_t)cap_n, stream_));
     return PSI_OK;
 }
@@ -363,6 +399,8 @@ int Solver::sync_and_check(const char *what)
     if (e != cudaSuccess) return fail(PSI_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
     int rc = collect_phases();
     if (rc) return rc;
+    times_.patches = (int64_t)hw_->patch[0];
+    times_.patched = (int64_t)hw_->patch[1];
     if (hw_->err) {
         uint32_t bits = hw_->err;
         cudaMemsetAsync(dw_, 0, sizeof(Words), stream_);
@@ -372,10 +410,18 @@ int Solver::sync_and_check(const char *what)
     return PSI_OK;
 }
 
+void Solver::reset_times()
+{
+    times_ = SolverTimes();
+    cudaMemsetAsync(dw_->patch, 0, sizeof(dw_->patch), stream_);
+    if (hw_) hw_->patch[0] = hw_->patch[1] = 0;
+}
+
 void Solver::reset_tracking()
 {
+    static const int32_t one = 1;
     cudaMemsetAsync(need_, 1, (size_t)n_, stream_);
-    cudaMemsetAsync(sig_, 0x80, 8 * (size_t)n_, stream_);   // matches no signature
+    cudaMemcpyAsync(&ctl_->quiet, &one, sizeof one, cudaMemcpyHostToDevice, stream_);
 }
 
 int Solver::init_strat()
@@ -399,9 +445,95 @@ int Solver::reset_opponent_strategy()
     int rc = set_device();
     if (rc) return rc;
     launch_reset_odd(stream_, n_, owner_, off_, tgt_, strat_);
-    PSI_CUDA_TRY(cudaMemsetAsync(need_, 1, (size_t)n_, stream_));   // Odd's choices start over
+    reset_tracking();   // Odd's choices start over
     tour_valid_ = false;
     return sync_and_check("reset_opponent_strategy");
+}
+
+PatchArgs Solver::patch_args()
+{
+    PatchArgs a;
+    a.g = ctl_;
+    a.ucount = &dw_->ucount;
+    a.sinkcount = &dw_->sinkcount;
+    a.clist = clist_;
+    a.strat = strat_;
+    a.pri = pri_;
+    a.rev_off = rev_off_;
+    a.rev_src = rev_src_;
+    a.solved = solved_;
+    a.alist = alist_;
+    a.apos = apos_;
+    a.ja = pj_;
+    a.jb = pj_ ? pj_ + acap_ : nullptr;
+    a.acap = acap_;
+    a.ccap = ccap_;
+    a.max_levels = max_levels_;
+    a.ucap = ucap_;
+    a.st = st_;
+    a.node = node_;
+    a.key = key_;
+    a.ulist = ulist_;
+    a.stats = dw_->patch;
+    a.track = track();
+    return a;
+}
+
+int Solver::enqueue_eval(bool timed)
+{
+    auto begin = [&](Phase p) {
+        if (timed) phase_begin(p);
+    };
+    auto end = [&](Phase p) {
+        if (timed) phase_end(p);
+    };
+    // 0. a patch, when the gates allow it and it succeeds; otherwise its
+    //    kernels return at once and the full evaluation's gates are open
+    begin(PH_PATCH);
+    const PatchArgs pa = patch_args();
+    launch_patch_begin(stream_, pa);
+    if (incremental_ != PSI_INCR_OFF) {
+        int pe = launch_patch_collect(stream_, pa);
+        if (!pe) pe = launch_patch_values(stream_, pa);
+        if (pe) return fail(PSI_ERR_CUDA, std::string("patch kernels: ") + cudaGetErrorString((cudaError_t)pe));
+    }
+    end(PH_PATCH);
+    // 1. Euler tour of the sink tree: built afresh (gate full) or the previous
+    //    one relinked where strategies or solved flags changed (gate incr);
+    //    jA_ is free until the cycle pass: it holds the list of dirty parents
+    begin(PH_TOUR);
+    launch_tour_build(stream_, n_, strat_, solved_, rev_off_, rev_src_, succ_, vloc_, ulist_, &dw_->sinkcount, dirty_,
+                      &ctl_->full);
+    int ce = launch_tour_update(stream_, n_, strat_, solved_, rev_off_, rev_src_, dirty_, succ_, vloc_, ulist_,
+                                &dw_->sinkcount, reinterpret_cast<int32_t *>(jA_), &dw_->cnt[0], &ctl_->incr);
+    if (ce) return fail(PSI_ERR_CUDA, std::string("tour update: ") + cudaGetErrorString((cudaError_t)ce));
+    end(PH_TOUR);
+    // 2. Helman-JaJa sublists, then the reduced list ranked on the device
+    begin(PH_SUBLIST);
+    launch_walk_sublists(stream_, nsub_, n_, L_, stride_, succ_, vloc_, redA_, &dw_->err, &ctl_->eval);
+    end(PH_SUBLIST);
+    begin(PH_REDUCED);
+    const int2 *fin = nullptr;
+    ce = launch_rank_reduced(stream_, nsub_, redA_, redB_, redC_, &fin, &ctl_->eval);
+    if (ce) return fail(PSI_ERR_CUDA, std::string("reduced-list kernel: ") + cudaGetErrorString((cudaError_t)ce));
+    end(PH_REDUCED);
+    // 3. broadcast depths; collect the vertices the sink does not reach
+    //    (ulist held the sink's children until here); root-path summaries
+    begin(PH_BROADCAST);
+    launch_broadcast_depth(stream_, n_, vloc_, fin, strat_, pri_, solved_, st_, node_, ulist_, &dw_->ucount,
+                           &ctl_->eval);
+    launch_rootinfo(stream_, n_, st_, node_, key_, &dw_->err, track(), &ctl_->eval);
+    end(PH_BROADCAST);
+    // 4. cycle parity by pointer jumping over the unreached vertices (the
+    //    tour's vloc array is free again: it holds the two active lists)
+    begin(PH_CYCLES);
+    int32_t *la = reinterpret_cast<int32_t *>(vloc_), *lb = la + n_;
+    ce = launch_cycles(stream_, &dw_->ucount, ulist_, strat_, pri_, solved_, st_, key_, jA_, jB_, la, lb, dw_->cnt,
+                       &dw_->err, track(), &ctl_->eval);
+    if (ce) return fail(PSI_ERR_CUDA, std::string("cycle kernel: ") + cudaGetErrorString((cudaError_t)ce));
+    PSI_CUDA_TRY(cudaMemsetAsync(&ctl_->quiet, 0, sizeof(int32_t), stream_));
+    end(PH_CYCLES);
+    return PSI_OK;
 }
 
 int Solver::compute_valuation()
@@ -409,51 +541,23 @@ int Solver::compute_valuation()
     if (!strat_ready_) return fail(PSI_ERR_STATE, "compute_valuation before init_strat");
     int rc = set_device();
     if (rc) return rc;
+    // the previous tour (and the switch steps' change list since) is usable
+    // only if no strategy changed outside a switch step since it was built
+    launch_eval_gates(stream_, ctl_, tour_valid_ ? 0 : 1, tour_valid_ ? 1 : 0,
+                      (tour_valid_ && incremental_ != PSI_INCR_OFF) ? 1 : 0);
+    const unsigned long long patches_before = hw_->patch[0];
     phase_begin(PH_EVAL);
-    // 1. Euler tour of the sink tree
-    phase_begin(PH_TOUR);
-    PSI_CUDA_TRY(cudaMemsetAsync(&dw_->ucount, 0, 2 * sizeof(int32_t), stream_));   // ucount, sinkcount
-    if (tour_valid_) {
-        // the previous tour, relinked where strategies or solved flags changed
-        // jA_ is free until the cycle pass: it holds the list of dirty parents
-        int te = launch_tour_update(stream_, n_, strat_, solved_, rev_off_, rev_src_, dirty_, succ_, vloc_, ulist_,
-                                    &dw_->sinkcount, reinterpret_cast<int32_t *>(jA_), &dw_->cnt[0]);
-        if (te) return fail(PSI_ERR_CUDA, std::string("tour update: ") + cudaGetErrorString((cudaError_t)te));
-    } else {
-        launch_tour_build(stream_, n_, strat_, solved_, rev_off_, rev_src_, succ_, vloc_, ulist_, &dw_->sinkcount,
-                          dirty_);
-    }
-    phase_end(PH_TOUR);
-    // 2. Helman-JaJa sublists, then the reduced list ranked on the device
-    phase_begin(PH_SUBLIST);
-    launch_walk_sublists(stream_, nsub_, n_, L_, stride_, succ_, vloc_, redA_, &dw_->err);
-    phase_end(PH_SUBLIST);
-    phase_begin(PH_REDUCED);
-    const int2 *fin = nullptr;
-    int re = launch_rank_reduced(stream_, nsub_, redA_, redB_, redC_, &fin);
-    if (re) return fail(PSI_ERR_CUDA, std::string("reduced-list kernel launch: ") + cudaGetErrorString((cudaError_t)re));
-    phase_end(PH_REDUCED);
-    // 3. broadcast depths; collect the vertices the sink does not reach
-    //    (ulist held the sink's children until here)
-    phase_begin(PH_BROADCAST);
-    launch_broadcast_depth(stream_, n_, vloc_, fin, strat_, pri_, solved_, st_, node_, ulist_, &dw_->ucount);
-    launch_rootinfo(stream_, n_, st_, node_, key_, &dw_->err, track());
-    phase_end(PH_BROADCAST);
-    // 4. cycle parity by pointer jumping over the unreached vertices
-    phase_begin(PH_CYCLES);
-    // the tour's vloc array is free again: it holds the two active lists
-    int32_t *la = reinterpret_cast<int32_t *>(vloc_), *lb = la + n_;
-    int ce = launch_cycles(stream_, &dw_->ucount, ulist_, strat_, pri_, solved_, st_, key_, jA_, jB_, la, lb,
-                           dw_->cnt, &dw_->err, track());
-    if (ce) return fail(PSI_ERR_CUDA, std::string("cycle kernel launch: ") + cudaGetErrorString((cudaError_t)ce));
-    phase_end(PH_CYCLES);
+    rc = enqueue_eval(true);
+    if (rc) return rc;
     phase_end(PH_EVAL);
     rc = sync_and_check("compute_valuation");
     if (rc) return rc;
-    int32_t nu = hw_->ucount;
-    last_unreached_ = nu;
-    times_.unreached += nu;
-    if (nu > 0) times_.jump_rounds += ceil_log2(nu) + 1;
+    if (hw_->patch[0] == patches_before) {   // a full evaluation: ucount is its unreached count
+        int32_t nu = hw_->ucount;
+        last_unreached_ = nu;
+        times_.unreached += nu;
+        if (nu > 0) times_.jump_rounds += ceil_log2(nu) + 1;
+    }
     times_.evals++;
     val_ready_ = true;
     tour_valid_ = true;
@@ -484,7 +588,7 @@ int Solver::switch_strategy(int32_t player, int64_t *switched)
     const int32_t *pl = plist_ + (player == 0 ? 0 : np0_);
     // jB_ is free until the next cycle pass: it holds the list of vertices to examine
     launch_switch(stream_, np, pl, player, off_, tgt_, strat_, st_, key_, node_, dw_->sw, game_of_, gcount_, gmask_,
-                  dirty_, &dw_->err, nullptr, need_, reinterpret_cast<int32_t *>(jB_), &dw_->cnt[2]);
+                  dirty_, &dw_->err, nullptr, need_, reinterpret_cast<int32_t *>(jB_), &dw_->cnt[2], changes());
     phase_end(PH_SWITCH);
     rc = sync_and_check("switch_strategy");
     if (rc) return rc;
@@ -821,7 +925,7 @@ int Solver::arena_add(const std::vector<const HostGame *> &gs, const std::vector
         const int32_t *vbd = d_tab + 2 * K + 2, *ebd = d_tab + 3 * K + 2, *sld = d_tab + 4 * K + 2;
         launch_arena_place(stream_, (int32_t)n, K, d_tab, vbd, ebd, sld, u_owner, u_pri, u_off, u_tgt, u_roff, u_rsrc,
                            owner_, pri_, off_, tgt_, rev_off_, rev_src_, strat_, st_, solved_, game_of_, gstate_,
-                           gcount_, succ_, dirty_, sig_, need_);
+                           gcount_, succ_, dirty_, need_);
         if (e == cudaSuccess) e = cudaGetLastError();
     }
     for (int i = 0; i < 7; i++)

@@ -16,7 +16,7 @@ namespace psi {
 struct PathNode;   // device_common.cuh
 
 // Device time per phase, summed over calls (CUDA events on the solver stream).
-enum Phase { PH_EVAL = 0, PH_SWITCH, PH_TOUR, PH_SUBLIST, PH_REDUCED, PH_BROADCAST, PH_CYCLES, PH_COUNT };
+enum Phase { PH_EVAL = 0, PH_SWITCH, PH_TOUR, PH_SUBLIST, PH_REDUCED, PH_BROADCAST, PH_CYCLES, PH_PATCH, PH_COUNT };
 
 struct SolverTimes {
     double ms[PH_COUNT] = {0};
@@ -27,19 +27,22 @@ struct SolverTimes {
     // the sink did not reach, pointer-jumping rounds over them)
     int64_t sw_edges = 0, sw_loads = 0, sw_changed = 0;
     int64_t unreached = 0, jump_rounds = 0;
+    // incremental evaluations (patch_kernels.cu) and the vertices they re-evaluated
+    int64_t patches = 0, patched = 0;
 };
 
 // Status word -> +1 / -1 / 0 as CPUParity's infinite[] (device_common.cuh:
 // -2 = +inf, -1 = -inf, depth >= 1 = finite).
 inline int32_t status_infinite(int32_t st) { return st == -2 ? 1 : (st == -1 ? -1 : 0); }
 
-// Control words of the graph-driven solve loop (solver_graph.cu), on the device.
-struct GraphCtl {
+// Control words on the device: the evaluation's gates (kernels.h), and those of
+// the graph-driven solve loop (solver_graph.cu).
+struct GraphCtl : EvalGates {
     enum { kRunning = 0, kConverged = 1, kEvalCap = 2, kRunaway = 3 };
-    int32_t full = 0;    // gate: the next evaluation builds the tour from scratch
-    int32_t incr = 0;    // gate: the next evaluation updates the previous tour
     int32_t even = 0;    // gate: Even's mark_solved and switch run in this step
     int32_t reset = 0;   // gate: Odd's strategy is reset before the next evaluation
+    int32_t quiet = 0;   // every need flag is set: the next evaluation's key changes flag nothing
+    int32_t patch_on = 0;   // evaluations after the first may be patches (psi_options.incremental)
     int32_t brs = 0, iters = 0, stop = kRunning, max_evals = 0;
 };
 
@@ -89,7 +92,7 @@ public:
     int32_t sublists() const { return nsub_; }
     cudaStream_t stream() const { return stream_; }
     const SolverTimes &times() const { return times_; }
-    void reset_times() { times_ = SolverTimes(); }
+    void reset_times();
     int last_unreached() const { return last_unreached_; }
     // Region timer: CUDA events on the solver stream, synchronised at the end.
     int timer_begin();
@@ -128,6 +131,12 @@ private:
     void set_extent(int32_t n);
     int sync_and_check(const char *what);
     int enqueue_step(cudaGraphConditionalHandle loop, bool reset);
+    // One evaluation on the stream, no synchronisation: the patch kernels and
+    // the full evaluation's, each set gated (which ones work is decided on
+    // the device, k_patch_begin).
+    int enqueue_eval(bool timed);
+    PatchArgs patch_args();
+    ChangeList changes() const { return clist_ ? ChangeList{clist_, &ctl_->ccount, ccap_} : ChangeList(); }
     int build_graph(bool reset);
     int get_range(const int32_t *src, int64_t v0, int64_t count, int32_t *out);
     int set_device();
@@ -172,16 +181,23 @@ private:
     // evaluation scratch
     int32_t *succ_ = nullptr, *ulist_ = nullptr;
     uint8_t *dirty_ = nullptr;   // parents whose child lists changed since the last evaluation
-    int2 *sig_ = nullptr;        // value signature of the last evaluation (ChangeTrack)
-    uint8_t *need_ = nullptr;    // vertices their owner's next switch step must examine
-    ChangeTrack track() const { return ChangeTrack{sig_, need_, rev_off_, rev_src_}; }
-    void reset_tracking();       // every vertex to be examined, no signature known
+    uint8_t *need_ = nullptr;    // vertices their owner's next switch step must examine (ChangeTrack)
+    ChangeTrack track() const { return ChangeTrack{need_, rev_off_, rev_src_, &ctl_->quiet}; }
+    void reset_tracking();       // every vertex to be examined (need = 1, quiet until the next evaluation)
     int32_t *rev_off_ = nullptr, *rev_src_ = nullptr;   // distinct in-neighbours (static)
     int2 *vloc_ = nullptr, *redA_ = nullptr, *redB_ = nullptr, *jA_ = nullptr, *jB_ = nullptr;
     int2 *redC_ = nullptr;
+    // incremental evaluation (patch_kernels.cu): the switch steps' change
+    // list, the re-evaluated set and its positions, the jump entries
+    int32_t incremental_ = 1;   // psi_options.incremental
+    int32_t *clist_ = nullptr, *alist_ = nullptr, *apos_ = nullptr;
+    int4 *pj_ = nullptr;
+    int32_t ccap_ = 0, acap_ = 0, max_levels_ = 0;
+    int64_t ucap_ = 0;   // entries of ulist_
     // small device words + pinned host mirrors
     struct Words {
         unsigned long long sw[4];   // switch counters (launch_switch)
+        unsigned long long patch[2];   // patches, vertices they re-evaluated (since reset_times)
         uint32_t err;
         int32_t ucount;             // vertices the sink did not reach
         int32_t sinkcount;          // children of the sink (tour build)

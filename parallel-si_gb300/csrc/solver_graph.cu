@@ -21,12 +21,15 @@ namespace psi {
 
 namespace {
 
-// after an evaluation: the tour is valid for updates, one more evaluation
+// after an evaluation: the tour is valid for updates (and the next
+// evaluation may be a patch), one more evaluation
 __global__ void k_ctl_evaluated(GraphCtl *c)
 {
     c->full = 0;
     c->incr = 1;
+    c->try_patch = c->patch_on;
     c->reset = 0;
+    c->quiet = 0;
     c->brs++;
 }
 
@@ -47,6 +50,7 @@ __global__ void k_ctl_even(GraphCtl *c, const unsigned long long *sw, cudaGraphC
             c->reset = 1;
             c->full = 1;              // many Odd strategies change: rebuild the tour
             c->incr = 0;
+            c->try_patch = 0;         // and no switch step lists those changes
         }
     }
     if (go && c->max_evals > 0 && c->brs >= c->max_evals) {
@@ -70,23 +74,9 @@ constexpr int32_t kEvalGuard = 1 << 20;
 int Solver::enqueue_step(cudaGraphConditionalHandle loop, bool reset)
 {
     launch_reset_odd(stream_, n_, owner_, off_, tgt_, strat_, &ctl_->reset, need_);
-    // evaluation (as compute_valuation, with both tour paths gated)
-    PSI_CUDA_TRY(cudaMemsetAsync(&dw_->ucount, 0, 2 * sizeof(int32_t), stream_));   // ucount, sinkcount
-    launch_tour_build(stream_, n_, strat_, solved_, rev_off_, rev_src_, succ_, vloc_, ulist_, &dw_->sinkcount, dirty_,
-                      &ctl_->full);
-    int ce = launch_tour_update(stream_, n_, strat_, solved_, rev_off_, rev_src_, dirty_, succ_, vloc_, ulist_,
-                                &dw_->sinkcount, reinterpret_cast<int32_t *>(jA_), &dw_->cnt[0], &ctl_->incr);
-    if (ce) return fail(PSI_ERR_CUDA, std::string("tour update: ") + cudaGetErrorString((cudaError_t)ce));
-    launch_walk_sublists(stream_, nsub_, n_, L_, stride_, succ_, vloc_, redA_, &dw_->err);
-    const int2 *fin = nullptr;
-    ce = launch_rank_reduced(stream_, nsub_, redA_, redB_, redC_, &fin);
-    if (ce) return fail(PSI_ERR_CUDA, std::string("reduced-list kernel: ") + cudaGetErrorString((cudaError_t)ce));
-    launch_broadcast_depth(stream_, n_, vloc_, fin, strat_, pri_, solved_, st_, node_, ulist_, &dw_->ucount);
-    launch_rootinfo(stream_, n_, st_, node_, key_, &dw_->err, track());
-    int32_t *la = reinterpret_cast<int32_t *>(vloc_), *lb = la + n_;
-    ce = launch_cycles(stream_, &dw_->ucount, ulist_, strat_, pri_, solved_, st_, key_, jA_, jB_, la, lb, dw_->cnt,
-                       &dw_->err, track());
-    if (ce) return fail(PSI_ERR_CUDA, std::string("cycle kernel: ") + cudaGetErrorString((cudaError_t)ce));
+    // evaluation (as compute_valuation: a patch or the full evaluation, gated)
+    int rc = enqueue_eval(false);
+    if (rc) return rc;
     count_launch();
     k_ctl_evaluated<<<1, 1, 0, stream_>>>(ctl_);
     // Odd: mark_solved(1), switch(1)
@@ -94,14 +84,14 @@ int Solver::enqueue_step(cudaGraphConditionalHandle loop, bool reset)
     PSI_CUDA_TRY(cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_));
     int32_t *todo = reinterpret_cast<int32_t *>(jB_);   // free until the next cycle pass
     launch_switch(stream_, np_ - np0_, plist_ + np0_, 1, off_, tgt_, strat_, st_, key_, node_, dw_->sw, nullptr,
-                  nullptr, nullptr, dirty_, &dw_->err, nullptr, need_, todo, &dw_->cnt[2]);
+                  nullptr, nullptr, dirty_, &dw_->err, nullptr, need_, todo, &dw_->cnt[2], changes());
     count_launch();
     k_ctl_odd<<<1, 1, 0, stream_>>>(ctl_, dw_->sw);
     // Even, when Odd made no strict improvement: mark_solved(0), switch(0)
     launch_mark_solved(stream_, &dw_->ucount, ulist_, 0, st_, solved_, dirty_, nullptr, nullptr, &ctl_->even);
     PSI_CUDA_TRY(cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_));
     launch_switch(stream_, np0_, plist_, 0, off_, tgt_, strat_, st_, key_, node_, dw_->sw, nullptr, nullptr, nullptr,
-                  dirty_, &dw_->err, &ctl_->even, need_, todo, &dw_->cnt[2]);
+                  dirty_, &dw_->err, &ctl_->even, need_, todo, &dw_->cnt[2], changes());
     count_launch();
     k_ctl_even<<<1, 1, 0, stream_>>>(ctl_, dw_->sw, loop, reset ? 1 : 0, kEvalGuard);
     PSI_CUDA_TRY(cudaGetLastError());
@@ -153,6 +143,8 @@ int Solver::solve_graph(int32_t reset, int32_t *iters, int32_t *brs, int64_t max
     }
     GraphCtl init;
     init.full = 1;   // init_strat: the first evaluation builds the tour
+    init.quiet = 1;  // and every need flag is set
+    init.patch_on = incremental_ != PSI_INCR_OFF ? 1 : 0;
     init.max_evals = max_evals > 0 && max_evals < INT32_MAX ? (int32_t)max_evals : 0;
     PSI_CUDA_TRY(cudaMemcpyAsync(ctl_, &init, sizeof init, cudaMemcpyHostToDevice, stream_));
     PSI_CUDA_TRY(cudaGraphLaunch(graph_exec_, stream_));

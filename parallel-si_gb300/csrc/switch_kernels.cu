@@ -23,10 +23,13 @@
 // gpu_parity.cu:264-300): scan the successors in CSR order, move to a
 // successor only on a strict improvement for the owner, count the moves.
 #include <climits>
+#include <cooperative_groups.h>
 #include <cub/block/block_reduce.cuh>
 
 #include "device_common.cuh"
 #include "kernels.h"
+
+namespace cg = cooperative_groups;
 
 namespace psi {
 
@@ -170,6 +173,20 @@ __global__ void k_need_list(int32_t np, const int32_t *__restrict__ plist, const
     }
 }
 
+// Appends a changed vertex to the change list, one atomic per group of lanes
+// that changed together; nothing once the list has overflowed (its count
+// then stays above the capacity, which marks it incomplete).
+__device__ __forceinline__ void note_change(const ChangeList &c, int32_t v)
+{
+    if (*(volatile int32_t *)c.count > c.cap) return;
+    cg::coalesced_group grp = cg::coalesced_threads();
+    int32_t base = 0;
+    if (grp.thread_rank() == 0) base = atomicAdd(c.count, (int32_t)grp.size());
+    base = grp.shfl(base, 0);
+    const int32_t p = base + (int32_t)grp.thread_rank();
+    if (p < c.cap) c.list[p] = v;
+}
+
 // One thread per vertex of the list (all owned by `player`; the list is plist
 // itself, np entries, or -- with count != nullptr -- the *count vertices
 // k_need_list selected).  Per compared edge the common case is one 4-byte
@@ -194,7 +211,8 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
                                                    unsigned long long *__restrict__ gcount,
                                                    const int32_t *__restrict__ gmask,
                                                    uint8_t *__restrict__ dirty, uint32_t *__restrict__ err,
-                                                   const int32_t *__restrict__ gate, uint8_t *__restrict__ need)
+                                                   const int32_t *__restrict__ gate, uint8_t *__restrict__ need,
+                                                   ChangeList changes)
 {
     if (gate && !*gate) return;
     if (count) np = *count;
@@ -291,6 +309,7 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
             if (game_of) atomicAdd(&gcount[game_of[v]], (unsigned long long)moves);
             t_changed++;
             t_moves += moves;
+            if (changes.list) note_change(changes, v);
         }
     }
     typedef cub::BlockReduce<longlong4, kBlock> Reduce;
@@ -383,7 +402,7 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
                    const int32_t *tgt, int32_t *strat, const int32_t *st, const int32_t *key, const PathNode *node,
                    unsigned long long *stats, const int32_t *game_of, unsigned long long *gcount,
                    const int32_t *gmask, uint8_t *dirty, uint32_t *err, const int32_t *gate, uint8_t *need,
-                   int32_t *list, int32_t *list_count)
+                   int32_t *list, int32_t *list_count, ChangeList changes)
 {
     if (np <= 0) return;
     static int blocks = 0;   // resident blocks on the device (same device for the process's solvers)
@@ -401,7 +420,7 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
     }
     count_launch();
     k_switch<<<g, kBlock, 0, s>>>(np, items, count, player, off, tgt, strat, st, key, node, stats, game_of, gcount,
-                                  gmask, dirty, err, gate, need);
+                                  gmask, dirty, err, gate, need, changes);
 }
 
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state, unsigned long long *gcount)

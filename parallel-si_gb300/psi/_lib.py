@@ -45,7 +45,8 @@ class Options(C.Structure):
         ("sublist_len", C.c_int32),
         ("timing", C.c_int32),
         ("graph", C.c_int32),
-        ("reserved", C.c_int32 * 3),
+        ("incremental", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -119,9 +120,10 @@ _SIGS = {
     "psi_server_info": ([_vp, _i32p, _i32p, _i64p, _i64p], C.c_int),
 }
 
-COUNTERS = ("evals", "switches", "sw_edges", "sw_loads", "sw_changed", "unreached", "jump_rounds")
+COUNTERS = ("evals", "switches", "sw_edges", "sw_loads", "sw_changed", "unreached", "jump_rounds", "patches",
+            "patched")
 
-PHASES = ("eval", "switch", "tour", "sublist", "reduced", "broadcast", "cycles")
+PHASES = ("eval", "switch", "tour", "sublist", "reduced", "broadcast", "cycles", "patch")
 
 for _name, (_args, _res) in _SIGS.items():
     _f = getattr(lib, _name)
