@@ -55,6 +55,9 @@ def workload_config(n, m=None, seed=1):
                       "from the same kernels in the host-driven loop",
         "l2": "inputs larger than L2 (game CSR + solver state ~1.3 GB at n=2^24), no flush",
         "parallelism": "replicas: one independent game per GPU",
+        "evaluation": "incremental where few strategies changed (psi_options.incremental = auto: patches after "
+                      "steps that changed <= max(1024, n/1024) strategies, else the full Euler-tour evaluation); "
+                      "results identical to full evaluations",
     }
     if m is not None:
         cfg["m"] = m
@@ -211,6 +214,10 @@ def phase_bytes(phase, n, m, nsub, counters, calls, n_even, n_odd, iters, brs):
 
 KERNEL_OF_PHASE = {"switch": "k_switch", "sublist": "k_walk_sublists", "tour": "k_tour_relink",
                    "broadcast": "k_broadcast_depth", "reduced": "k_rank_reduced", "cycles": "k_cycles"}
+# phases of the full evaluation: their kernels work only in evaluations that
+# are not patches (in a patch they return at their gate), so their per-launch
+# time is their phase time over the full evaluations
+FULL_EVAL_PHASES = ("sublist", "tour", "broadcast", "reduced", "cycles")
 
 
 def cpu_baseline_sample(solves=3, seed=1):
@@ -277,7 +284,8 @@ def run_gb300(args, rank, world, local):
     n_even = game.n - n_odd
     # the product path: psi_solve with default options (the whole solve_si
     # loop as one CUDA graph, device-side loop control)
-    solver = psi.GPUList(game, device=local, sublist_len=args.sublist_len, graph=int(not args.host_loop))
+    solver = psi.GPUList(game, device=local, sublist_len=args.sublist_len, graph=int(not args.host_loop),
+                         patch_limit=args.patch_limit)
 
     for _ in range(args.warmup):
         solver.solve()
@@ -306,7 +314,8 @@ def run_gb300(args, rank, world, local):
     if args.host_loop:
         phase_solver = solver
     else:
-        phase_solver = psi.GPUList(game, device=local, sublist_len=args.sublist_len, graph=0)
+        phase_solver = psi.GPUList(game, device=local, sublist_len=args.sublist_len, graph=0,
+                                   patch_limit=args.patch_limit)
         phase_solver.solve()
         phase_solver.reset_times()
         for _ in range(args.steps):
@@ -316,11 +325,16 @@ def run_gb300(args, rank, world, local):
     if phase_solver is not solver:
         phase_solver.close()
     nsub = (2 * game.n + 1 + args.sublist_len - 1) // args.sublist_len + 1
+    full_evals = max(1, counters["evals"] - counters["patches"])
 
-    # roofline of the dominant kernel-level phase
+    def launches_of(p):
+        return full_evals if p in FULL_EVAL_PHASES else phases[p][1]
+
+    # roofline of the dominant kernel-level phase (the patch phase, a few
+    # latency-bound cooperative launches per evaluation, is reported apart)
     kernel_phases = ("switch", "sublist", "tour", "broadcast", "reduced", "cycles")
     dom = max(kernel_phases, key=lambda p: phases[p][0])
-    dom_ms, dom_calls = phases[dom]
+    dom_ms, dom_calls = phases[dom][0], launches_of(dom)
     bpc = phase_bytes(dom, game.n, game.m, nsub, counters, dom_calls, n_even, n_odd, iters, brs)
     peak, peak_kind = hbm_peak()
     roofline = None
@@ -336,7 +350,7 @@ def run_gb300(args, rank, world, local):
             roofline["traffic_frac"] = roofline["traffic_GBps"] / peak
     lr = {}
     for p in ("sublist", "tour", "broadcast"):
-        pm, pc = phases[p]
+        pm, pc = phases[p][0], launches_of(p)
         b = phase_bytes(p, game.n, game.m, nsub, counters, pc, n_even, n_odd, iters, brs)
         if pc:
             lr[p] = {"ms_per_call": pm / pc, "GBps": b / (pm / pc / 1e3) / 1e9, "frac": b / (pm / pc / 1e3) / 1e9 / peak}
@@ -350,7 +364,7 @@ def run_gb300(args, rank, world, local):
     e2e_iters = 0
     d2h = 0
     for _ in range(args.steps):
-        s2 = psi.GPUList.from_csr(*csr, device=local, sublist_len=args.sublist_len)
+        s2 = psi.GPUList.from_csr(*csr, device=local, sublist_len=args.sublist_len, patch_limit=args.patch_limit)
         it, _ = s2.solve()
         w0 = s2.get_winning(0)
         strat = s2.get_strategy()
@@ -368,7 +382,7 @@ def run_gb300(args, rank, world, local):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic", "config": dict(workload_config(game.n, game.m, args.seed),
-                                                sublist_len=args.sublist_len,
+                                                sublist_len=args.sublist_len, patch_limit=args.patch_limit,
                                                 iters_per_solve=iters // args.steps, brs_per_solve=brs // args.steps),
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
             "e2e": {"value": e2e_iters_all / e2e_max, "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -550,6 +564,8 @@ def main():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--sublist-len", type=int, default=64)
+    ap.add_argument("--patch-limit", type=int, default=0,
+                    help="psi_options.patch_limit (0: the library default, max(1024, n/1024))")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--host-loop", action="store_true",
                     help="time the host-driven solve loop instead of the default one-graph solve")

@@ -36,6 +36,7 @@ int check_options(const psi_options &opt)
     if (opt.sublist_len < 2) return fail(PSI_ERR_INVALID, "sublist_len must be >= 2");
     if (opt.incremental < PSI_INCR_OFF || opt.incremental > PSI_INCR_ALWAYS)
         return fail(PSI_ERR_INVALID, "unknown incremental mode");
+    if (opt.patch_limit < 0) return fail(PSI_ERR_INVALID, "patch_limit must be >= 0");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0) return fail(PSI_ERR_NO_DEVICE, "no CUDA device available");
@@ -58,6 +59,7 @@ int Solver::create(const CsrView &g, const psi_options &opt, Solver **out, bool 
     s->stride_ = opt.sublist_len;
     s->use_graph_ = opt.graph != 0;
     s->incremental_ = opt.incremental;
+    s->patch_limit_ = opt.patch_limit;
     rc = s->alloc_arrays(g.n, g.m);
     if (!rc) rc = s->upload_game(g, validate);
     if (rc) {
@@ -128,6 +130,7 @@ int Solver::create_union(const std::vector<const HostGame *> &gs, const psi_opti
     s->stride_ = opt.sublist_len;
     s->use_graph_ = opt.graph != 0;
     s->incremental_ = opt.incremental;
+    s->patch_limit_ = opt.patch_limit;
     rc = s->alloc_arrays(n, m);
     if (!rc) rc = s->upload_union(gs, table, base->back());
     if (rc) {
@@ -199,7 +202,7 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
     // evaluation), re-evaluated set capacity, level cap of its search
     if (incremental_ != PSI_INCR_OFF) {
         const bool always = incremental_ == PSI_INCR_ALWAYS;
-        const int64_t cc = always ? cap_n : std::max<int64_t>(1024, cap_n >> 10);
+        const int64_t cc = always ? cap_n : patch_limit_ > 0 ? patch_limit_ : std::max<int64_t>(1024, cap_n >> 10);
         const int64_t ac = always ? cap_n : std::max<int64_t>(4096, cap_n >> 3);
         ccap_ = (int32_t)std::max<int64_t>(1, std::min(cc, cap_n));
         acap_ = (int32_t)std::max<int64_t>(1, std::min(ac, cap_n));

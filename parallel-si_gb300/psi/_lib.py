@@ -46,7 +46,8 @@ class Options(C.Structure):
         ("timing", C.c_int32),
         ("graph", C.c_int32),
         ("incremental", C.c_int32),
-        ("reserved", C.c_int32 * 2),
+        ("patch_limit", C.c_int32),
+        ("reserved", C.c_int32 * 1),
     ]
 
 
