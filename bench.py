@@ -7,9 +7,9 @@ game of n = 2^24 vertices, solved on GB300 (one game replica per GPU).
 A step is one full solve (solve_si: init_strat until Even makes no switch) of
 the 2^24-vertex game resident in HBM.  value = SI iterations of all ranks /
 max-over-ranks device time of the K timed solves (CUDA events on the solver
-stream).  e2e repeats the solve through the C ABI from host buffers: upload of
-the game, the solve, and the read-back of the winning set and strategy are
-inside the timed region.  Prints one JSON line (rank 0).
+stream).  e2e repeats the solve through the C ABI from page-locked host buffers
+(psi_host_alloc): upload of the game, the solve, and the read-back of the
+winning set and strategy are inside the timed region.  Prints one JSON line (rank 0).
 
 --impl reference times the reference algorithm's CPU implementation instead:
 the oracle (a C restatement of the reference's CPUParity), single thread, on a
@@ -355,8 +355,13 @@ def run_gb300(args, rank, world, local):
         if pc:
             lr[p] = {"ms_per_call": pm / pc, "GBps": b / (pm / pc / 1e3) / 1e9, "frac": b / (pm / pc / 1e3) / 1e9 / peak}
 
-    # end to end through the C ABI from host buffers
-    csr = [np.ascontiguousarray(a, dtype=np.int32) for a in game.csr()]
+    # end to end through the C ABI from page-locked host buffers (psi_host_alloc)
+    csr = []
+    for a in game.csr():
+        h = psi.pinned(len(a))
+        h[:] = a
+        csr.append(h)
+    out_w, out_s = psi.pinned(game.n), psi.pinned(game.n)
     h2d = sum(int(a.nbytes) for a in csr)        # owner, priority, offsets, targets (int32)
     del solver
     dist.barrier()
@@ -366,8 +371,8 @@ def run_gb300(args, rank, world, local):
     for _ in range(args.steps):
         s2 = psi.GPUList.from_csr(*csr, device=local, sublist_len=args.sublist_len, patch_limit=args.patch_limit)
         it, _ = s2.solve()
-        w0 = s2.get_winning(0)
-        strat = s2.get_strategy()
+        w0 = s2.get_winning(0, out=out_w)
+        strat = s2.get_strategy(out=out_s)
         s2.close()
         e2e_iters += it
         d2h = 4 * (len(w0) + 1) + int(strat.nbytes)   # winning set and its size, strategy

@@ -170,6 +170,9 @@ int psi_solver_reset_times(psi_solver *s);
 enum { PSI_PHASE_EVAL = 0, PSI_PHASE_SWITCH, PSI_PHASE_TOUR, PSI_PHASE_SUBLIST, PSI_PHASE_REDUCED,
        PSI_PHASE_BROADCAST, PSI_PHASE_CYCLES, PSI_PHASE_PATCH, PSI_PHASE_COUNT };
 int psi_solver_phase_times(psi_solver *s, double *ms, int64_t *calls, int32_t nphases);
+/* The solver's game: vertices, edges and largest priority (computed on the
+ * device when the solver was created from a CSR).  Any pointer may be NULL. */
+int psi_solver_info(psi_solver *s, int32_t *n, int64_t *m, int32_t *max_pri);
 /* The solver's CUDA stream (a cudaStream_t), so callers can order their own
  * work or record events against it. */
 int psi_solver_stream(psi_solver *s, void **stream);
@@ -183,6 +186,11 @@ int psi_solver_unreached(psi_solver *s, int64_t *count);
 int psi_solver_counters(psi_solver *s, int64_t *out, int32_t k);
 /* Kernel launches issued by this library in this process so far. */
 int64_t psi_launch_count(void);
+/* Page-locked host memory (cudaMallocHost), for callers that upload games and
+ * read results back at full DMA speed: every psi_* call that takes or fills a
+ * host array accepts it.  psi_host_free(NULL) does nothing. */
+int psi_host_alloc(size_t bytes, void **out);
+void psi_host_free(void *p);
 /* Region timer on the solver stream: begin synchronises the stream and records
  * a CUDA event; end records a second one, waits for it and returns the elapsed
  * device time in ms (host gaps between the solver's launches included). */

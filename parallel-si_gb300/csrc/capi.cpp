@@ -317,6 +317,15 @@ int psi_solver_phase_times(psi_solver *s, double *ms, int64_t *calls, int32_t np
     return PSI_OK;
 }
 
+int psi_solver_info(psi_solver *s, int32_t *n, int64_t *m, int32_t *max_pri)
+{
+    if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null solver");
+    if (n) *n = s->s->n();
+    if (m) *m = s->s->m();
+    if (max_pri) *max_pri = s->s->max_pri();
+    return PSI_OK;
+}
+
 int psi_solver_counters(psi_solver *s, int64_t *out, int32_t k)
 {
     if (!s || !s->s || !out) return psi::fail(PSI_ERR_INVALID, "null argument");
@@ -328,6 +337,25 @@ int psi_solver_counters(psi_solver *s, int64_t *out, int32_t k)
 }
 
 int64_t psi_launch_count(void) { return psi::launch_count(); }
+
+int psi_host_alloc(size_t bytes, void **out)
+{
+    if (!out) return psi::fail(PSI_ERR_INVALID, "null argument");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return psi::fail(PSI_ERR_NO_DEVICE, "no CUDA device available");
+    cudaError_t e = cudaMallocHost(out, bytes ? bytes : 1);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return psi::fail(PSI_ERR_NOMEM, std::string("page-locked host allocation: ") + cudaGetErrorString(e));
+    }
+    return PSI_OK;
+}
+
+void psi_host_free(void *p)
+{
+    if (p) cudaFreeHost(p);
+}
 
 int psi_solver_timer_begin(psi_solver *s)
 {

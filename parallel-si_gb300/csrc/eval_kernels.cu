@@ -500,12 +500,14 @@ __global__ void __launch_bounds__(kBlock, 6) k_cycles(const int32_t *__restrict_
 __global__ void k_mark_solved(const int32_t *__restrict__ ucount, const int32_t *__restrict__ ulist,
                               int32_t player, const int32_t *__restrict__ st, uint8_t *__restrict__ solved,
                               uint8_t *__restrict__ dirty, const int32_t *__restrict__ game_of,
-                              const int32_t *__restrict__ gmask, const int32_t *__restrict__ gate)
+                              const int32_t *__restrict__ gmask, const int32_t *__restrict__ gate,
+                              int32_t *__restrict__ from, uint32_t *__restrict__ done)
 {
     if (gate && !*gate) return;
-    int32_t nu = *ucount;
-    int32_t target = (player == 0) ? ST_POS_INF : ST_NEG_INF;
-    for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < nu; i += gridDim.x * blockDim.x) {
+    const int32_t nu = *ucount;
+    const int32_t i0 = from ? *from : 0;
+    const int32_t target = (player == 0) ? ST_POS_INF : ST_NEG_INF;
+    for (int32_t i = i0 + blockIdx.x * blockDim.x + threadIdx.x; i < nu; i += gridDim.x * blockDim.x) {
         int32_t u = ulist[i];
         if (gmask) {
             int32_t g = game_of[u];
@@ -515,6 +517,20 @@ __global__ void k_mark_solved(const int32_t *__restrict__ ucount, const int32_t 
             solved[u] = 1;
             dirty[u] = 1;
         }
+    }
+    if (!from) return;
+    // the last block to finish (every block has read *from by then) moves
+    // the start past the entries scanned
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        *from = nu;
+        *done = 0;
     }
 }
 
@@ -676,10 +692,11 @@ int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, c
 
 void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, int32_t player,
                         const int32_t *st, uint8_t *solved, uint8_t *dirty, const int32_t *game_of,
-                        const int32_t *gmask, const int32_t *gate)
+                        const int32_t *gmask, const int32_t *gate, int32_t *from, uint32_t *done)
 {
     count_launch();
-    k_mark_solved<<<608, kBlock, 0, s>>>(ucount, ulist, player, st, solved, dirty, game_of, gmask, gate);
+    k_mark_solved<<<608, kBlock, 0, s>>>(ucount, ulist, player, st, solved, dirty, game_of, gmask, gate, from,
+                                         done);
 }
 
 }  // namespace psi

@@ -39,6 +39,8 @@ struct EvalGates {
     int32_t lcnt[3] = {0, 0, 0};              // per-level append counters of the patch's search
     int32_t saved_full = 0, saved_incr = 0;   // tour gates while a patch holds them closed
     int32_t skip = 0, backoff = 1;            // evaluations not to try a patch after a failed one
+    int32_t mfrom[2] = {0, 0};   // per player: unreached-list index its next mark_solved scans from
+    uint32_t mdone = 0;          // blocks of the running mark_solved that have finished
 };
 
 // A list of the vertices whose strategy a switch step changes (appended while
@@ -133,11 +135,16 @@ int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, c
                   int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err, ChangeTrack track = ChangeTrack(),
                   const int32_t *gate = nullptr);
 // mark_solved over the last evaluation's unreached vertices (cpu_parity.cpp:265-274);
-// with game_of/gmask only for games whose mask is set (nullptr: all).
+// with game_of/gmask only for games whose mask is set (nullptr: all).  With
+// from (a device word; done: a zeroed counter) only the entries from *from on
+// are scanned, and *from moves to the list's end: the entries before it were
+// scanned by this player's last mark_solved, and a vertex whose status has
+// changed since was appended again by a patch (EvalGates::mfrom).
 // Newly solved vertices are flagged in dirty (their children leave the tour).
 void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, int32_t player,
                         const int32_t *st, uint8_t *solved, uint8_t *dirty, const int32_t *game_of = nullptr,
-                        const int32_t *gmask = nullptr, const int32_t *gate = nullptr);
+                        const int32_t *gmask = nullptr, const int32_t *gate = nullptr,
+                        int32_t *from = nullptr, uint32_t *done = nullptr);
 
 // ---- all-switches (gpu_parity.cu:191-317, cpu_parity.cpp:154-263)
 // Switches the np vertices listed in plist (all owned by `player`).

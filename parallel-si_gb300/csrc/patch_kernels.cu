@@ -93,6 +93,7 @@ __global__ void k_patch_begin(PatchArgs a)
         g->patch = 0;
         *a.ucount = 0;      // the full evaluation collects the unreached vertices afresh
         *a.sinkcount = 0;
+        g->mfrom[0] = g->mfrom[1] = 0;
     }
 }
 
@@ -215,6 +216,7 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_collect(PatchArgs a)
         g->incr = g->saved_incr;
         *a.ucount = 0;
         *a.sinkcount = 0;
+        g->mfrom[0] = g->mfrom[1] = 0;
         g->skip = g->backoff;
         g->backoff = g->backoff < kBackoffMax ? 2 * g->backoff : kBackoffMax;
     }

@@ -573,8 +573,9 @@ int Solver::mark_solved(int32_t player)
     if (!val_ready_) return fail(PSI_ERR_STATE, "mark_solved before compute_valuation");
     int rc = set_device();
     if (rc) return rc;
+    // a masked step (served games) scans the whole list
     launch_mark_solved(stream_, &dw_->ucount, ulist_, player, st_, solved_, dirty_, gmask_ ? game_of_ : nullptr,
-                       gmask_);
+                       gmask_, nullptr, gmask_ ? nullptr : &ctl_->mfrom[player], &ctl_->mdone);
     PSI_CUDA_TRY(cudaGetLastError());
     return PSI_OK;   // ordered on the stream before the next call
 }

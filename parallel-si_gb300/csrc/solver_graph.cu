@@ -80,7 +80,8 @@ int Solver::enqueue_step(cudaGraphConditionalHandle loop, bool reset)
     count_launch();
     k_ctl_evaluated<<<1, 1, 0, stream_>>>(ctl_);
     // Odd: mark_solved(1), switch(1)
-    launch_mark_solved(stream_, &dw_->ucount, ulist_, 1, st_, solved_, dirty_);
+    launch_mark_solved(stream_, &dw_->ucount, ulist_, 1, st_, solved_, dirty_, nullptr, nullptr, nullptr,
+                       &ctl_->mfrom[1], &ctl_->mdone);
     PSI_CUDA_TRY(cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_));
     int32_t *todo = reinterpret_cast<int32_t *>(jB_);   // free until the next cycle pass
     launch_switch(stream_, np_ - np0_, plist_ + np0_, 1, off_, tgt_, strat_, st_, key_, node_, dw_->sw, nullptr,
@@ -88,7 +89,8 @@ int Solver::enqueue_step(cudaGraphConditionalHandle loop, bool reset)
     count_launch();
     k_ctl_odd<<<1, 1, 0, stream_>>>(ctl_, dw_->sw);
     // Even, when Odd made no strict improvement: mark_solved(0), switch(0)
-    launch_mark_solved(stream_, &dw_->ucount, ulist_, 0, st_, solved_, dirty_, nullptr, nullptr, &ctl_->even);
+    launch_mark_solved(stream_, &dw_->ucount, ulist_, 0, st_, solved_, dirty_, nullptr, nullptr, &ctl_->even,
+                       &ctl_->mfrom[0], &ctl_->mdone);
     PSI_CUDA_TRY(cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_));
     launch_switch(stream_, np0_, plist_, 0, off_, tgt_, strat_, st_, key_, node_, dw_->sw, nullptr, nullptr, nullptr,
                   dirty_, &dw_->err, &ctl_->even, need_, todo, &dw_->cnt[2], changes());

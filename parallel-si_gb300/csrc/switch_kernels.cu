@@ -138,7 +138,11 @@ __device__ int compare_equal_keys(const PathNode *__restrict__ node, const int32
 // gcount[game of the vertex]; with gmask only vertices of games whose mask is
 // set switch.
 // The vertices of plist whose need flag is set (and, with gmask, whose game
-// takes this step), appended to list with one atomic per block.
+// takes this step), appended to list with one atomic per block.  A block
+// pass covers kNeedPer * blockDim entries (each thread kNeedPer of them,
+// blockDim apart, so every load is coalesced; plist + offset may not be
+// 16-byte aligned, so no vector loads): two block barriers per pass.
+constexpr int kNeedPer = 4;
 __global__ void k_need_list(int32_t np, const int32_t *__restrict__ plist, const uint8_t *__restrict__ need,
                             const int32_t *__restrict__ game_of, const int32_t *__restrict__ gmask,
                             const int32_t *__restrict__ gate, int32_t *__restrict__ list, int32_t *__restrict__ count)
@@ -146,30 +150,45 @@ __global__ void k_need_list(int32_t np, const int32_t *__restrict__ plist, const
     if (gate && !*gate) return;
     __shared__ int32_t warp_base[kBlock / 32];
     __shared__ int32_t block_base;
-    for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < np; b0 += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t i = b0 + threadIdx.x;
-        int32_t v = -1;
-        bool take = false;
-        if (i < np) {
-            v = plist[i];
-            take = need[v] && (!gmask || gmask[game_of[v]]);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t pass = (int64_t)kNeedPer * blockDim.x;
+    for (int64_t b0 = (int64_t)blockIdx.x * pass; b0 < np; b0 += (int64_t)gridDim.x * pass) {
+        int32_t v[kNeedPer];
+        int mine = 0;
+#pragma unroll
+        for (int k = 0; k < kNeedPer; k++) {
+            const int64_t i = b0 + (int64_t)k * blockDim.x + threadIdx.x;
+            v[k] = (i < np) ? plist[i] : -1;
         }
-        const unsigned mask = __ballot_sync(0xffffffffu, take);
-        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-        if (lane == 0) warp_base[w] = __popc(mask);
+#pragma unroll
+        for (int k = 0; k < kNeedPer; k++) {
+            const bool take = v[k] >= 0 && need[v[k]] && (!gmask || gmask[game_of[v[k]]]);
+            if (!take) v[k] = -1;
+            mine += take;
+        }
+        int32_t incl = mine;   // inclusive prefix over the warp
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) warp_base[w] = incl;
         __syncthreads();
         if (threadIdx.x == 0) {
             int32_t sum = 0;
             for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
-                int32_t t = warp_base[k];
+                const int32_t t = warp_base[k];
                 warp_base[k] = sum;
                 sum += t;
             }
             block_base = sum ? atomicAdd(count, sum) : 0;
         }
         __syncthreads();
-        if (take) list[block_base + warp_base[w] + __popc(mask & ((1u << lane) - 1))] = v;
-        __syncthreads();
+        int32_t at = block_base + warp_base[w] + incl - mine;
+#pragma unroll
+        for (int k = 0; k < kNeedPer; k++)
+            if (v[k] >= 0) list[at++] = v[k];
+        __syncthreads();   // warp_base and block_base are rewritten by the next pass
     }
 }
 
@@ -413,8 +432,10 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
     if (need && list && list_count) {
         // only the vertices whose need flag is set (ChangeTrack)
         cudaMemsetAsync(list_count, 0, sizeof(int32_t), s);
+        unsigned gn = grid_for(ceil_div(np, kNeedPer));
+        gn = gn < (unsigned)blocks ? gn : (unsigned)blocks;
         count_launch();
-        k_need_list<<<g, kBlock, 0, s>>>(np, plist, need, game_of, gmask, gate, list, list_count);
+        k_need_list<<<gn, kBlock, 0, s>>>(np, plist, need, game_of, gmask, gate, list, list_count);
         items = list;
         count = list_count;
     }

@@ -28,6 +28,28 @@ def version() -> str:
     return lib.psi_version().decode()
 
 
+def _out_array(out: np.ndarray, n: int) -> np.ndarray:
+    if out.dtype != np.int32 or not out.flags.c_contiguous or out.size < n:
+        raise ValueError(f"out must be a contiguous int32 array of at least {n} entries")
+    return out
+
+
+def pinned(shape, dtype=np.int32) -> np.ndarray:
+    """An uninitialised numpy array in page-locked host memory
+    (psi_host_alloc), freed when the array and its views are gone: uploads
+    from it and read-backs into it run at full DMA speed."""
+    import weakref
+
+    dt = np.dtype(dtype)
+    count = int(np.prod(shape)) if np.ndim(shape) else int(shape)
+    nbytes = max(1, count * dt.itemsize)
+    p = C.c_void_p()
+    check(lib.psi_host_alloc(nbytes, C.byref(p)))
+    buf = (C.c_char * nbytes).from_address(p.value)
+    weakref.finalize(buf, lib.psi_host_free, C.c_void_p(p.value))
+    return np.frombuffer(buf, dtype=dt, count=count).reshape(shape)
+
+
 def default_options(**kw) -> Options:
     o = Options()
     lib.psi_options_default(C.byref(o))
@@ -157,8 +179,9 @@ class GPUList:
         tg = np.ascontiguousarray(targets, dtype=np.int32)
         s = cls(None)
         check(lib.psi_solver_create_csr(len(ow), ptr(ow), ptr(pr), ptr(off), ptr(tg), C.byref(o), C.byref(s._h)))
-        s.n = len(ow)
-        s.max_pri = int(pr.max()) if len(pr) else 0
+        n, mp = C.c_int32(), C.c_int32()
+        check(lib.psi_solver_info(s._h, C.byref(n), None, C.byref(mp)))   # max priority found on the device
+        s.n, s.max_pri = n.value, mp.value
         return s
 
     # ---- StrategyImprovement
@@ -179,9 +202,11 @@ class GPUList:
         check(lib.psi_switch_strategy(self._h, player, C.byref(k)))
         return k.value
 
-    def get_winning(self, player: int) -> np.ndarray:
+    def get_winning(self, player: int, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """The winning set in increasing vertex order; `out` (int32, n
+        entries, e.g. from pinned()) receives it when given."""
         cnt = C.c_int64()
-        out = np.empty(self.n, np.int32)
+        out = np.empty(self.n, np.int32) if out is None else _out_array(out, self.n)
         check(lib.psi_get_winning(self._h, player, ptr(out), self.n, C.byref(cnt)))
         return out[: cnt.value]
 
@@ -189,8 +214,8 @@ class GPUList:
         check(lib.psi_reset_opponent_strategy(self._h))
 
     # ---- state
-    def get_strategy(self) -> np.ndarray:
-        out = np.empty(self.n, np.int32)
+    def get_strategy(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        out = np.empty(self.n, np.int32) if out is None else _out_array(out, self.n)
         check(lib.psi_get_strategy(self._h, ptr(out)))
         return out
 

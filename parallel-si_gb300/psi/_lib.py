@@ -101,6 +101,9 @@ _SIGS = {
     "psi_solver_unreached": ([_vp, _i64p], C.c_int),
     "psi_solver_counters": ([_vp, _i64p, C.c_int32], C.c_int),
     "psi_launch_count": ([], C.c_int64),
+    "psi_host_alloc": ([C.c_size_t, _pp], C.c_int),
+    "psi_solver_info": ([_vp, _i32p, _i64p, _i32p], C.c_int),
+    "psi_host_free": ([_vp], None),
     "psi_solver_timer_begin": ([_vp], C.c_int),
     "psi_solver_timer_end": ([_vp, C.POINTER(C.c_double)], C.c_int),
     "psi_generate_batch_sizes": ([C.c_int32, C.c_int32, C.c_int32, C.c_uint64, _vp], C.c_int),

@@ -59,6 +59,22 @@ def test_solver_without_gpu_fails_loudly():
         psi.GPUList(g)
 
 
+def test_pinned_host_memory_needs_a_device():
+    """psi_host_alloc is page-locked memory from the CUDA driver: without a
+    device it fails loudly; freeing NULL is a no-op; solver info of no solver
+    is an argument error."""
+    p = C.c_void_p()
+    rc = lib.psi_host_alloc(64, C.byref(p))
+    if rc == PSI_OK:
+        lib.psi_host_free(p)
+        pytest.skip("a CUDA device is present")
+    assert rc == PSI_ERR_NO_DEVICE and not p.value
+    with pytest.raises(psi.PsiError):
+        psi.pinned(16)
+    lib.psi_host_free(None)
+    assert lib.psi_solver_info(None, None, None, None) == PSI_ERR_INVALID
+
+
 def test_invalid_options_rejected_before_device_use():
     g = psi.Game.random(100, 2, 4, 100, 1)
     for bad in (dict(sublist_len=1), dict(valuation_mode=7)):

@@ -88,6 +88,36 @@ def test_gpu_solver_from_host_csr_matches_game_handle():
     b.close()
 
 
+def test_gpu_solver_from_pinned_buffers_and_info():
+    """Upload from page-locked host buffers (psi_host_alloc) and read-back
+    into them give the same solve; psi_solver_info reports the device-side
+    shape (its largest priority is found on the device)."""
+    import ctypes as C
+    from psi._lib import lib
+    g = make("c4", 30000, 72)
+    csr = []
+    for a in g.csr():
+        h = psi.pinned(len(a))
+        h[:] = a
+        csr.append(h)
+    s = psi.GPUList.from_csr(*csr)
+    n, m, mp = C.c_int32(), C.c_int64(), C.c_int32()
+    assert lib.psi_solver_info(s._h, C.byref(n), C.byref(m), C.byref(mp)) == 0
+    assert (n.value, m.value, mp.value) == (g.n, g.m, int(g.csr()[1].max()))
+    assert s.max_pri == mp.value
+    ref = psi.GPUList(g)
+    assert s.solve() == ref.solve()
+    out = psi.pinned(g.n)
+    strat = s.get_strategy(out=out)
+    assert np.shares_memory(strat, out) and np.array_equal(strat, ref.get_strategy())
+    w0 = s.get_winning(0, out=psi.pinned(g.n))
+    assert np.array_equal(w0, ref.get_winning(0))
+    with pytest.raises(ValueError):
+        s.get_strategy(out=np.empty(3, np.int32))
+    s.close()
+    ref.close()
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("fam,n,seed,reset", [("c1", 10000, 81, False), ("c2", 200000, 82, False),
                                               ("c3", 50000, 83, False), ("smallpri", 30000, 84, False),
