@@ -56,7 +56,7 @@ def workload_config(n, m=None, seed=1):
         "l2": "inputs larger than L2 (game CSR + solver state ~1.3 GB at n=2^24), no flush",
         "parallelism": "replicas: one independent game per GPU",
         "evaluation": "incremental where few strategies changed (psi_options.incremental = auto: patches after "
-                      "steps that changed <= max(1024, n/1024) strategies, else the full Euler-tour evaluation); "
+                      "steps that changed <= max(1024, n/64) strategies, else the full Euler-tour evaluation); "
                       "results identical to full evaluations",
     }
     if m is not None:
@@ -570,7 +570,7 @@ def main():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--sublist-len", type=int, default=64)
     ap.add_argument("--patch-limit", type=int, default=0,
-                    help="psi_options.patch_limit (0: the library default, max(1024, n/1024))")
+                    help="psi_options.patch_limit (0: the library default, max(1024, n/64))")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--host-loop", action="store_true",
                     help="time the host-driven solve loop instead of the default one-graph solve")

@@ -97,13 +97,13 @@ typedef struct {
                                 strategy path passes through a changed one (the result is
                                 the same as a full evaluation's) */
     int32_t patch_limit;     /* PSI_INCR_AUTO: the most changed strategies after which a
-                                patch is tried (0, the default: max(1024, n/1024)) */
+                                patch is tried (0, the default: max(1024, n/64)) */
     int32_t reserved[1];
 } psi_options;
 
 /* incremental: PSI_INCR_AUTO (default) patches after steps that changed at
  * most patch_limit strategies, giving up for a full evaluation when more
- * than max(4096, n/8) vertices or 160 levels of descendants are affected;
+ * than max(4096, n/8) vertices or 256 levels of descendants are affected;
  * PSI_INCR_OFF evaluates in full every time; PSI_INCR_ALWAYS patches
  * whenever the previous evaluation's state allows it, without the size
  * limits (n extra entries of device memory per buffer; for tests). */

@@ -36,6 +36,7 @@ struct EvalGates {
     int32_t ccount = 0;      // changed vertices the switch steps listed since the last evaluation
     int32_t csnap = 0;       // ccount as the current evaluation found it
     int32_t acount = 0;      // vertices the current patch re-evaluates
+    int32_t nseeds = 0;      // of them the changed ones (alist[0, nseeds))
     int32_t lcnt[3] = {0, 0, 0};              // per-level append counters of the patch's search
     int32_t saved_full = 0, saved_incr = 0;   // tour gates while a patch holds them closed
     int32_t skip = 0, backoff = 1;            // evaluations not to try a patch after a failed one
@@ -217,7 +218,8 @@ struct PatchArgs {
     const uint8_t *solved = nullptr;
     int32_t *alist = nullptr;   // the vertices re-evaluated (acap entries)
     int32_t *apos = nullptr;    // per vertex: its position in alist, -1 if none (n entries, -1 between patches)
-    int4 *ja = nullptr, *jb = nullptr;   // pointer-jumping entries (acap each)
+    int4 *rel = nullptr;                 // per position of alist: seed, path summary to it (acap)
+    int4 *sja = nullptr, *sjb = nullptr; // pointer-jumping entries of the seeds (acap each)
     int32_t acap = 0, ccap = 0, max_levels = 0;
     int64_t ucap = 0;           // capacity of ulist
     int32_t *st = nullptr;

@@ -20,24 +20,30 @@
 //     permission (the tour and the list cover every change since the last
 //     evaluation) and room in the unreached list.
 //  2. k_patch_collect (cooperative) finds A level by level: the changed
-//     vertices, then the in-neighbours u with strat[u] == x of each vertex x
-//     found (reverse CSR), and so on.  Every vertex has one successor, so it
-//     is found once, by its own successor, with no atomics on the vertex; a
-//     warp spreads its vertices' in-edges over its lanes.  If A outgrows its
-//     buffer or the levels their cap, the patch gives up: the full
-//     evaluation's gates open instead, and the next few evaluations do not
-//     try (doubling each time).
-//  3. k_patch_values (cooperative) ranks A by pointer jumping, entries
-//     indexed by position in A: (next, steps, top priority, its count).  A
-//     successor outside A (the sink, a solved vertex, or any vertex whose
-//     path avoids the changes) is an exit with a known value.  After
-//     ceil(log2 |A|) + 1 rounds every entry has reached its exit or sits on
-//     a cycle inside A, whose top priority the window from a cycle vertex
-//     gives (as in the cycle pass).  A finite vertex gets depth = steps +
-//     depth(exit) and the merged path summary, the others the exit's or the
-//     cycle's infinity; the infinite ones are appended to the unreached list
-//     that mark_solved scans (an entry that has since become finite is
-//     skipped there, st being finite).
+//     vertices (the seeds, level 0), then the in-neighbours u with
+//     strat[u] == x of each vertex x found (reverse CSR), and so on.  Every
+//     vertex has one successor, so a vertex other than a seed is found once,
+//     by its own successor, with no atomics on the vertex; a warp spreads its
+//     vertices' in-edges over its lanes.  On the way down each vertex gets
+//     its seed and the summary of its path up to that seed (`rel`: seed
+//     index, vertices, top priority, its count), from its successor's.  If A
+//     outgrows its buffer or the levels their cap, the patch gives up: the
+//     full evaluation's gates open instead, and the next few evaluations do
+//     not try (doubling each time).
+//  3. k_patch_values (cooperative).  A cycle inside A passes through a seed
+//     (a cycle of unchanged vertices has no path to a changed one), so only
+//     the seeds need pointer jumping: a seed's successor is the sink, a
+//     vertex outside A (an exit with a known value: solved, or its path
+//     avoids the changes) or a vertex of A, which leads to its own seed by
+//     its rel summary.  After ceil(log2 seeds) + 1 rounds over (next seed,
+//     vertices, top priority, its count) every seed has reached its exit or
+//     sits on a cycle of seeds, whose top priority the window from a cycle
+//     seed gives (as in the cycle pass).  Then every vertex of A takes its
+//     seed's value merged with its rel summary, in one parallel pass: depth
+//     = its vertices + its seed's depth, or the seed's infinity.  The
+//     infinite ones are appended to the unreached list that mark_solved scans
+//     (an entry that has since become finite is skipped there, st being
+//     finite).
 #include <climits>
 #include <cooperative_groups.h>
 
@@ -97,18 +103,21 @@ __global__ void k_patch_begin(PatchArgs a)
     }
 }
 
-// Warp-collective: the in-edges of the lanes' vertices x (valid ones) laid
-// end to end over the warp's lanes, 32 per round; each lane tests its edge's
-// source u for being a child of its x outside A and appends it to alist at
-// position end + (its slot counted in *lcount).
-__device__ __forceinline__ void expand_children(const PatchArgs &a, bool valid, int32_t x, int32_t end,
+// Warp-collective: the in-edges of the lanes' vertices x (valid ones, at
+// positions i of alist) laid end to end over the warp's lanes, 32 per round;
+// each lane tests its edge's source u for being a child of its x outside A,
+// appends it to alist at position end + (its slot counted in *lcount) and
+// gives it x's seed with the path summary extended by u.
+__device__ __forceinline__ void expand_children(const PatchArgs &a, bool valid, int32_t x, int64_t i, int32_t end,
                                                 int32_t *lcount)
 {
     const int lane = threadIdx.x & 31;
     int32_t b = 0, d = 0;
+    int4 r = make_int4(0, 0, -1, 0);
     if (valid) {
         b = a.rev_off[x];
         d = a.rev_off[x + 1] - b;
+        r = a.rel[i];
     }
     int32_t incl = d;
 #pragma unroll
@@ -128,16 +137,25 @@ __device__ __forceinline__ void expand_children(const PatchArgs &a, bool valid, 
         }
         const int32_t bl = __shfl_sync(kAll, b, l), el = __shfl_sync(kAll, incl - d, l),
                       xl = __shfl_sync(kAll, x, l);
-        int32_t u = -1;
+        int4 rl;
+        rl.x = __shfl_sync(kAll, r.x, l);
+        rl.y = __shfl_sync(kAll, r.y, l);
+        rl.z = __shfl_sync(kAll, r.z, l);
+        rl.w = __shfl_sync(kAll, r.w, l);
+        int32_t u = -1, pu = 0;
         bool child = false;
         if (j < total) {
             u = a.rev_src[bl + (j - el)];
             child = a.strat[u] == xl && !a.solved[u] && a.apos[u] == -1;
+            pu = a.pri[u];
         }
         const int32_t p = warp_reserve(child, lcount, end);
         if (child && p < a.acap) {
             a.alist[p] = u;
             a.apos[u] = p;
+            int32_t m = pu, c = 1;
+            top1_merge(m, c, rl.z, rl.w);
+            a.rel[p] = make_int4(rl.x, rl.y + 1, m, c);
         }
     }
 }
@@ -167,6 +185,7 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_collect(PatchArgs a)
             if (p < a.acap) {
                 a.alist[p] = v;
                 a.apos[v] = p;
+                a.rel[p] = make_int4(p, 0, -1, 0);   // its own seed, empty path above it
             } else {
                 a.apos[v] = -1;
             }
@@ -178,6 +197,7 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_collect(PatchArgs a)
     // counter is read right after the barrier that ends its level and reset
     // two levels later, when every thread has read it.
     int32_t lo = 0, end = *(volatile int32_t *)&g->lcnt[0];
+    const int32_t nseeds = end;
     bool bail = false;
     for (int32_t level = 1;; level++) {
         if (end > a.acap) {
@@ -191,10 +211,14 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_collect(PatchArgs a)
         }
         int32_t *lcount = &g->lcnt[level % 3];
         if (leader) g->lcnt[(level + 1) % 3] = 0;
-        for (int64_t i0 = lo + gw * 32; i0 < end; i0 += nw * 32) {
+        // vertices per warp: as few as the frontier allows (one when it fits
+        // the grid), so a warp's in-edges take one round of dependent loads
+        const int64_t f = end - lo;
+        const int64_t k = f >= nw * 32 ? 32 : (f + nw - 1) / nw;
+        for (int64_t i0 = lo + gw * k; i0 < end; i0 += nw * k) {
             const int64_t i = i0 + lane;
-            const bool valid = i < end;
-            expand_children(a, valid, valid ? a.alist[i] : 0, end, lcount);
+            const bool valid = lane < k && i < end;
+            expand_children(a, valid, valid ? a.alist[i] : 0, i, end, lcount);
         }
         grid.sync();
         lo = end;
@@ -202,7 +226,10 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_collect(PatchArgs a)
     }
 
     if (!bail) {
-        if (leader) g->acount = end;
+        if (leader) {
+            g->acount = end;
+            g->nseeds = nseeds;
+        }
         return;
     }
     // give up: A's marks cleared, the full evaluation's gates opened
@@ -227,74 +254,90 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_values(PatchArgs a)
     EvalGates *g = a.g;
     if (!g->patch) return;
     cg::grid_group grid = cg::this_grid();
-    const int32_t na = g->acount;
+    const int32_t na = g->acount, ns = g->nseeds;   // the seeds are alist[0, ns)
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nth = (int64_t)gridDim.x * blockDim.x;
 
-    // entries: next = position in A of the successor, -1 the sink, -2 - t an
-    // exit at vertex t outside A; steps, (top priority, count) of the segment
-    for (int64_t i = tid; i < na; i += nth) {
-        const int32_t v = a.alist[i], t = a.strat[v];
-        int32_t nx = -1;
+    // seed entries: next = the seed its successor leads to, -1 the sink, -2 - t
+    // an exit at vertex t outside A; vertices, (top priority, count) of the
+    // segment from the seed to there
+    for (int64_t s = tid; s < ns; s += nth) {
+        const int32_t v = a.alist[s], t = a.strat[v];
+        int4 e = make_int4(-1, 1, a.pri[v], 1);
         if (t >= 0) {
             const int32_t p = a.apos[t];
-            nx = p >= 0 ? p : -2 - t;
+            if (p < 0) {
+                e.x = -2 - t;
+            } else {
+                const int4 r = a.rel[p];
+                e.x = r.x;
+                e.y += r.y;
+                top1_merge(e.z, e.w, r.z, r.w);
+            }
         }
-        a.ja[i] = make_int4(nx, 1, a.pri[v], 1);
+        a.sja[s] = e;
     }
-    int4 *in = a.ja, *out = a.jb;
-    const int rounds = na > 0 ? ceil_log2_i(na) + 1 : 0;
+    int4 *in = a.sja, *out = a.sjb;
+    const int rounds = ns > 0 ? ceil_log2_i(ns) + 1 : 0;
     for (int r = 0; r < rounds; r++) {
         grid.sync();
-        for (int64_t i = tid; i < na; i += nth) {
-            int4 e = in[i];
+        for (int64_t s = tid; s < ns; s += nth) {
+            int4 e = in[s];
             if (e.x >= 0) {
                 const int4 f = in[e.x];
                 e.x = f.x;
                 e.y += f.y;
                 top1_merge(e.z, e.w, f.z, f.w);
             }
-            out[i] = e;
+            out[s] = e;
         }
         int4 *t = in;
         in = out;
         out = t;
     }
     grid.sync();
+    // seed values, into `out` (free now): (status or depth, top priority, count, 0)
+    for (int64_t s = tid; s < ns; s += nth) {
+        const int4 e = in[s];
+        int4 val = make_int4(e.y, e.z, e.w, 0);                      // reaches the sink
+        if (e.x >= 0) {
+            val.x = (in[e.x].z % 2 == 0) ? ST_POS_INF : ST_NEG_INF;   // on or into a cycle of seeds
+        } else if (e.x <= -2) {
+            const int32_t t = -2 - e.x;                               // exit outside A: its value is current
+            const int32_t st = a.st[t];
+            if (st >= 1) {
+                const PathNode q = a.node[t];
+                val.x += st;
+                top1_merge(val.y, val.z, q.rmax, q.rcnt);
+            } else {
+                val.x = st;
+            }
+        }
+        out[s] = val;
+    }
+    grid.sync();
 
-    // results, in block-uniform passes (flag_in_neighbours and block_append
-    // need every thread of the block)
+    // every vertex of A: its seed's value merged with its rel summary, in
+    // block-uniform passes (flag_in_neighbours and block_append need every
+    // thread of the block)
     for (int64_t b0 = tid - threadIdx.x; b0 < na; b0 += nth) {
         const int64_t i = b0 + threadIdx.x;
         int32_t v = -1;
         bool changed = false, unreached = false;
         if (i < na) {
             v = a.alist[i];
-            const int4 e = in[i];
-            int32_t m = e.z, c = e.w, depth = e.y, s = ST_UNRESOLVED;
-            bool fin = false;
-            if (e.x >= 0) {
-                s = (in[e.x].z % 2 == 0) ? ST_POS_INF : ST_NEG_INF;   // on or into a cycle inside A
-            } else if (e.x == -1) {
-                fin = true;                                          // reaches the sink
-            } else {
-                const int32_t t = -2 - e.x;                          // exit outside A: its value is current
-                s = a.st[t];
-                if (s >= 1) {
-                    const PathNode q = a.node[t];
-                    depth += s;
-                    top1_merge(m, c, q.rmax, q.rcnt);
-                    fin = true;
-                }
-            }
+            const int4 r = a.rel[i];
+            const int4 sv = out[r.x];
             int32_t k;
-            if (fin) {
-                a.st[v] = depth;
+            if (sv.x >= 1) {
+                int32_t m = r.z, c = r.w;
+                top1_merge(m, c, sv.y, sv.z);
+                a.st[v] = r.y + sv.x;
                 a.node[v] = PathNode{a.strat[v], a.pri[v], m, c};
                 k = finite_key(m, c);
             } else {
-                a.st[v] = s;
-                k = (s == ST_POS_INF) ? KEY_POS_INF : KEY_NEG_INF;
+                a.st[v] = sv.x;
+                k = (sv.x == ST_POS_INF) ? KEY_POS_INF : KEY_NEG_INF;
                 unreached = true;
             }
             if (a.key && a.key[v] != k) {

@@ -202,11 +202,11 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
     // evaluation), re-evaluated set capacity, level cap of its search
     if (incremental_ != PSI_INCR_OFF) {
         const bool always = incremental_ == PSI_INCR_ALWAYS;
-        const int64_t cc = always ? cap_n : patch_limit_ > 0 ? patch_limit_ : std::max<int64_t>(1024, cap_n >> 10);
+        const int64_t cc = always ? cap_n : patch_limit_ > 0 ? patch_limit_ : std::max<int64_t>(1024, cap_n >> 6);
         const int64_t ac = always ? cap_n : std::max<int64_t>(4096, cap_n >> 3);
         ccap_ = (int32_t)std::max<int64_t>(1, std::min(cc, cap_n));
         acap_ = (int32_t)std::max<int64_t>(1, std::min(ac, cap_n));
-        max_levels_ = always ? INT32_MAX : 160;
+        max_levels_ = always ? INT32_MAX : 256;
     }
     ucap_ = cap_n + acap_;
     PSI_CUDA_TRY(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
@@ -258,7 +258,7 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
             {(void **)&clist_, 4 * (size_t)ccap_},
             {(void **)&alist_, 4 * (size_t)acap_},
             {(void **)&apos_, 4 * (size_t)std::max<int64_t>(1, cap_n)},
-            {(void **)&pj_, 2 * sizeof(int4) * (size_t)acap_},
+            {(void **)&pj_, 3 * sizeof(int4) * (size_t)acap_},
         };
         for (const auto &a : patch) {
             cudaError_t e = device_alloc(a.ptr, a.bytes, stream_);
@@ -467,8 +467,9 @@ PatchArgs Solver::patch_args()
     a.solved = solved_;
     a.alist = alist_;
     a.apos = apos_;
-    a.ja = pj_;
-    a.jb = pj_ ? pj_ + acap_ : nullptr;
+    a.rel = pj_;
+    a.sja = pj_ ? pj_ + acap_ : nullptr;
+    a.sjb = pj_ ? pj_ + 2 * (size_t)acap_ : nullptr;
     a.acap = acap_;
     a.ccap = ccap_;
     a.max_levels = max_levels_;
@@ -484,15 +485,18 @@ PatchArgs Solver::patch_args()
 
 int Solver::enqueue_eval(bool timed)
 {
-    auto begin = [&](Phase p) {
-        if (timed) phase_begin(p);
-    };
-    auto end = [&](Phase p) {
-        if (timed) phase_end(p);
-    };
-    // 0. a patch, when the gates allow it and it succeeds; otherwise its
-    //    kernels return at once and the full evaluation's gates are open
-    begin(PH_PATCH);
+    int rc = enqueue_patch(timed);
+    if (!rc) rc = enqueue_full(timed);
+    if (rc) return rc;
+    PSI_CUDA_TRY(cudaMemsetAsync(&ctl_->quiet, 0, sizeof(int32_t), stream_));
+    return PSI_OK;
+}
+
+// 0. a patch, when the gates allow it and it succeeds; otherwise its
+//    kernels return at once and the full evaluation's gates are open
+int Solver::enqueue_patch(bool timed)
+{
+    if (timed) phase_begin(PH_PATCH);
     const PatchArgs pa = patch_args();
     launch_patch_begin(stream_, pa);
     if (incremental_ != PSI_INCR_OFF) {
@@ -500,7 +504,19 @@ int Solver::enqueue_eval(bool timed)
         if (!pe) pe = launch_patch_values(stream_, pa);
         if (pe) return fail(PSI_ERR_CUDA, std::string("patch kernels: ") + cudaGetErrorString((cudaError_t)pe));
     }
-    end(PH_PATCH);
+    if (timed) phase_end(PH_PATCH);
+    return PSI_OK;
+}
+
+// The full evaluation, every kernel gated (ctl_->full / incr / eval).
+int Solver::enqueue_full(bool timed)
+{
+    auto begin = [&](Phase p) {
+        if (timed) phase_begin(p);
+    };
+    auto end = [&](Phase p) {
+        if (timed) phase_end(p);
+    };
     // 1. Euler tour of the sink tree: built afresh (gate full) or the previous
     //    one relinked where strategies or solved flags changed (gate incr);
     //    jA_ is free until the cycle pass: it holds the list of dirty parents
@@ -534,7 +550,6 @@ int Solver::enqueue_eval(bool timed)
     ce = launch_cycles(stream_, &dw_->ucount, ulist_, strat_, pri_, solved_, st_, key_, jA_, jB_, la, lb, dw_->cnt,
                        &dw_->err, track(), &ctl_->eval);
     if (ce) return fail(PSI_ERR_CUDA, std::string("cycle kernel: ") + cudaGetErrorString((cudaError_t)ce));
-    PSI_CUDA_TRY(cudaMemsetAsync(&ctl_->quiet, 0, sizeof(int32_t), stream_));
     end(PH_CYCLES);
     return PSI_OK;
 }

@@ -130,11 +130,14 @@ private:
     int init_arena(int32_t slots);
     void set_extent(int32_t n);
     int sync_and_check(const char *what);
-    int enqueue_step(cudaGraphConditionalHandle loop, bool reset);
+    // One SI step captured into the loop body of the solve graph.
+    int enqueue_step(cudaGraph_t body, cudaGraphConditionalHandle loop, bool reset);
     // One evaluation on the stream, no synchronisation: the patch kernels and
     // the full evaluation's, each set gated (which ones work is decided on
     // the device, k_patch_begin).
     int enqueue_eval(bool timed);
+    int enqueue_patch(bool timed);
+    int enqueue_full(bool timed);
     PatchArgs patch_args();
     ChangeList changes() const { return clist_ ? ChangeList{clist_, &ctl_->ccount, ccap_} : ChangeList(); }
     int build_graph(bool reset);
@@ -211,6 +214,7 @@ private:
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t graph_exec_ = nullptr;
     long long graph_step_launches_ = 0;   // kernels per loop pass (for the launch counter)
+    long long graph_full_launches_ = 0;   // of them in the full evaluation's conditional node
     std::vector<void *> allocs_;
 };
 

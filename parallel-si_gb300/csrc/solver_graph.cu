@@ -11,6 +11,7 @@
 // launch and one synchronisation.  The kernels are the same as the host
 // loop's; gated ones return at once when their gate word is 0.
 #include <string>
+#include <vector>
 
 #include "device_common.cuh"
 #include "kernels.h"
@@ -70,19 +71,65 @@ constexpr int32_t kEvalGuard = 1 << 20;
 
 }  // namespace
 
-// One SI step on the stream, no synchronisation (captured into the loop body).
-int Solver::enqueue_step(cudaGraphConditionalHandle loop, bool reset)
+// Opens the full evaluation's conditional node iff this evaluation is not a
+// patch (its gate word was set by k_patch_begin / k_patch_collect).
+__global__ void k_eval_cond(const GraphCtl *c, cudaGraphConditionalHandle h) { cudaGraphSetConditional(h, c->eval ? 1 : 0); }
+
+// One SI step captured into the loop body `body`, in three pieces: (A) Odd's
+// reset and the patch kernels, then a kernel that sets the condition of (B),
+// a conditional "if" node holding the full evaluation, so that a patched
+// evaluation launches none of its kernels; (C) the rest of the step.
+int Solver::enqueue_step(cudaGraph_t body, cudaGraphConditionalHandle loop, bool reset)
 {
+    const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+    cudaGraphConditionalHandle evalc;
+    PSI_CUDA_TRY(cudaGraphConditionalHandleCreate(&evalc, body, 1, 0));
+    auto abort_capture = [&](int rc) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(stream_, &g);
+        return rc;
+    };
+
+    // (A)
+    PSI_CUDA_TRY(cudaStreamBeginCaptureToGraph(stream_, body, nullptr, nullptr, 0, mode));
     launch_reset_odd(stream_, n_, owner_, off_, tgt_, strat_, &ctl_->reset, need_);
-    // evaluation (as compute_valuation: a patch or the full evaluation, gated)
-    int rc = enqueue_eval(false);
-    if (rc) return rc;
+    int rc = enqueue_patch(false);
+    if (rc) return abort_capture(rc);
+    count_launch();
+    k_eval_cond<<<1, 1, 0, stream_>>>(ctl_, evalc);
+    cudaStreamCaptureStatus status;
+    const cudaGraphNode_t *deps = nullptr;
+    size_t ndeps = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(stream_, &status, nullptr, nullptr, &deps, nullptr, &ndeps);
+    if (e != cudaSuccess) return abort_capture(fail(PSI_ERR_CUDA, std::string("capture info: ") + cudaGetErrorString(e)));
+    std::vector<cudaGraphNode_t> tail(deps, deps + ndeps);
+    cudaGraph_t g = nullptr;
+    PSI_CUDA_TRY(cudaStreamEndCapture(stream_, &g));
+
+    // (B) the full evaluation (as compute_valuation), inside the "if" node
+    cudaGraphNodeParams ip = {};
+    ip.type = cudaGraphNodeTypeConditional;
+    ip.conditional.handle = evalc;
+    ip.conditional.type = cudaGraphCondTypeIf;
+    ip.conditional.size = 1;
+    cudaGraphNode_t ifnode;
+    PSI_CUDA_TRY(cudaGraphAddNode(&ifnode, body, tail.data(), nullptr, tail.size(), &ip));
+    PSI_CUDA_TRY(cudaStreamBeginCaptureToGraph(stream_, ip.conditional.phGraph_out[0], nullptr, nullptr, 0, mode));
+    const long long full_before = launch_count();
+    rc = enqueue_full(false);
+    graph_full_launches_ = launch_count() - full_before;
+    if (rc) return abort_capture(rc);
+    PSI_CUDA_TRY(cudaStreamEndCapture(stream_, &g));
+
+    // (C)
+    PSI_CUDA_TRY(cudaStreamBeginCaptureToGraph(stream_, body, &ifnode, nullptr, 1, mode));
     count_launch();
     k_ctl_evaluated<<<1, 1, 0, stream_>>>(ctl_);
     // Odd: mark_solved(1), switch(1)
     launch_mark_solved(stream_, &dw_->ucount, ulist_, 1, st_, solved_, dirty_, nullptr, nullptr, nullptr,
                        &ctl_->mfrom[1], &ctl_->mdone);
-    PSI_CUDA_TRY(cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_));
+    e = cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_);
+    if (e != cudaSuccess) return abort_capture(fail(PSI_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e)));
     int32_t *todo = reinterpret_cast<int32_t *>(jB_);   // free until the next cycle pass
     launch_switch(stream_, np_ - np0_, plist_ + np0_, 1, off_, tgt_, strat_, st_, key_, node_, dw_->sw, nullptr,
                   nullptr, nullptr, dirty_, &dw_->err, nullptr, need_, todo, &dw_->cnt[2], changes());
@@ -91,12 +138,15 @@ int Solver::enqueue_step(cudaGraphConditionalHandle loop, bool reset)
     // Even, when Odd made no strict improvement: mark_solved(0), switch(0)
     launch_mark_solved(stream_, &dw_->ucount, ulist_, 0, st_, solved_, dirty_, nullptr, nullptr, &ctl_->even,
                        &ctl_->mfrom[0], &ctl_->mdone);
-    PSI_CUDA_TRY(cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_));
+    e = cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_);
+    if (e != cudaSuccess) return abort_capture(fail(PSI_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e)));
     launch_switch(stream_, np0_, plist_, 0, off_, tgt_, strat_, st_, key_, node_, dw_->sw, nullptr, nullptr, nullptr,
                   dirty_, &dw_->err, &ctl_->even, need_, todo, &dw_->cnt[2], changes());
     count_launch();
     k_ctl_even<<<1, 1, 0, stream_>>>(ctl_, dw_->sw, loop, reset ? 1 : 0, kEvalGuard);
-    PSI_CUDA_TRY(cudaGetLastError());
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return abort_capture(fail(PSI_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString(e)));
+    PSI_CUDA_TRY(cudaStreamEndCapture(stream_, &g));
     return PSI_OK;
 }
 
@@ -121,14 +171,10 @@ int Solver::build_graph(bool reset)
     cudaGraphNode_t node;
     PSI_CUDA_TRY(cudaGraphAddNode(&node, graph_, nullptr, nullptr, 0, &cp));
     cudaGraph_t body = cp.conditional.phGraph_out[0];
-    PSI_CUDA_TRY(cudaStreamBeginCaptureToGraph(stream_, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
     const long long before = launch_count();
-    int rc = enqueue_step(loop, reset);
+    int rc = enqueue_step(body, loop, reset);
     graph_step_launches_ = launch_count() - before;
-    cudaGraph_t captured = nullptr;
-    cudaError_t e = cudaStreamEndCapture(stream_, &captured);
     if (rc) return rc;
-    if (e != cudaSuccess) return fail(PSI_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
     PSI_CUDA_TRY(cudaGraphInstantiate(&graph_exec_, graph_, 0));
     graph_reset_ = reset;
     return PSI_OK;
@@ -139,6 +185,7 @@ int Solver::solve_graph(int32_t reset, int32_t *iters, int32_t *brs, int64_t max
 {
     int rc = init_strat();
     if (rc) return rc;
+    const unsigned long long patches_before = hw_->patch[0];   // as of init_strat's synchronisation
     if (!graph_exec_ || graph_reset_ != (reset != 0)) {
         rc = build_graph(reset != 0);
         if (rc) return rc;
@@ -156,7 +203,11 @@ int Solver::solve_graph(int32_t reset, int32_t *iters, int32_t *brs, int64_t max
     if (rc) return rc;
     *iters = out.iters;
     *brs = out.brs;
-    add_launches(graph_step_launches_ * out.brs);   // every pass launches each kernel of the body once
+    // every pass launches each kernel of the body once, those of the full
+    // evaluation only when it is not a patch
+    const long long patched = (long long)(hw_->patch[0] - patches_before);
+    add_launches((graph_step_launches_ - graph_full_launches_) * out.brs +
+                 graph_full_launches_ * (out.brs - patched));
     times_.evals += out.brs;
     times_.switches += out.brs + out.iters;
     val_ready_ = true;

@@ -74,7 +74,7 @@ def hanging_chain(length):
 @pytest.mark.parametrize("mode", [AUTO, ALWAYS])
 def test_deep_affected_trees_match_oracle(mode):
     """1000 levels below the changed vertices: the automatic policy's level
-    cap (160) makes the patch give up and the full evaluation run; without
+    cap (256) makes the patch give up and the full evaluation run; without
     the cap the patch walks them all.  Every state matches the oracle."""
     g = hanging_chain(1000)
     gpu = psi.GPUList(g, incremental=mode)
