@@ -65,20 +65,22 @@ __host__ __device__ __forceinline__ int key_infinite(int32_t k)
 }
 
 // Change tracking (kernels.h: ChangeTrack), warp-collective: every lane of a
-// converged warp calls it, and the in-neighbours of each lane's vertex v with
-// `changed` set get need = 1.  The in-edges of the changed lanes are spread
-// over the warp's lanes (their rev_off spans laid end to end), so one round of
-// rev_src loads usually covers them all, instead of one dependent load per
-// in-edge on the changed lanes while the rest of the warp waits.
-__device__ __forceinline__ void flag_in_neighbours(const ChangeTrack &t, bool changed, int32_t v)
+// converged warp calls it.  mode 2 (a changed key): every in-neighbour of the
+// lane's vertex v gets need = 1; mode 1 (v re-evaluated, key unchanged):
+// those with tie set; 0: none.  The in-edges of the lanes with a mode are
+// spread over the warp's lanes (their rev_off spans laid end to end), so one
+// round of rev_src loads usually covers them all, instead of one dependent
+// load per in-edge on those lanes while the rest of the warp waits.
+__device__ __forceinline__ void flag_in_neighbours(const ChangeTrack &t, int mode, int32_t v)
 {
     if (!t.need || (t.quiet && *t.quiet)) return;
+    if (!t.tie && mode == 1) mode = 0;
     constexpr unsigned kAll = 0xffffffffu;
-    const unsigned lanes = __ballot_sync(kAll, changed);
+    const unsigned lanes = __ballot_sync(kAll, mode != 0);
     if (!lanes) return;
     const int lane = threadIdx.x & 31;
     int32_t b = 0, d = 0;
-    if (changed) {
+    if (mode) {
         b = t.rev_off[v];
         d = t.rev_off[v + 1] - b;
     }
@@ -92,13 +94,25 @@ __device__ __forceinline__ void flag_in_neighbours(const ChangeTrack &t, bool ch
     for (int64_t j0 = 0; j0 < total; j0 += 32) {
         const int64_t j = j0 + lane;
         int64_t e = -1;
+        int all = 0;
         for (unsigned s = lanes; s; s &= s - 1) {
             const int l = __ffs(s) - 1;
             const int32_t el = __shfl_sync(kAll, excl, l), dl = __shfl_sync(kAll, d, l), bl = __shfl_sync(kAll, b, l);
-            if (j >= el && j < (int64_t)el + dl) e = bl + (j - el);
+            const int ml = __shfl_sync(kAll, mode, l);
+            if (j >= el && j < (int64_t)el + dl) {
+                e = bl + (j - el);
+                all = ml == 2;
+            }
         }
-        if (e >= 0) t.need[t.rev_src[e]] = 1;
+        if (e >= 0) {
+            const int32_t u = t.rev_src[e];
+            if (all || t.tie[u]) t.need[u] = 1;
+        }
     }
+}
+__device__ __forceinline__ void flag_in_neighbours(const ChangeTrack &t, bool changed, int32_t v)
+{
+    flag_in_neighbours(t, changed ? 2 : 0, v);
 }
 
 // (max, count of max) of the union of two priority multisets

@@ -87,7 +87,8 @@ __global__ void k_reset_odd(int32_t n, const int8_t *__restrict__ owner, const i
 // parent links (solved, or child of a solved vertex) points back at its up
 // node.  The sink's down node ends the list.
 __global__ void k_tour_init(int32_t n, int32_t *__restrict__ succ, int2 *__restrict__ vloc,
-                            uint8_t *__restrict__ dirty, const int32_t *__restrict__ gate)
+                            uint8_t *__restrict__ dirty, const int32_t *__restrict__ gate,
+                            const uint8_t *__restrict__ tie, uint8_t *__restrict__ need)
 {
     if (gate && !*gate) return;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -96,6 +97,7 @@ __global__ void k_tour_init(int32_t n, int32_t *__restrict__ succ, int2 *__restr
         if (i < n) {
             vloc[i] = make_int2(-1, 0);
             dirty[i] = 0;   // a full build leaves nothing to relink
+            if (tie && tie[i]) need[i] = 1;
         }
     }
 }
@@ -144,14 +146,18 @@ __global__ void k_tour_link(int32_t n, const int32_t *__restrict__ strat, const 
 // are still exact.  The dirty parents are compacted first (k_dirty_list, which
 // also clears the flags), so the relinking threads are all busy.
 __global__ void k_dirty_list(int32_t n, uint8_t *__restrict__ dirty, int32_t *__restrict__ list,
-                             int32_t *__restrict__ count, int2 *__restrict__ vloc, const int32_t *__restrict__ gate)
+                             int32_t *__restrict__ count, int2 *__restrict__ vloc, const int32_t *__restrict__ gate,
+                             const uint8_t *__restrict__ tie, uint8_t *__restrict__ need)
 {
     if (gate && !*gate) return;
     for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < n; b0 += (int64_t)gridDim.x * blockDim.x) {
         const int32_t p = (int32_t)(b0 + threadIdx.x);
         const bool take = p < n && dirty[p];
         if (take) dirty[p] = 0;
-        if (p < n) vloc[p] = make_int2(-1, -1);   // on no walked sublist until the walk reaches it
+        if (p < n) {
+            vloc[p] = make_int2(-1, -1);   // on no walked sublist until the walk reaches it
+            if (tie && tie[p]) need[p] = 1;
+        }
         block_append(take, p, list, count);
     }
 }
@@ -591,10 +597,11 @@ void launch_reset_odd(cudaStream_t s, int32_t n, const int8_t *owner, const int3
 
 void launch_tour_build(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
                        const int32_t *rev_off, const int32_t *rev_src, int32_t *succ, int2 *vloc,
-                       int32_t *sinklist, int32_t *sinkcount, uint8_t *dirty, const int32_t *gate)
+                       int32_t *sinklist, int32_t *sinkcount, uint8_t *dirty, const int32_t *gate,
+                       const uint8_t *tie, uint8_t *need)
 {
     count_launch();
-    k_tour_init<<<capped_grid((int64_t)n + 1), kBlock, 0, s>>>(n, succ, vloc, dirty, gate);
+    k_tour_init<<<capped_grid((int64_t)n + 1), kBlock, 0, s>>>(n, succ, vloc, dirty, gate, tie, need);
     count_launch();
     k_tour_link<<<capped_grid(n), kBlock, 0, s>>>(n, strat, solved, rev_off, rev_src, succ, sinklist, sinkcount,
                                                   gate);
@@ -606,12 +613,12 @@ void launch_tour_build(cudaStream_t s, int32_t n, const int32_t *strat, const ui
 int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
                        const int32_t *rev_off, const int32_t *rev_src, uint8_t *dirty, int32_t *succ, int2 *vloc,
                        int32_t *sinklist, int32_t *sinkcount, int32_t *dlist, int32_t *dcount,
-                       const int32_t *gate)
+                       const int32_t *gate, const uint8_t *tie, uint8_t *need)
 {
     cudaError_t e = cudaMemsetAsync(dcount, 0, sizeof(int32_t), s);
     if (e != cudaSuccess) return (int)e;
     count_launch();
-    k_dirty_list<<<capped_grid(n), kBlock, 0, s>>>(n, dirty, dlist, dcount, vloc, gate);
+    k_dirty_list<<<capped_grid(n), kBlock, 0, s>>>(n, dirty, dlist, dcount, vloc, gate, tie, need);
     count_launch();
     unsigned g = grid_for(n);
     g = g < 1216u ? g : 1216u;

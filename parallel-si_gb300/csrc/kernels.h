@@ -18,10 +18,19 @@ struct PathNode;   // device_common.cuh
 // vertex keeps need = 1 (switch_kernels.cu).  need == nullptr: no tracking.
 // quiet (a device word, optional): while nonzero every need flag is already
 // set, and changed keys flag nothing (the first evaluation after a reset).
+// tie (optional): vertices whose last switch examination rested on a walk
+// (equal keys at their best successor).  Such a vertex needs another look
+// when the exact value of a successor may have changed: after every full
+// evaluation (need |= tie), and after a patch that re-evaluated one of its
+// successors, even with its key unchanged.  watch marks the vertices some
+// tied vertex rests on (set by the switch, cleared with the tracking), so a
+// patch looks for tied in-neighbours of those only.
 struct ChangeTrack {
     uint8_t *need = nullptr;
     const int32_t *rev_off = nullptr, *rev_src = nullptr;
     const int32_t *quiet = nullptr;
+    const uint8_t *tie = nullptr;
+    const uint8_t *watch = nullptr;
 };
 
 // Device words deciding which kernels of an evaluation do work (their gates;
@@ -101,15 +110,17 @@ void launch_reset_odd(cudaStream_t s, int32_t n, const int8_t *owner, const int3
 // n entries.
 void launch_tour_build(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
                        const int32_t *rev_off, const int32_t *rev_src, int32_t *succ, int2 *vloc,
-                       int32_t *sinklist, int32_t *sinkcount, uint8_t *dirty, const int32_t *gate = nullptr);
+                       int32_t *sinklist, int32_t *sinkcount, uint8_t *dirty, const int32_t *gate = nullptr,
+                       const uint8_t *tie = nullptr, uint8_t *need = nullptr);
 // The same tour brought up to date from the previous one: only the parents
 // flagged in dirty (cleared here; dlist: n entries of scratch, dcount: one
 // counter) are relinked and the sink's list is rebuilt.  Returns a
-// cudaError_t value.
+// cudaError_t value.  Both set need[v] wherever tie[v] is set (a full
+// evaluation: ChangeTrack), when tie is given.
 int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
                        const int32_t *rev_off, const int32_t *rev_src, uint8_t *dirty, int32_t *succ, int2 *vloc,
                        int32_t *sinklist, int32_t *sinkcount, int32_t *dlist, int32_t *dcount,
-                       const int32_t *gate = nullptr);
+                       const int32_t *gate = nullptr, const uint8_t *tie = nullptr, uint8_t *need = nullptr);
 // Sublist walks; heads are the nodes j*stride (j < nsub-1) and the list start.
 void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, int32_t stride, const int32_t *succ,
                           int2 *vloc, int2 *red, uint32_t *err, const int32_t *gate = nullptr);
@@ -163,7 +174,8 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
                    const int32_t *key, const PathNode *node, unsigned long long *stats, const int32_t *game_of,
                    unsigned long long *gcount, const int32_t *gmask, uint8_t *dirty, uint32_t *err,
                    const int32_t *gate = nullptr, uint8_t *need = nullptr, int32_t *list = nullptr,
-                   int32_t *list_count = nullptr, ChangeList changes = ChangeList());
+                   int32_t *list_count = nullptr, ChangeList changes = ChangeList(), uint8_t *tie = nullptr,
+                   uint8_t *watch = nullptr);
 // ---- batches: per-game accounting of solve_si (state[g] = brs, iters,
 // odd_done, done; gcount[g] = strict improvements of the last switch step)
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state,

@@ -324,6 +324,7 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_values(PatchArgs a)
         const int64_t i = b0 + threadIdx.x;
         int32_t v = -1;
         bool changed = false, unreached = false;
+        int mode = 0;
         if (i < na) {
             v = a.alist[i];
             const int4 r = a.rel[i];
@@ -344,9 +345,11 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_values(PatchArgs a)
                 a.key[v] = k;
                 changed = true;
             }
+            // re-evaluated: a tied in-neighbour looks again even at an unchanged key
+            mode = changed ? 2 : (a.track.watch && a.track.watch[v] ? 1 : 0);
             a.apos[v] = -1;
         }
-        flag_in_neighbours(a.track, changed, v);
+        flag_in_neighbours(a.track, mode, v);
         block_append(unreached, v, a.ulist, a.ucount);
     }
     if (tid == 0) {

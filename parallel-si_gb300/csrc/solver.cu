@@ -235,6 +235,8 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
         {(void **)&succ_, 4 * (size_t)capL},
         {(void **)&dirty_, (size_t)cap_n},
         {(void **)&need_, (size_t)cap_n},
+        {(void **)&tie_, (size_t)cap_n},
+        {(void **)&watch_, (size_t)cap_n},
         {(void **)&ulist_, 4 * (size_t)ucap_},
         {(void **)&vloc_, 8 * (size_t)cap_n},
         {(void **)&redA_, 8 * (size_t)cap_sub},
@@ -424,6 +426,8 @@ void Solver::reset_tracking()
 {
     static const int32_t one = 1;
     cudaMemsetAsync(need_, 1, (size_t)n_, stream_);
+    cudaMemsetAsync(tie_, 0, (size_t)n_, stream_);
+    cudaMemsetAsync(watch_, 0, (size_t)n_, stream_);
     cudaMemcpyAsync(&ctl_->quiet, &one, sizeof one, cudaMemcpyHostToDevice, stream_);
 }
 
@@ -522,9 +526,10 @@ int Solver::enqueue_full(bool timed)
     //    jA_ is free until the cycle pass: it holds the list of dirty parents
     begin(PH_TOUR);
     launch_tour_build(stream_, n_, strat_, solved_, rev_off_, rev_src_, succ_, vloc_, ulist_, &dw_->sinkcount, dirty_,
-                      &ctl_->full);
+                      &ctl_->full, tie_, need_);
     int ce = launch_tour_update(stream_, n_, strat_, solved_, rev_off_, rev_src_, dirty_, succ_, vloc_, ulist_,
-                                &dw_->sinkcount, reinterpret_cast<int32_t *>(jA_), &dw_->cnt[0], &ctl_->incr);
+                                &dw_->sinkcount, reinterpret_cast<int32_t *>(jA_), &dw_->cnt[0], &ctl_->incr, tie_,
+                                need_);
     if (ce) return fail(PSI_ERR_CUDA, std::string("tour update: ") + cudaGetErrorString((cudaError_t)ce));
     end(PH_TOUR);
     // 2. Helman-JaJa sublists, then the reduced list ranked on the device
@@ -607,7 +612,7 @@ int Solver::switch_strategy(int32_t player, int64_t *switched)
     const int32_t *pl = plist_ + (player == 0 ? 0 : np0_);
     // jB_ is free until the next cycle pass: it holds the list of vertices to examine
     launch_switch(stream_, np, pl, player, off_, tgt_, strat_, st_, key_, node_, dw_->sw, game_of_, gcount_, gmask_,
-                  dirty_, &dw_->err, nullptr, need_, reinterpret_cast<int32_t *>(jB_), &dw_->cnt[2], changes());
+                  dirty_, &dw_->err, nullptr, need_, reinterpret_cast<int32_t *>(jB_), &dw_->cnt[2], changes(), tie_, watch_);
     phase_end(PH_SWITCH);
     rc = sync_and_check("switch_strategy");
     if (rc) return rc;

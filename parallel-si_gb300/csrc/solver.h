@@ -185,7 +185,9 @@ private:
     int32_t *succ_ = nullptr, *ulist_ = nullptr;
     uint8_t *dirty_ = nullptr;   // parents whose child lists changed since the last evaluation
     uint8_t *need_ = nullptr;    // vertices their owner's next switch step must examine (ChangeTrack)
-    ChangeTrack track() const { return ChangeTrack{need_, rev_off_, rev_src_, &ctl_->quiet}; }
+    uint8_t *tie_ = nullptr;     // vertices whose last examination rested on a walk (ChangeTrack)
+    uint8_t *watch_ = nullptr;   // vertices such an examination rested on (ChangeTrack)
+    ChangeTrack track() const { return ChangeTrack{need_, rev_off_, rev_src_, &ctl_->quiet, tie_, watch_}; }
     void reset_tracking();       // every vertex to be examined (need = 1, quiet until the next evaluation)
     int32_t *rev_off_ = nullptr, *rev_src_ = nullptr;   // distinct in-neighbours (static)
     int2 *vloc_ = nullptr, *redA_ = nullptr, *redB_ = nullptr, *jA_ = nullptr, *jB_ = nullptr;

@@ -216,9 +216,12 @@ __device__ __forceinline__ void note_change(const ChangeList &c, int32_t v)
 // += strict improvements.  For a batch of games (game_of != nullptr) the
 // strict improvements are also added to gcount[game of the vertex]; with
 // gmask only vertices of games whose mask is set switch.  With need, an
-// examined vertex keeps need = 1 only if its best key is shared by two
-// distinct finite vertices (start or successors): its choice then rests on a
-// walk, which depends on more than the signatures tracked between steps.
+// examined vertex is sticky if its best key is shared by two distinct
+// finite vertices (start or successors): its choice then rests on a walk,
+// which depends on more than the keys tracked between steps.  With tie_out
+// the examined vertex gets need = 0 and tie_out = sticky (ChangeTrack says
+// when it is looked at again), and the successors a sticky vertex's choice
+// rests on (those at its best key) get watch = 1; without it, need = sticky.
 __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__restrict__ plist,
                                                    const int32_t *__restrict__ count, int32_t player,
                                                    const int32_t *__restrict__ off, const int32_t *__restrict__ tgt,
@@ -231,7 +234,8 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
                                                    const int32_t *__restrict__ gmask,
                                                    uint8_t *__restrict__ dirty, uint32_t *__restrict__ err,
                                                    const int32_t *__restrict__ gate, uint8_t *__restrict__ need,
-                                                   ChangeList changes)
+                                                   ChangeList changes, uint8_t *__restrict__ tie_out,
+                                                   uint8_t *__restrict__ watch)
 {
     if (gate && !*gate) return;
     if (count) np = *count;
@@ -320,7 +324,18 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
                 }
             }
         }
-        if (need) need[v] = (tie && ext != 0 && !key_infinite(ext)) ? 1 : 0;
+        const bool sticky = tie && ext != 0 && !key_infinite(ext);
+        if (tie_out) {
+            need[v] = 0;
+            tie_out[v] = sticky ? 1 : 0;
+            if (sticky && watch)   // the successors the tie rests on
+                for (int32_t e = e0; e < e1; e++) {
+                    const int32_t u = tgt[e];
+                    if (key[u] == ext) watch[u] = 1;
+                }
+        } else if (need) {
+            need[v] = sticky ? 1 : 0;
+        }
         if (moves) {   // strict improvements never return to cur0: cur != cur0
             strat[v] = cur;
             if (cur0 >= 0) dirty[cur0] = 1;
@@ -421,7 +436,7 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
                    const int32_t *tgt, int32_t *strat, const int32_t *st, const int32_t *key, const PathNode *node,
                    unsigned long long *stats, const int32_t *game_of, unsigned long long *gcount,
                    const int32_t *gmask, uint8_t *dirty, uint32_t *err, const int32_t *gate, uint8_t *need,
-                   int32_t *list, int32_t *list_count, ChangeList changes)
+                   int32_t *list, int32_t *list_count, ChangeList changes, uint8_t *tie, uint8_t *watch)
 {
     if (np <= 0) return;
     static int blocks = 0;   // resident blocks on the device (same device for the process's solvers)
@@ -441,7 +456,7 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
     }
     count_launch();
     k_switch<<<g, kBlock, 0, s>>>(np, items, count, player, off, tgt, strat, st, key, node, stats, game_of, gcount,
-                                  gmask, dirty, err, gate, need, changes);
+                                  gmask, dirty, err, gate, need, changes, tie, watch);
 }
 
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state, unsigned long long *gcount)
