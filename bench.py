@@ -214,6 +214,9 @@ def phase_bytes(phase, n, m, nsub, counters, calls, n_even, n_odd, iters, brs):
 
 KERNEL_OF_PHASE = {"switch": "k_switch", "sublist": "k_walk_sublists", "tour": "k_tour_relink",
                    "broadcast": "k_broadcast_depth", "reduced": "k_rank_reduced", "cycles": "k_cycles"}
+# the kernels of a timed phase (for their DRAM traffic per launch)
+PHASE_KERNELS = {"sublist": ("k_walk_sublists",), "tour": ("k_dirty_list", "k_tour_relink", "k_sink_list"),
+                 "broadcast": ("k_broadcast_depth", "k_rootinfo")}
 # phases of the full evaluation: their kernels work only in evaluations that
 # are not patches (in a patch they return at their gate), so their per-launch
 # time is their phase time over the full evaluations
@@ -353,7 +356,14 @@ def run_gb300(args, rank, world, local):
         pm, pc = phases[p][0], launches_of(p)
         b = phase_bytes(p, game.n, game.m, nsub, counters, pc, n_even, n_odd, iters, brs)
         if pc:
-            lr[p] = {"ms_per_call": pm / pc, "GBps": b / (pm / pc / 1e3) / 1e9, "frac": b / (pm / pc / 1e3) / 1e9 / peak}
+            sec = pm / pc / 1e3
+            lr[p] = {"ms_per_call": pm / pc, "GBps": b / sec / 1e9, "frac": b / sec / 1e9 / peak}
+            # DRAM bytes the phase's kernels move per full evaluation (ncu): random
+            # 4-byte accesses move whole 32-byte sectors
+            t = [traffic_per_launch(k, game.n) for k in PHASE_KERNELS[p]]
+            if all(x is not None for x in t):
+                lr[p].update({"traffic": sum(t), "traffic_GBps": sum(t) / sec / 1e9,
+                              "traffic_frac": sum(t) / sec / 1e9 / peak})
 
     # end to end through the C ABI from page-locked host buffers (psi_host_alloc)
     csr = []

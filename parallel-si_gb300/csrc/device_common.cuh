@@ -152,6 +152,46 @@ __device__ __forceinline__ void block_append(bool flag, int32_t value, int32_t *
     if (flag) list[block_base + warp_base[w] + __popc(mask & ((1u << lane) - 1))] = value;
 }
 
+// Block-aggregated append of up to K values per thread (v[k] < 0: none):
+// every thread of the block calls it; one atomic per block and three block
+// barriers per call (the last one frees the shared words for the next call).
+// Scans give each thread K items per pass, so K loads are in flight before
+// the barriers instead of one.
+template <int K>
+__device__ __forceinline__ void block_append_k(const int32_t (&v)[K], int32_t *__restrict__ list,
+                                               int32_t *__restrict__ count)
+{
+    __shared__ int32_t warp_base[kBlock / 32];
+    __shared__ int32_t block_base;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int32_t mine = 0;
+#pragma unroll
+    for (int k = 0; k < K; k++) mine += v[k] >= 0;
+    int32_t incl = mine;   // inclusive prefix over the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) warp_base[w] = incl;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int32_t sum = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+            const int32_t t = warp_base[i];
+            warp_base[i] = sum;
+            sum += t;
+        }
+        block_base = sum ? atomicAdd(count, sum) : 0;
+    }
+    __syncthreads();
+    int32_t at = block_base + warp_base[w] + incl - mine;
+#pragma unroll
+    for (int k = 0; k < K; k++)
+        if (v[k] >= 0) list[at++] = v[k];
+    __syncthreads();
+}
+
 // Warp-aggregated slot reservation: every lane of a converged warp calls it;
 // a lane with flag set gets base + its rank among the flagged lanes, where
 // base = atomicAdd(count, flagged lanes) (one atomic per warp); -1 otherwise.

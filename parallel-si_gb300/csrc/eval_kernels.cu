@@ -54,6 +54,10 @@ inline unsigned grid_for(int64_t items, int block = kBlock)
     return (unsigned)(g < 1 ? 1 : g);
 }
 
+// Scans of all vertices take kScanPer of them per thread and pass (blockDim
+// apart, so every load is coalesced).
+constexpr int kScanPer = 4;
+
 __device__ __forceinline__ int ceil_log2_dev(int64_t x)
 {
     int r = 0;
@@ -150,15 +154,23 @@ __global__ void k_dirty_list(int32_t n, uint8_t *__restrict__ dirty, int32_t *__
                              const uint8_t *__restrict__ tie, uint8_t *__restrict__ need)
 {
     if (gate && !*gate) return;
-    for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < n; b0 += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t p = (int32_t)(b0 + threadIdx.x);
-        const bool take = p < n && dirty[p];
-        if (take) dirty[p] = 0;
-        if (p < n) {
-            vloc[p] = make_int2(-1, -1);   // on no walked sublist until the walk reaches it
-            if (tie && tie[p]) need[p] = 1;
+    const int64_t pass = (int64_t)kScanPer * blockDim.x;
+    for (int64_t b0 = (int64_t)blockIdx.x * pass; b0 < n; b0 += (int64_t)gridDim.x * pass) {
+        int32_t v[kScanPer];
+#pragma unroll
+        for (int k = 0; k < kScanPer; k++) {
+            const int64_t i = b0 + (int64_t)k * blockDim.x + threadIdx.x;
+            v[k] = -1;
+            if (i < n) {
+                if (dirty[i]) {
+                    dirty[i] = 0;
+                    v[k] = (int32_t)i;
+                }
+                vloc[i] = make_int2(-1, -1);   // on no walked sublist until the walk reaches it
+                if (tie && tie[i]) need[i] = 1;
+            }
         }
-        block_append(take, p, list, count);
+        block_append_k(v, list, count);
     }
 }
 
@@ -196,9 +208,15 @@ __global__ void k_sink_list(int32_t n, const int32_t *__restrict__ strat, const 
                             const int32_t *__restrict__ gate)
 {
     if (gate && !*gate) return;
-    for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < n; b0 += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t v = (int32_t)(b0 + threadIdx.x);
-        block_append(v < n && strat[v] < 0 && !solved[v], v, sinklist, sinkcount);
+    const int64_t pass = (int64_t)kScanPer * blockDim.x;
+    for (int64_t b0 = (int64_t)blockIdx.x * pass; b0 < n; b0 += (int64_t)gridDim.x * pass) {
+        int32_t v[kScanPer];
+#pragma unroll
+        for (int k = 0; k < kScanPer; k++) {
+            const int64_t i = b0 + (int64_t)k * blockDim.x + threadIdx.x;
+            v[k] = (i < n && strat[i] < 0 && !solved[i]) ? (int32_t)i : -1;
+        }
+        block_append_k(v, sinklist, sinkcount);
     }
 }
 
@@ -618,13 +636,14 @@ int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const ui
     cudaError_t e = cudaMemsetAsync(dcount, 0, sizeof(int32_t), s);
     if (e != cudaSuccess) return (int)e;
     count_launch();
-    k_dirty_list<<<capped_grid(n), kBlock, 0, s>>>(n, dirty, dlist, dcount, vloc, gate, tie, need);
+    k_dirty_list<<<capped_grid(ceil_div(n, kScanPer)), kBlock, 0, s>>>(n, dirty, dlist, dcount, vloc, gate, tie,
+                                                                        need);
     count_launch();
     unsigned g = grid_for(n);
     g = g < 1216u ? g : 1216u;
     k_tour_relink<<<g, kBlock, 0, s>>>(dlist, dcount, strat, solved, rev_off, rev_src, succ, gate);
     count_launch();
-    k_sink_list<<<capped_grid(n), kBlock, 0, s>>>(n, strat, solved, sinklist, sinkcount, gate);
+    k_sink_list<<<capped_grid(ceil_div(n, kScanPer)), kBlock, 0, s>>>(n, strat, solved, sinklist, sinkcount, gate);
     count_launch();
     k_sink_chain<<<g, kBlock, 0, s>>>(n, sinklist, sinkcount, succ, gate);
     return 0;

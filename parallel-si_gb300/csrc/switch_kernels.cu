@@ -141,54 +141,25 @@ __device__ int compare_equal_keys(const PathNode *__restrict__ node, const int32
 // takes this step), appended to list with one atomic per block.  A block
 // pass covers kNeedPer * blockDim entries (each thread kNeedPer of them,
 // blockDim apart, so every load is coalesced; plist + offset may not be
-// 16-byte aligned, so no vector loads): two block barriers per pass.
+// 16-byte aligned, so no vector loads): block_append_k per pass.
 constexpr int kNeedPer = 4;
 __global__ void k_need_list(int32_t np, const int32_t *__restrict__ plist, const uint8_t *__restrict__ need,
                             const int32_t *__restrict__ game_of, const int32_t *__restrict__ gmask,
                             const int32_t *__restrict__ gate, int32_t *__restrict__ list, int32_t *__restrict__ count)
 {
     if (gate && !*gate) return;
-    __shared__ int32_t warp_base[kBlock / 32];
-    __shared__ int32_t block_base;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t pass = (int64_t)kNeedPer * blockDim.x;
     for (int64_t b0 = (int64_t)blockIdx.x * pass; b0 < np; b0 += (int64_t)gridDim.x * pass) {
         int32_t v[kNeedPer];
-        int mine = 0;
 #pragma unroll
         for (int k = 0; k < kNeedPer; k++) {
             const int64_t i = b0 + (int64_t)k * blockDim.x + threadIdx.x;
             v[k] = (i < np) ? plist[i] : -1;
         }
 #pragma unroll
-        for (int k = 0; k < kNeedPer; k++) {
-            const bool take = v[k] >= 0 && need[v[k]] && (!gmask || gmask[game_of[v[k]]]);
-            if (!take) v[k] = -1;
-            mine += take;
-        }
-        int32_t incl = mine;   // inclusive prefix over the warp
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
-        }
-        if (lane == 31) warp_base[w] = incl;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int32_t sum = 0;
-            for (int k = 0; k < (int)(blockDim.x >> 5); k++) {
-                const int32_t t = warp_base[k];
-                warp_base[k] = sum;
-                sum += t;
-            }
-            block_base = sum ? atomicAdd(count, sum) : 0;
-        }
-        __syncthreads();
-        int32_t at = block_base + warp_base[w] + incl - mine;
-#pragma unroll
         for (int k = 0; k < kNeedPer; k++)
-            if (v[k] >= 0) list[at++] = v[k];
-        __syncthreads();   // warp_base and block_base are rewritten by the next pass
+            if (v[k] >= 0 && !(need[v[k]] && (!gmask || gmask[game_of[v[k]]]))) v[k] = -1;
+        block_append_k(v, list, count);
     }
 }
 
