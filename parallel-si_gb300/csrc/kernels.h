@@ -200,6 +200,10 @@ void launch_union_fixup(cudaStream_t s, int32_t nu, int64_t mu, int32_t k_games,
 // following the vertex count from old_n to new_n.
 void launch_isolate_pairs(cudaStream_t s, int64_t count, int32_t *succ);
 void launch_move_extent(cudaStream_t s, int32_t old_n, int32_t new_n, int32_t *succ);
+// A finished game's strategy (its own ids) and infinite flags into out
+// (2 count entries).
+void launch_arena_export(cudaStream_t s, int32_t vb, int32_t count, const int32_t *strat, const int32_t *st,
+                         int32_t *out);
 void launch_arena_clear(cudaStream_t s, int32_t vb, int32_t count, uint8_t *solved, int32_t *game_of, int32_t *st,
                         int32_t *succ, uint8_t *dirty);
 // Appends the vertices of `player` that belong to a game to plist (*count += k).

@@ -113,26 +113,26 @@ public:
         bool changed = false;
         int rc = admit(&changed);
         if (rc) return rc;
-        if (changed) {
+        if (changed || lists_stale_) {   // one rebuild for this step's admissions and the last step's retirements
             rc = solver_->arena_rebuild_lists();
             if (rc) return rc;
+            lists_stale_ = false;
         }
         if (resident_ == 0) return PSI_OK;
         std::vector<int32_t> done, iters, brs;
         rc = solver_->arena_step(reset_, done, iters, brs);
         if (rc) return rc;
-        // retire the finished games together: copy their results out, free
-        // their ranges, then turn the copies into game-local results
+        // retire the finished games together: copy their results out (in
+        // game-local ids, converted on the device), then free their ranges
         std::vector<Request *> fin;
-        std::vector<std::vector<int32_t>> status;
         for (size_t i = 0; i < done.size(); i++) {
             Request *r = slot_req_[done[i]];
             if (!r) continue;
             r->iters = iters[i];
             r->brs = brs[i];
             r->strategy.resize(r->game.n);
-            status.emplace_back(r->game.n);
-            rc = solver_->arena_fetch((int32_t)r->vb, r->game.n, r->strategy.data(), status.back().data());
+            r->infinite.resize(r->game.n);
+            rc = solver_->arena_export((int32_t)r->vb, r->game.n, r->strategy.data(), r->infinite.data());
             if (rc) return rc;
             fin.push_back(r);
         }
@@ -147,18 +147,14 @@ public:
         }
         rc = solver_->arena_remove(vbs, counts, slots, (int32_t)extent());
         if (rc) return rc;
-        for (size_t i = 0; i < fin.size(); i++) {
-            Request *r = fin[i];
-            for (int32_t &t : r->strategy)
-                if (t >= 0) t -= (int32_t)r->vb;
-            r->infinite.resize(r->game.n);
-            for (int32_t v = 0; v < r->game.n; v++) r->infinite[v] = status_infinite(status[i][v]);
+        for (Request *r : fin) {
             release(r);
             r->state = 2;
             last_finished_.push_back(r->ticket);
             (*finished)++;
         }
-        return solver_->arena_rebuild_lists();
+        lists_stale_ = true;   // the player lists still hold the retired vertices
+        return PSI_OK;
     }
 
     int status(int64_t ticket, int32_t *state, int32_t *iters, int32_t *brs)
@@ -271,6 +267,7 @@ private:
     int64_t next_ticket_ = 1;
     int32_t resident_ = 0;
     int64_t used_v_ = 0, used_e_ = 0;
+    bool lists_stale_ = false;
 };
 
 int make_server(int64_t max_vertices, int64_t max_edges, int32_t slots, bool reset, const psi_options &opt,

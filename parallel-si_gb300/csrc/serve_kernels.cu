@@ -142,6 +142,19 @@ __global__ void k_move_extent(int32_t old_n, int32_t new_n, int32_t *__restrict_
     succ[2 * (int64_t)new_n + 1] = 2 * new_n;
 }
 
+// A finished game's results in its own vertex ids: out[0, count) its
+// strategy (-1 = the sink), out[count, 2 count) +1 where Even wins (valuation
+// +inf), -1 at -inf, 0 at a finite valuation (CPUParity's infinite[]).
+__global__ void k_arena_export(int32_t vb, int32_t count, const int32_t *__restrict__ strat,
+                               const int32_t *__restrict__ st, int32_t *__restrict__ out)
+{
+    const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const int32_t t = strat[vb + i];
+    out[i] = t >= 0 ? t - vb : t;
+    out[count + i] = st_infinite(st[vb + i]);
+}
+
 // A removed game's range becomes inert: solved, in no game, with no finite
 // depth left behind (the root-path summary pass visits every vertex with a
 // finite depth), and out of the tour.
@@ -283,6 +296,14 @@ void launch_move_extent(cudaStream_t s, int32_t old_n, int32_t new_n, int32_t *s
 {
     count_launch();
     k_move_extent<<<1, 1, 0, s>>>(old_n, new_n, succ);
+}
+
+void launch_arena_export(cudaStream_t s, int32_t vb, int32_t count, const int32_t *strat, const int32_t *st,
+                         int32_t *out)
+{
+    if (count <= 0) return;
+    count_launch();
+    k_arena_export<<<grid_for(count), kBlock, 0, s>>>(vb, count, strat, st, out);
 }
 
 void launch_arena_clear(cudaStream_t s, int32_t vb, int32_t count, uint8_t *solved, int32_t *game_of, int32_t *st,

@@ -984,15 +984,19 @@ int Solver::arena_remove(const std::vector<int32_t> &vb, const std::vector<int32
     return sync_and_check("arena_remove");
 }
 
-// Copies a game's strategy and status words out (no synchronisation; the
-// host buffers are complete after the next synchronising call).
-int Solver::arena_fetch(int32_t vb, int32_t count, int32_t *strategy, int32_t *status)
+int Solver::arena_export(int32_t vb, int32_t count, int32_t *strategy, int32_t *infinite)
 {
     if (vb < 0 || count < 0 || (int64_t)vb + count > n_) return fail(PSI_ERR_INVALID, "arena range out of range");
     if (count == 0) return PSI_OK;
-    PSI_CUDA_TRY(cudaMemcpyAsync(strategy, strat_ + vb, 4 * (size_t)count, cudaMemcpyDeviceToHost, stream_));
-    PSI_CUDA_TRY(cudaMemcpyAsync(status, st_ + vb, 4 * (size_t)count, cudaMemcpyDeviceToHost, stream_));
-    return PSI_OK;
+    int32_t *out = nullptr;
+    cudaError_t e = device_alloc((void **)&out, 8 * (size_t)count, stream_);
+    if (e != cudaSuccess) return fail(PSI_ERR_NOMEM, "arena export buffer");
+    launch_arena_export(stream_, vb, count, strat_, st_, out);
+    e = cudaMemcpyAsync(strategy, out, 4 * (size_t)count, cudaMemcpyDeviceToHost, stream_);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(infinite, out + count, 4 * (size_t)count, cudaMemcpyDeviceToHost, stream_);
+    cudaFreeAsync(out, stream_);
+    if (e != cudaSuccess) return fail(PSI_ERR_CUDA, std::string("arena export: ") + cudaGetErrorString(e));
+    return sync_and_check("arena_export");
 }
 
 // Player lists of the vertices that belong to games (Even's first).

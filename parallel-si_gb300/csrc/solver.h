@@ -113,7 +113,9 @@ public:
                   const std::vector<int32_t> &eb, const std::vector<int32_t> &slot, int32_t extent);
     int arena_remove(const std::vector<int32_t> &vb, const std::vector<int32_t> &count,
                      const std::vector<int32_t> &slot, int32_t extent);
-    int arena_fetch(int32_t vb, int32_t count, int32_t *strategy, int32_t *status);
+    // A game's results in its own vertex ids (strategy, infinite flags),
+    // converted on the device; the host buffers are complete on return.
+    int arena_export(int32_t vb, int32_t count, int32_t *strategy, int32_t *infinite);
     int arena_rebuild_lists();
     // One solve_si step of every resident game (its reset variant when `reset`);
     // `done` receives the slots that finished in this step with their
