@@ -176,20 +176,22 @@ __global__ void k_arena_clear(int32_t vb, int32_t count, uint8_t *__restrict__ s
 
 // Vertices of `player` that belong to a game, appended in any order (the
 // switch step treats every vertex independently).
+// Four slots per thread and pass, appended with one atomic per block (one per
+// warp on a single counter serialised over the 2^25-slot arena).
+constexpr int kPlistPer = 4;
 __global__ void k_build_plist(int32_t n, int32_t player, const int8_t *__restrict__ owner,
                               const int32_t *__restrict__ game_of, int32_t *__restrict__ plist,
                               int32_t *__restrict__ count)
 {
-    int32_t v = blockIdx.x * blockDim.x + threadIdx.x;
-    bool take = v < n && game_of[v] >= 0 && owner[v] == player;
-    unsigned mask = __ballot_sync(0xffffffffu, take);
-    if (mask) {
-        int lane = threadIdx.x & 31;
-        int leader = __ffs(mask) - 1;
-        int32_t base = 0;
-        if (lane == leader) base = atomicAdd(count, __popc(mask));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (take) plist[base + __popc(mask & ((1u << lane) - 1))] = v;
+    const int64_t pass = (int64_t)kPlistPer * blockDim.x;
+    for (int64_t b0 = (int64_t)blockIdx.x * pass; b0 < n; b0 += (int64_t)gridDim.x * pass) {
+        int32_t v[kPlistPer];
+#pragma unroll
+        for (int k = 0; k < kPlistPer; k++) {
+            const int64_t i = b0 + (int64_t)k * blockDim.x + threadIdx.x;
+            v[k] = (i < n && game_of[i] >= 0 && owner[i] == player) ? (int32_t)i : -1;
+        }
+        block_append_k(v, plist, count);
     }
 }
 
@@ -319,7 +321,9 @@ void launch_build_plist(cudaStream_t s, int32_t n, int32_t player, const int8_t 
 {
     if (n <= 0) return;
     count_launch();
-    k_build_plist<<<grid_for(n), kBlock, 0, s>>>(n, player, owner, game_of, plist, count);
+    unsigned g = grid_for(ceil_div(n, kPlistPer));
+    g = g < 2432u ? g : 2432u;   // 16 blocks per SM: a few passes per block
+    k_build_plist<<<g, kBlock, 0, s>>>(n, player, owner, game_of, plist, count);
 }
 
 void launch_serve_account(cudaStream_t s, int32_t slots, int32_t event, int4 *state, unsigned long long *gcount,
