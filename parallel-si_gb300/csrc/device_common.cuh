@@ -4,6 +4,7 @@
 
 #include <climits>
 #include <cstdint>
+#include <cooperative_groups.h>
 
 #include "kernels.h"
 #include <cuda_runtime.h>
@@ -204,6 +205,20 @@ __device__ __forceinline__ int32_t warp_reserve(bool flag, int32_t *count, int32
     if (lane == leader) base = atomicAdd(count, __popc(m));
     base = __shfl_sync(0xffffffffu, base, leader);
     return flag ? base_offset + base + __popc(m & ((1u << lane) - 1)) : -1;
+}
+
+// Appends a changed vertex to the change list, one atomic per group of lanes
+// that changed together; nothing once the list has overflowed (its count
+// then stays above the capacity, which marks it incomplete).
+__device__ __forceinline__ void note_change(const ChangeList &c, int32_t v)
+{
+    if (*(volatile int32_t *)c.count > c.cap) return;
+    cooperative_groups::coalesced_group grp = cooperative_groups::coalesced_threads();
+    int32_t base = 0;
+    if (grp.thread_rank() == 0) base = atomicAdd(c.count, (int32_t)grp.size());
+    base = grp.shfl(base, 0);
+    const int32_t p = base + (int32_t)grp.thread_rank();
+    if (p < c.cap) c.list[p] = v;
 }
 
 // Tour node ids (an Euler tour of the strategy forest, two nodes per vertex):

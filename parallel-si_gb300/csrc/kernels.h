@@ -190,7 +190,8 @@ void launch_arena_place(cudaStream_t s, int32_t nu, int32_t k_games, const int32
                         const int32_t *u_off, const int32_t *u_tgt, const int32_t *u_roff, const int32_t *u_rsrc,
                         int8_t *owner, int32_t *pri, int32_t *off, int32_t *tgt, int32_t *rev_off, int32_t *rev_src,
                         int32_t *strat, int32_t *st, uint8_t *solved, int32_t *game_of, int4 *gstate,
-                        unsigned long long *gcount, int32_t *succ, uint8_t *dirty, uint8_t *need);
+                        unsigned long long *gcount, int32_t *succ, uint8_t *dirty, uint8_t *need,
+                        ChangeList changes = ChangeList());
 // Games copied as they are into a union (game k at vertices ub[k], edges
 // ue[k]): offsets and targets shifted to union numbering, u_off[nu] = ue[K],
 // and game_of[v] = v's game when game_of != nullptr.
@@ -217,7 +218,8 @@ void launch_serve_account(cudaStream_t s, int32_t slots, int32_t event, int4 *st
 // switched go back to their first successor.
 void launch_serve_reset_odd(cudaStream_t s, int32_t np, const int32_t *plist, const int32_t *game_of,
                             const int32_t *gmask, const unsigned long long *gcount, const int32_t *off,
-                            const int32_t *tgt, int32_t *strat, uint8_t *dirty, uint8_t *need);
+                            const int32_t *tgt, int32_t *strat, uint8_t *dirty, uint8_t *need,
+                            ChangeList changes = ChangeList());
 
 // ---- dense valuation rows for export (the reference's ArrayVal layout)
 void launch_materialize(cudaStream_t s, int32_t v0, int32_t count, int32_t d, const int32_t *st,

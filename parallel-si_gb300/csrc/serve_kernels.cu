@@ -38,7 +38,7 @@ __global__ void k_arena_place(int32_t nu, int32_t k_games, const int32_t *__rest
                               int32_t *__restrict__ strat, int32_t *__restrict__ st, uint8_t *__restrict__ solved,
                               int32_t *__restrict__ game_of, int4 *__restrict__ gstate,
                               unsigned long long *__restrict__ gcount, int32_t *__restrict__ succ,
-                              uint8_t *__restrict__ dirty, uint8_t *__restrict__ need)
+                              uint8_t *__restrict__ dirty, uint8_t *__restrict__ need, ChangeList changes)
 {
     int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nu) return;
@@ -69,6 +69,7 @@ __global__ void k_arena_place(int32_t nu, int32_t k_games, const int32_t *__rest
     succ[2 * (int64_t)a + 1] = 2 * a;
     dirty[a] = 1;
     need[a] = 1;
+    if (changes.list) note_change(changes, a);   // a new vertex: the next evaluation may patch it in
     if (i == u0) {
         gstate[slot[k]] = make_int4(0, 0, 1, 0);
         gcount[slot[k]] = 0;
@@ -236,7 +237,7 @@ __global__ void k_serve_reset_odd(int32_t np, const int32_t *__restrict__ plist,
                                   const int32_t *__restrict__ gmask, const unsigned long long *__restrict__ gcount,
                                   const int32_t *__restrict__ off, const int32_t *__restrict__ tgt,
                                   int32_t *__restrict__ strat, uint8_t *__restrict__ dirty,
-                                  uint8_t *__restrict__ need)
+                                  uint8_t *__restrict__ need, ChangeList changes)
 {
     int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
@@ -249,17 +250,19 @@ __global__ void k_serve_reset_odd(int32_t np, const int32_t *__restrict__ plist,
     if (old >= 0) dirty[old] = 1;   // both parents' child lists change
     dirty[first] = 1;
     need[v] = 1;                    // its choice starts over
+    if (changes.list) note_change(changes, v);
 }
 
 }  // namespace
 
 void launch_serve_reset_odd(cudaStream_t s, int32_t np, const int32_t *plist, const int32_t *game_of,
                             const int32_t *gmask, const unsigned long long *gcount, const int32_t *off,
-                            const int32_t *tgt, int32_t *strat, uint8_t *dirty, uint8_t *need)
+                            const int32_t *tgt, int32_t *strat, uint8_t *dirty, uint8_t *need, ChangeList changes)
 {
     if (np <= 0) return;
     count_launch();
-    k_serve_reset_odd<<<grid_for(np), kBlock, 0, s>>>(np, plist, game_of, gmask, gcount, off, tgt, strat, dirty, need);
+    k_serve_reset_odd<<<grid_for(np), kBlock, 0, s>>>(np, plist, game_of, gmask, gcount, off, tgt, strat, dirty, need,
+                                                      changes);
 }
 
 void launch_arena_place(cudaStream_t s, int32_t nu, int32_t k_games, const int32_t *ub, const int32_t *vb,
@@ -267,13 +270,14 @@ void launch_arena_place(cudaStream_t s, int32_t nu, int32_t k_games, const int32
                         const int32_t *u_off, const int32_t *u_tgt, const int32_t *u_roff, const int32_t *u_rsrc,
                         int8_t *owner, int32_t *pri, int32_t *off, int32_t *tgt, int32_t *rev_off, int32_t *rev_src,
                         int32_t *strat, int32_t *st, uint8_t *solved, int32_t *game_of, int4 *gstate,
-                        unsigned long long *gcount, int32_t *succ, uint8_t *dirty, uint8_t *need)
+                        unsigned long long *gcount, int32_t *succ, uint8_t *dirty, uint8_t *need,
+                        ChangeList changes)
 {
     if (nu <= 0) return;
     count_launch();
     k_arena_place<<<grid_for(nu), kBlock, 0, s>>>(nu, k_games, ub, vb, eb, slot, u_owner, u_pri, u_off, u_tgt, u_roff,
                                                   u_rsrc, owner, pri, off, tgt, rev_off, rev_src, strat, st, solved,
-                                                  game_of, gstate, gcount, succ, dirty, need);
+                                                  game_of, gstate, gcount, succ, dirty, need, changes);
 }
 
 void launch_union_fixup(cudaStream_t s, int32_t nu, int64_t mu, int32_t k_games, const int32_t *ub, const int32_t *ue,

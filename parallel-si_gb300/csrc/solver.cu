@@ -83,7 +83,9 @@ int Solver::create_arena(int64_t max_vertices, int64_t max_edges, int32_t slots,
     s->device_ = opt.device;
     s->timing_ = opt.timing != 0;
     s->stride_ = opt.sublist_len;
-    s->incremental_ = PSI_INCR_OFF;   // admissions and retirements change vertices outside any switch step
+    // admissions list their new vertices as changed ones: a patch evaluates them
+    s->incremental_ = opt.incremental;
+    s->patch_limit_ = opt.patch_limit;
     rc = s->alloc_arrays(max_vertices, max_edges);
     if (!rc) rc = s->init_arena(slots);
     if (rc) {
@@ -944,12 +946,14 @@ int Solver::arena_add(const std::vector<const HostGame *> &gs, const std::vector
         ce = build_reverse_csr(stream_, (int32_t)n, m, u_off, u_tgt, u_roff, u_rsrc, &mr);
     }
     if (e == cudaSuccess && !ce) {
-        e = cudaMemsetAsync(&dw_->ucount, 0, sizeof(int32_t), stream_);   // the unreached list is stale
+        // with full evaluations only, the unreached list is rebuilt before its next use; after a
+        // patch mark_solved reads it (the new vertices are appended by the patch)
+        if (incremental_ == PSI_INCR_OFF) e = cudaMemsetAsync(&dw_->ucount, 0, sizeof(int32_t), stream_);
         if (extent != n_) launch_move_extent(stream_, n_, extent, succ_);
         const int32_t *vbd = d_tab + 2 * K + 2, *ebd = d_tab + 3 * K + 2, *sld = d_tab + 4 * K + 2;
         launch_arena_place(stream_, (int32_t)n, K, d_tab, vbd, ebd, sld, u_owner, u_pri, u_off, u_tgt, u_roff, u_rsrc,
                            owner_, pri_, off_, tgt_, rev_off_, rev_src_, strat_, st_, solved_, game_of_, gstate_,
-                           gcount_, succ_, dirty_, need_);
+                           gcount_, succ_, dirty_, need_, changes());
         if (e == cudaSuccess) e = cudaGetLastError();
     }
     for (int i = 0; i < 7; i++)
@@ -978,7 +982,8 @@ int Solver::arena_remove(const std::vector<int32_t> &vb, const std::vector<int32
         launch_arena_clear(stream_, vb[k], count[k], solved_, game_of_, st_, succ_, dirty_);
         PSI_CUDA_TRY(cudaMemsetAsync(gstate_ + slot[k], 0, sizeof(int4), stream_));
     }
-    PSI_CUDA_TRY(cudaMemsetAsync(&dw_->ucount, 0, sizeof(int32_t), stream_));
+    // the retired vertices left in the unreached list are solved: mark_solved passes them by
+    if (incremental_ == PSI_INCR_OFF) PSI_CUDA_TRY(cudaMemsetAsync(&dw_->ucount, 0, sizeof(int32_t), stream_));
     if (extent != n_) launch_move_extent(stream_, n_, extent, succ_);
     set_extent(extent);
     return sync_and_check("arena_remove");
@@ -1044,7 +1049,7 @@ int Solver::arena_step(bool reset, std::vector<int32_t> &done, std::vector<int32
     if (rc) return rc;
     if (reset)
         launch_serve_reset_odd(stream_, np_ - np0_, plist_ + np0_, game_of_, gmask_, gcount_, off_, tgt_, strat_,
-                               dirty_, need_);
+                               dirty_, need_, changes());
     launch_serve_account(stream_, games_, 2, gstate_, gcount_, gmask_);
     std::vector<int4> st((size_t)games_);
     PSI_CUDA_TRY(cudaMemcpyAsync(st.data(), gstate_, sizeof(int4) * (size_t)games_, cudaMemcpyDeviceToHost, stream_));

@@ -163,20 +163,6 @@ __global__ void k_need_list(int32_t np, const int32_t *__restrict__ plist, const
     }
 }
 
-// Appends a changed vertex to the change list, one atomic per group of lanes
-// that changed together; nothing once the list has overflowed (its count
-// then stays above the capacity, which marks it incomplete).
-__device__ __forceinline__ void note_change(const ChangeList &c, int32_t v)
-{
-    if (*(volatile int32_t *)c.count > c.cap) return;
-    cg::coalesced_group grp = cg::coalesced_threads();
-    int32_t base = 0;
-    if (grp.thread_rank() == 0) base = atomicAdd(c.count, (int32_t)grp.size());
-    base = grp.shfl(base, 0);
-    const int32_t p = base + (int32_t)grp.thread_rank();
-    if (p < c.cap) c.list[p] = v;
-}
-
 // One thread per vertex of the list (all owned by `player`; the list is plist
 // itself, np entries, or -- with count != nullptr -- the *count vertices
 // k_need_list selected).  Per compared edge the common case is one 4-byte
