@@ -127,6 +127,80 @@ __device__ __forceinline__ void top1_merge(int32_t &m, int32_t &c, int32_t m2, i
     }
 }
 
+struct Top2 {
+    int32_t m1, c1, m2, c2;
+};
+
+__device__ __forceinline__ void top2_add(Top2 &t, int32_t p)
+{
+    if (p > t.m1) {
+        t.m2 = t.m1;
+        t.c2 = t.c1;
+        t.m1 = p;
+        t.c1 = 1;
+    } else if (p == t.m1) {
+        t.c1++;
+    } else if (p > t.m2) {
+        t.m2 = p;
+        t.c2 = 1;
+    } else if (p == t.m2) {
+        t.c2++;
+    }
+}
+
+// adds count occurrences of priority p
+__device__ __forceinline__ void top2_add_n(Top2 &t, int32_t p, int32_t count)
+{
+    if (count <= 0) return;
+    if (p > t.m1) {
+        t.m2 = t.m1;
+        t.c2 = t.c1;
+        t.m1 = p;
+        t.c1 = count;
+    } else if (p == t.m1) {
+        t.c1 += count;
+    } else if (p > t.m2) {
+        t.m2 = p;
+        t.c2 = count;
+    } else if (p == t.m2) {
+        t.c2 += count;
+    }
+}
+
+// Landmark skips for the comparison walks.  A finite vertex at depth d has
+// its landmark at depth L = SKIP_K * floor((d - 1) / SKIP_K): the ancestor
+// there (the sink at L = 0).  skip[v] = (landmark, top two priorities of the
+// segment from v up to the landmark, exclusive, and their counts packed as
+// c1 | c2 << 16; a segment holds at most SKIP_K vertices).  Written by the
+// root-summary pass of a full evaluation; a patch marks its vertices'
+// records unknown (the paths of all other vertices are unchanged).
+constexpr int32_t SKIP_K = 32;
+constexpr int32_t SKIP_UNKNOWN = INT32_MIN;
+__host__ __device__ __forceinline__ int32_t skip_landmark_depth(int32_t d) { return ((d - 1) / SKIP_K) * SKIP_K; }
+__device__ __forceinline__ int4 skip_pack(int32_t anc, const Top2 &t)
+{
+    return make_int4(anc, t.m1, t.m2, (t.c1 & 0xffff) | (t.c2 << 16));
+}
+__device__ __forceinline__ void skip_merge(Top2 &t, const int4 s)
+{
+    top2_add_n(t, s.y, s.w & 0xffff);
+    top2_add_n(t, s.z, (int32_t)((uint32_t)s.w >> 16));
+}
+
+// Release store of a root-path summary (rmax, rcnt) as one 8-byte word: the
+// skip record written before it is visible to any thread that acquires it.
+__device__ __forceinline__ void publish_summary(PathNode *p, int32_t m, int32_t c)
+{
+    const unsigned long long w = (unsigned long long)(uint32_t)m | ((unsigned long long)(uint32_t)c << 32);
+    asm volatile("st.release.gpu.global.b64 [%0], %1;" ::"l"(&p->rmax), "l"(w) : "memory");
+}
+__device__ __forceinline__ int32_t acquire_rmax(const PathNode *p)
+{
+    int32_t x;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(x) : "l"(&p->rmax) : "memory");
+    return x;
+}
+
 // Block-aggregated append: every thread of the block calls it (no early
 // return before); one atomic on the shared counter per block instead of one
 // per warp, which serialises when most warps append (the sink's children,

@@ -359,9 +359,11 @@ __global__ void k_broadcast_depth(int32_t n, const int2 *__restrict__ vloc, cons
 // the final pair, which is written as one 8-byte store.  The key is written
 // only where it changed; all threads stay to the end (flag_in_neighbours is
 // warp-collective).
-__global__ void k_rootinfo(int32_t n, const int32_t *__restrict__ st, PathNode *__restrict__ node,
+// eight blocks per SM (at most 32 registers): the walks are latency-bound
+__global__ void __launch_bounds__(kBlock, 8) k_rootinfo(int32_t n, const int32_t *__restrict__ st,
+                                                        PathNode *__restrict__ node,
                            int32_t *__restrict__ key, uint32_t *__restrict__ err, ChangeTrack track,
-                           const int32_t *__restrict__ gate)
+                           const int32_t *__restrict__ gate, int4 *__restrict__ skip)
 {
     if (gate && !*gate) return;
     for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < n; b0 += (int64_t)gridDim.x * blockDim.x) {
@@ -369,8 +371,12 @@ __global__ void k_rootinfo(int32_t n, const int32_t *__restrict__ st, PathNode *
         bool changed = false;
         if (v < n && st[v] >= 1) {
             const int32_t old = key ? key[v] : 0;
+            const int32_t d = st[v], L = skip_landmark_depth(d);
             PathNode q = node[v];
-            int32_t m = q.pri, c = 1, y = q.parent;
+            int32_t m = q.pri, c = 1, y = q.parent, dy = d - 1;
+            // the landmark segment: v, then the ancestors above it down to depth L + 1
+            Top2 seg = {q.pri, 1, -1, 0};
+            int32_t anc = (dy == L) ? y : SKIP_UNKNOWN;
             int32_t steps = 0;
             while (y >= 0) {
                 int4 r = *reinterpret_cast<const int4 *>(&node[y]);
@@ -379,13 +385,38 @@ __global__ void k_rootinfo(int32_t n, const int32_t *__restrict__ st, PathNode *
                     break;
                 }
                 top1_merge(m, c, r.y, 1);
+                if (anc == SKIP_UNKNOWN) top2_add(seg, r.y);
                 y = r.x;
+                if (--dy == L && anc == SKIP_UNKNOWN) anc = y;
                 if (++steps > n) {
                     atomicOr(err, DERR_WALK_CAP);
                     break;
                 }
             }
-            *reinterpret_cast<int2 *>(&node[v].rmax) = make_int2(m, c);
+            if (skip) {
+                // stopped inside the segment at y, whose summary is known: its skip was
+                // published before it (same landmark); if not yet visible, walk on
+                for (int32_t guard = 0; anc == SKIP_UNKNOWN && y >= 0 && guard <= SKIP_K; guard++) {
+                    // only a summary published in this evaluation vouches for the skip
+                    // (the broadcast reset every reached vertex's summary)
+                    if (acquire_rmax(&node[y]) != RM_UNKNOWN) {
+                        const int4 sy = __ldcg(&skip[y]);
+                        if (sy.x != SKIP_UNKNOWN) {
+                            skip_merge(seg, sy);
+                            anc = sy.x;
+                            break;
+                        }
+                    }
+                    const int2 r = *reinterpret_cast<const int2 *>(&node[y]);
+                    top2_add(seg, r.y);
+                    y = r.x;
+                    if (--dy == L) anc = y;
+                }
+                skip[v] = skip_pack(anc, seg);
+                publish_summary(&node[v], m, c);   // release: the skip before the summary that vouches for it
+            } else {
+                *reinterpret_cast<int2 *>(&node[v].rmax) = make_int2(m, c);
+            }
             const int32_t k = finite_key(m, c);
             if (key && k != old) {
                 key[v] = k;
@@ -691,10 +722,10 @@ void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const i
 }
 
 void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, int32_t *key, uint32_t *err,
-                     ChangeTrack track, const int32_t *gate)
+                     ChangeTrack track, const int32_t *gate, int4 *skip)
 {
     count_launch();
-    k_rootinfo<<<capped_grid(n), kBlock, 0, s>>>(n, st, node, key, err, track, gate);
+    k_rootinfo<<<capped_grid(n), kBlock, 0, s>>>(n, st, node, key, err, track, gate, skip);
 }
 
 int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, const int32_t *strat,

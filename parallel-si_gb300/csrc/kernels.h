@@ -136,8 +136,9 @@ void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const i
                             const int32_t *gate = nullptr);
 // Root-path summaries (rmax, rcnt) of every reached vertex, also stored as its
 // comparison key when key != nullptr.
+// With skip (n entries), also each reached vertex's landmark skip (device_common.cuh).
 void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, int32_t *key, uint32_t *err,
-                     ChangeTrack track = ChangeTrack(), const int32_t *gate = nullptr);
+                     ChangeTrack track = ChangeTrack(), const int32_t *gate = nullptr, int4 *skip = nullptr);
 // Cycle parity of the *ucount vertices in ulist (cooperative launch), also
 // stored as their comparison keys when key != nullptr.  ja, jb: n entries;
 // la, lb: n entries (active lists); cnt: 3 counters.  Returns a cudaError_t
@@ -175,7 +176,7 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
                    unsigned long long *gcount, const int32_t *gmask, uint8_t *dirty, uint32_t *err,
                    const int32_t *gate = nullptr, uint8_t *need = nullptr, int32_t *list = nullptr,
                    int32_t *list_count = nullptr, ChangeList changes = ChangeList(), uint8_t *tie = nullptr,
-                   uint8_t *watch = nullptr);
+                   uint8_t *watch = nullptr, const int4 *skip = nullptr);
 // ---- batches: per-game accounting of solve_si (state[g] = brs, iters,
 // odd_done, done; gcount[g] = strict improvements of the last switch step)
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state,
@@ -246,6 +247,7 @@ struct PatchArgs {
     int32_t *ulist = nullptr;   // unreached list, appended to (mark_solved scans it)
     unsigned long long *stats = nullptr;   // [0] += 1 per patch, [1] += vertices re-evaluated
     ChangeTrack track;
+    int4 *skip = nullptr;       // landmark skips: a patched vertex's record becomes unknown
 };
 // Sets the gates the host decides before an evaluation (one thread).
 void launch_eval_gates(cudaStream_t s, EvalGates *g, int32_t full, int32_t incr, int32_t try_patch);

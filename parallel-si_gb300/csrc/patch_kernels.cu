@@ -347,6 +347,7 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_values(PatchArgs a)
             }
             // re-evaluated: a tied in-neighbour looks again even at an unchanged key
             mode = changed ? 2 : (a.track.watch && a.track.watch[v] ? 1 : 0);
+            if (a.skip) a.skip[v] = make_int4(SKIP_UNKNOWN, 0, 0, 0);   // its path changed: walks step here
             a.apos[v] = -1;
         }
         flag_in_neighbours(a.track, mode, v);

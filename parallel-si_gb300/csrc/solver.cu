@@ -233,6 +233,7 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
         {(void **)&st_, 4 * (size_t)cap_n},
         {(void **)&solved_, (size_t)cap_n},
         {(void **)&node_, sizeof(PathNode) * (size_t)cap_n},
+        {(void **)&skip_, sizeof(int4) * (size_t)cap_n},
         {(void **)&key_, 4 * (size_t)cap_n},
         {(void **)&succ_, 4 * (size_t)capL},
         {(void **)&dirty_, (size_t)cap_n},
@@ -486,6 +487,7 @@ PatchArgs Solver::patch_args()
     a.ulist = ulist_;
     a.stats = dw_->patch;
     a.track = track();
+    a.skip = skip_;
     return a;
 }
 
@@ -548,7 +550,7 @@ int Solver::enqueue_full(bool timed)
     begin(PH_BROADCAST);
     launch_broadcast_depth(stream_, n_, vloc_, fin, strat_, pri_, solved_, st_, node_, ulist_, &dw_->ucount,
                            &ctl_->eval);
-    launch_rootinfo(stream_, n_, st_, node_, key_, &dw_->err, track(), &ctl_->eval);
+    launch_rootinfo(stream_, n_, st_, node_, key_, &dw_->err, track(), &ctl_->eval, skip_);
     end(PH_BROADCAST);
     // 4. cycle parity by pointer jumping over the unreached vertices (the
     //    tour's vloc array is free again: it holds the two active lists)
@@ -614,7 +616,7 @@ int Solver::switch_strategy(int32_t player, int64_t *switched)
     const int32_t *pl = plist_ + (player == 0 ? 0 : np0_);
     // jB_ is free until the next cycle pass: it holds the list of vertices to examine
     launch_switch(stream_, np, pl, player, off_, tgt_, strat_, st_, key_, node_, dw_->sw, game_of_, gcount_, gmask_,
-                  dirty_, &dw_->err, nullptr, need_, reinterpret_cast<int32_t *>(jB_), &dw_->cnt[2], changes(), tie_, watch_);
+                  dirty_, &dw_->err, nullptr, need_, reinterpret_cast<int32_t *>(jB_), &dw_->cnt[2], changes(), tie_, watch_, skip_);
     phase_end(PH_SWITCH);
     rc = sync_and_check("switch_strategy");
     if (rc) return rc;

@@ -182,6 +182,7 @@ private:
     int32_t *strat_ = nullptr, *st_ = nullptr;
     uint8_t *solved_ = nullptr;
     PathNode *node_ = nullptr;   // parent, priority and root-path summary (evaluation snapshot)
+    int4 *skip_ = nullptr;       // landmark skips of the comparison walks (device_common.cuh)
     int32_t *key_ = nullptr;   // comparison key per vertex (device_common.cuh)
     // evaluation scratch
     int32_t *succ_ = nullptr, *ulist_ = nullptr;

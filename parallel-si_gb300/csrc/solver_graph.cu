@@ -132,7 +132,7 @@ int Solver::enqueue_step(cudaGraph_t body, cudaGraphConditionalHandle loop, bool
     if (e != cudaSuccess) return abort_capture(fail(PSI_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e)));
     int32_t *todo = reinterpret_cast<int32_t *>(jB_);   // free until the next cycle pass
     launch_switch(stream_, np_ - np0_, plist_ + np0_, 1, off_, tgt_, strat_, st_, key_, node_, dw_->sw, nullptr,
-                  nullptr, nullptr, dirty_, &dw_->err, nullptr, need_, todo, &dw_->cnt[2], changes(), tie_, watch_);
+                  nullptr, nullptr, dirty_, &dw_->err, nullptr, need_, todo, &dw_->cnt[2], changes(), tie_, watch_, skip_);
     count_launch();
     k_ctl_odd<<<1, 1, 0, stream_>>>(ctl_, dw_->sw);
     // Even, when Odd made no strict improvement: mark_solved(0), switch(0)
@@ -141,7 +141,7 @@ int Solver::enqueue_step(cudaGraph_t body, cudaGraphConditionalHandle loop, bool
     e = cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_);
     if (e != cudaSuccess) return abort_capture(fail(PSI_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e)));
     launch_switch(stream_, np0_, plist_, 0, off_, tgt_, strat_, st_, key_, node_, dw_->sw, nullptr, nullptr, nullptr,
-                  dirty_, &dw_->err, &ctl_->even, need_, todo, &dw_->cnt[2], changes(), tie_, watch_);
+                  dirty_, &dw_->err, &ctl_->even, need_, todo, &dw_->cnt[2], changes(), tie_, watch_, skip_);
     count_launch();
     k_ctl_even<<<1, 1, 0, stream_>>>(ctl_, dw_->sw, loop, reset ? 1 : 0, kEvalGuard);
     e = cudaGetLastError();

@@ -41,27 +41,6 @@ inline unsigned grid_for(int64_t items, int block = kBlock)
     return (unsigned)(g < 1 ? 1 : g);
 }
 
-struct Top2 {
-    int32_t m1, c1, m2, c2;
-};
-
-__device__ __forceinline__ void top2_add(Top2 &t, int32_t p)
-{
-    if (p > t.m1) {
-        t.m2 = t.m1;
-        t.c2 = t.c1;
-        t.m1 = p;
-        t.c1 = 1;
-    } else if (p == t.m1) {
-        t.c1++;
-    } else if (p > t.m2) {
-        t.m2 = p;
-        t.c2 = 1;
-    } else if (p == t.m2) {
-        t.c2++;
-    }
-}
-
 // Even's view of a difference at priority p: +1 if side a is better.
 __device__ __forceinline__ int decide(int32_t p, int32_t ca, int32_t cb)
 {
@@ -70,20 +49,64 @@ __device__ __forceinline__ int decide(int32_t p, int32_t ca, int32_t cb)
 }
 
 // Tier 3: walks to the lowest common ancestor of u and w (depths du, dw; w may
-// be the sink, -1 with depth 0).
-__device__ int walk_compare(const PathNode *__restrict__ node, int32_t u, int32_t du, int32_t w, int32_t dw,
-                            int32_t &loads, uint32_t *__restrict__ err)
+// be the sink, -1 with depth 0), collecting the top two priorities of each
+// side's segment below it; passes after the first repeat the walk counting
+// only priorities below the last tie.  With skip, the first pass jumps whole
+// landmark segments (device_common.cuh): the deeper side jumps while its
+// landmark is no shallower than the other side; at equal depths both jump
+// while their landmarks differ (the common ancestor is then above both);
+// once they share one, the common ancestor lies in that segment and both
+// step one vertex at a time.
+__device__ int walk_compare(const PathNode *__restrict__ node, const int4 *__restrict__ skip, int32_t u, int32_t du,
+                            int32_t w, int32_t dw, int32_t &loads, uint32_t *__restrict__ err)
 {
     int32_t thr = INT_MAX;
     const int32_t max_pass = (du + dw) / 2 + 2;
     for (int32_t pass = 0; pass < max_pass; pass++) {
         Top2 A = {-1, 0, -1, 0}, B = {-1, 0, -1, 0};
         int32_t a = u, b = w, da = du, db = dw;
+        bool jumps = skip != nullptr && pass == 0;
         while (a != b || da != db) {
             bool adv_a = da >= db, adv_b = db >= da;
             if ((adv_a && (a < 0 || da <= 0)) || (adv_b && (b < 0 || db <= 0))) {   // inconsistent: cannot happen
                 atomicOr(err, DERR_WALK_CAP);
                 return 0;
+            }
+            if (jumps) {
+                if (adv_a && adv_b) {
+                    const int4 sa = skip[a], sb = skip[b];
+                    loads += 2;
+                    if (sa.x != SKIP_UNKNOWN && sb.x != SKIP_UNKNOWN) {
+                        if (sa.x != sb.x) {
+                            skip_merge(A, sa);
+                            skip_merge(B, sb);
+                            a = sa.x;
+                            b = sb.x;
+                            da = db = skip_landmark_depth(da);
+                            continue;
+                        }
+                        jumps = false;   // one landmark: the common ancestor is within this segment
+                    }
+                } else {
+                    const int32_t x = adv_a ? a : b, dx = adv_a ? da : db, other = adv_a ? db : da;
+                    const int32_t L = skip_landmark_depth(dx);
+                    if (L >= other) {
+                        const int4 sx = skip[x];
+                        loads++;
+                        if (sx.x != SKIP_UNKNOWN) {
+                            if (adv_a) {
+                                skip_merge(A, sx);
+                                a = sx.x;
+                                da = L;
+                            } else {
+                                skip_merge(B, sx);
+                                b = sx.x;
+                                db = L;
+                            }
+                            continue;
+                        }
+                    }
+                }
             }
             if (adv_a) {
                 int2 q = *reinterpret_cast<const int2 *>(&node[a]);
@@ -118,14 +141,15 @@ __device__ int walk_compare(const PathNode *__restrict__ node, int32_t u, int32_
 // Even's view of finite u against finite w (u != w) when their keys are
 // equal: the exact summaries decide, else a walk to the lowest common
 // ancestor (w = -1 is the sink).
-__device__ int compare_equal_keys(const PathNode *__restrict__ node, const int32_t *__restrict__ st,
-                                               int32_t u, int32_t w, int32_t &loads, uint32_t *__restrict__ err)
+__device__ int compare_equal_keys(const PathNode *__restrict__ node, const int4 *__restrict__ skip,
+                                  const int32_t *__restrict__ st, int32_t u, int32_t w, int32_t &loads,
+                                  uint32_t *__restrict__ err)
 {
     const int2 ru = *reinterpret_cast<const int2 *>(&node[u].rmax);
     const int2 rw = (w >= 0) ? *reinterpret_cast<const int2 *>(&node[w].rmax) : make_int2(-1, 0);
     if (ru.x != rw.x) return ru.x > rw.x ? decide(ru.x, ru.y, 0) : decide(rw.x, 0, rw.y);
     if (ru.y != rw.y) return decide(ru.x, ru.y, rw.y);
-    return walk_compare(node, u, st[u], w, w >= 0 ? st[w] : 0, loads, err);
+    return walk_compare(node, skip, u, st[u], w, w >= 0 ? st[w] : 0, loads, err);
 }
 
 // One thread per vertex of plist (all owned by `player`).  Per compared edge
@@ -192,7 +216,7 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
                                                    uint8_t *__restrict__ dirty, uint32_t *__restrict__ err,
                                                    const int32_t *__restrict__ gate, uint8_t *__restrict__ need,
                                                    ChangeList changes, uint8_t *__restrict__ tie_out,
-                                                   uint8_t *__restrict__ watch)
+                                                   uint8_t *__restrict__ watch, const int4 *__restrict__ skip)
 {
     if (gate && !*gate) return;
     if (count) np = *count;
@@ -273,7 +297,7 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
                 int c;
                 if (ku != kc) c = ku > kc ? 1 : -1;
                 else if (u == cur || key_infinite(ku)) c = 0;
-                else c = compare_equal_keys(node, st, u, cur, t_loads, err);
+                else c = compare_equal_keys(node, skip, st, u, cur, t_loads, err);
                 if ((player == 0 && c > 0) || (player == 1 && c < 0)) {
                     cur = u;
                     kc = ku;
@@ -393,7 +417,8 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
                    const int32_t *tgt, int32_t *strat, const int32_t *st, const int32_t *key, const PathNode *node,
                    unsigned long long *stats, const int32_t *game_of, unsigned long long *gcount,
                    const int32_t *gmask, uint8_t *dirty, uint32_t *err, const int32_t *gate, uint8_t *need,
-                   int32_t *list, int32_t *list_count, ChangeList changes, uint8_t *tie, uint8_t *watch)
+                   int32_t *list, int32_t *list_count, ChangeList changes, uint8_t *tie, uint8_t *watch,
+                   const int4 *skip)
 {
     if (np <= 0) return;
     static int blocks = 0;   // resident blocks on the device (same device for the process's solvers)
@@ -413,7 +438,7 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
     }
     count_launch();
     k_switch<<<g, kBlock, 0, s>>>(np, items, count, player, off, tgt, strat, st, key, node, stats, game_of, gcount,
-                                  gmask, dirty, err, gate, need, changes, tie, watch);
+                                  gmask, dirty, err, gate, need, changes, tie, watch, skip);
 }
 
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state, unsigned long long *gcount)
