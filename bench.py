@@ -37,6 +37,7 @@ for _p in (ROOT, PKG):
 METRIC = "SI iters/s"
 UNIT = "SI iters/s"
 N_DEFAULT = 1 << 24
+LONGPATH_N = 1 << 23
 DEG_LO, DEG_HI = 2, 5
 CPU_SAMPLE_N = 1 << 15          # bounded sample for the CPU reference algorithm
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -44,10 +45,26 @@ FALLBACK_HBM_GBS = 6800.0
 TRAFFIC_PATH = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
 
 
-def workload_config(n, m=None, seed=1):
+LONGPATH_PRI = 1024            # long-path games: priority U[0,1024)
+
+
+def make_game(psi, family, n, seed):
+    """The single game a step solves: the random headline game or the long-path game."""
+    if family == "longpath":
+        return psi.Game.longpath(n, LONGPATH_PRI, seed)
+    return psi.Game.random(n, DEG_LO, DEG_HI, n, seed)
+
+
+def workload_config(n, m=None, seed=1, family="single"):
+    if family == "longpath":
+        text = (f"long-path parity game, n={n} (2^{n.bit_length() - 1}): chain v_i -> v_(i+1) plus one back-edge "
+                f"per vertex to a uniformly random earlier vertex, owner alternating, priority uniform in "
+                f"[0,{LONGPATH_PRI})")
+    else:
+        text = (f"single random parity game, n={n} (2^{n.bit_length() - 1}): owner uniform, priority uniform in "
+                f"[0,n), out-degree uniform in [{DEG_LO},{DEG_HI}], distinct non-self successors")
     cfg = {
-        "workload": f"single random parity game, n={n} (2^{n.bit_length() - 1}): owner uniform, priority "
-                    f"uniform in [0,n), out-degree uniform in [{DEG_LO},{DEG_HI}], distinct non-self successors",
+        "workload": text,
         "n": n,
         "seed": seed,
         "step": "one full solve_si (init_strat to convergence) through psi_solve, game resident in HBM",
@@ -223,13 +240,13 @@ PHASE_KERNELS = {"sublist": ("k_walk_sublists",), "tour": ("k_dirty_list", "k_to
 FULL_EVAL_PHASES = ("sublist", "tour", "broadcast", "reduced", "cycles")
 
 
-def cpu_baseline_sample(solves=3, seed=1):
+def cpu_baseline_sample(solves=3, seed=1, family="single"):
     """The oracle (C restatement of CPUParity), single thread, on the bounded
     sample: `solves` full solves of the n=2^15 game of the same distribution."""
     import oracle
     import psi
 
-    g = psi.Game.random(CPU_SAMPLE_N, DEG_LO, DEG_HI, CPU_SAMPLE_N, seed)
+    g = make_game(psi, family, CPU_SAMPLE_N, seed)
     o = oracle.Oracle(*g.csr())
     t0 = time.perf_counter()
     iters = 0
@@ -240,7 +257,8 @@ def cpu_baseline_sample(solves=3, seed=1):
     o.close()
     return {"value": iters / dt, "unit": UNIT, "cores": 1, "kind": "port",
             "sample": f"{solves} full solves of the n=2^15 game of the same distribution (seed {seed}); "
-                      f"{dt:.1f} s; the reference's CPUParity keeps n*(max_pri+1) ints and cannot hold n=2^24"}
+                      f"{dt:.1f} s; the reference's CPUParity keeps n*(max_pri+1) ints and cannot hold the "
+                      f"full-size game"}
 
 
 # ------------------------------------------------------------------ arms
@@ -250,7 +268,7 @@ def run_reference(args, rank, world):
     import oracle
     import psi
 
-    g = psi.Game.random(CPU_SAMPLE_N, DEG_LO, DEG_HI, CPU_SAMPLE_N, args.seed)
+    g = make_game(psi, args.workload, CPU_SAMPLE_N, args.seed)
     o = oracle.Oracle(*g.csr())
     for _ in range(args.warmup):
         o.solve()
@@ -263,12 +281,12 @@ def run_reference(args, rank, world):
     value = iters / dt
     sample = (f"each step: one full solve of the n=2^15 game of the same distribution (seed {args.seed}) by "
               f"the oracle (C restatement of the reference CPUParity, single thread; the reference's dense "
-              f"valuation table cannot hold n=2^24)")
+              f"valuation table cannot hold the full-size game)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": workload_config(args.n, seed=args.seed),
+        "config": workload_config(args.n, seed=args.seed, family=args.workload),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -281,7 +299,7 @@ def run_gb300(args, rank, world, local):
 
     dist = Dist(world, local)
     seed = args.seed + rank
-    game = psi.Game.random(args.n, DEG_LO, DEG_HI, args.n, seed)
+    game = make_game(psi, args.workload, args.n, seed)
     owner, _, _, _ = game.csr()
     n_odd = int(owner.sum())
     n_even = game.n - n_odd
@@ -343,7 +361,8 @@ def run_gb300(args, rank, world, local):
     roofline = None
     if bpc is not None and dom_calls:
         achieved = bpc / (dom_ms / dom_calls / 1e3) / 1e9
-        traffic = traffic_per_launch(KERNEL_OF_PHASE[dom], game.n)
+        # the committed DRAM captures are of the random game: no figure for another workload
+        traffic = traffic_per_launch(KERNEL_OF_PHASE[dom], game.n) if args.workload == "single" else None
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                     "traffic": traffic, "kernel": KERNEL_OF_PHASE[dom], "peak_source": peak_kind,
                     "algorithmic_bytes_per_launch": bpc, "ms_per_launch": dom_ms / dom_calls}
@@ -361,7 +380,7 @@ def run_gb300(args, rank, world, local):
             # DRAM bytes the phase's kernels move per full evaluation (ncu): random
             # 4-byte accesses move whole 32-byte sectors
             t = [traffic_per_launch(k, game.n) for k in PHASE_KERNELS[p]]
-            if all(x is not None for x in t):
+            if args.workload == "single" and all(x is not None for x in t):
                 lr[p].update({"traffic": sum(t), "traffic_GBps": sum(t) / sec / 1e9,
                               "traffic_frac": sum(t) / sec / 1e9 / peak})
 
@@ -390,13 +409,14 @@ def run_gb300(args, rank, world, local):
     e2e_max = dist.max(e2e_s)
     e2e_iters_all = dist.sum(e2e_iters)
 
-    cpu = cpu_baseline_sample(seed=args.seed) if (rank == 0 and world == 1 and not args.no_cpu) else None
+    cpu = (cpu_baseline_sample(seed=args.seed, family=args.workload) if (rank == 0 and world == 1 and not args.no_cpu)
+           else None)
     if rank == 0:
         line = {
             "metric": METRIC, "value": iters_all / (ms_max / 1e3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic", "config": dict(workload_config(game.n, game.m, args.seed),
+            "data": "synthetic", "config": dict(workload_config(game.n, game.m, args.seed, args.workload),
                                                 sublist_len=args.sublist_len, patch_limit=args.patch_limit,
                                                 iters_per_solve=iters // args.steps, brs_per_solve=brs // args.steps),
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
@@ -576,7 +596,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
-    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--n", type=int, default=0, help="vertices (default 2^24; 2^23 for --workload longpath)")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--sublist-len", type=int, default=64)
     ap.add_argument("--patch-limit", type=int, default=0,
@@ -584,9 +604,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--host-loop", action="store_true",
                     help="time the host-driven solve loop instead of the default one-graph solve")
-    ap.add_argument("--workload", choices=("single", "batch", "serve"), default="single",
-                    help="single: the 2^24 game (headline); batch: many mixed-size games solved together; "
-                         "serve: the same kind of games arriving at a continuous-batching server")
+    ap.add_argument("--workload", choices=("single", "longpath", "batch", "serve"), default="single",
+                    help="single: the 2^24 game (headline); longpath: the 2^23 long-path game; batch: many "
+                         "mixed-size games solved together; serve: the same kind of games arriving at a "
+                         "continuous-batching server")
     ap.add_argument("--batch-games", type=int, default=4096)
     ap.add_argument("--solo-stride", type=int, default=16)
     ap.add_argument("--serve-games", type=int, default=256)
@@ -595,6 +616,8 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=1024)
     ap.add_argument("--arena-vertices", type=int, default=1 << 25)
     args = ap.parse_args()
+    if args.n <= 0:
+        args.n = LONGPATH_N if args.workload == "longpath" else N_DEFAULT
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     rank, world, local = dist_env()
