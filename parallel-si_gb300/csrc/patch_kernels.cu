@@ -43,7 +43,9 @@
 //     = its vertices + its seed's depth, or the seed's infinity.  The
 //     infinite ones are appended to the unreached list that mark_solved scans
 //     (an entry that has since become finite is skipped there, st being
-//     finite).
+//     finite).  A changed key flags the vertex's in-neighbours as in a full
+//     evaluation; an unchanged one only those tied on it (ChangeTrack); the
+//     vertex's landmark skip becomes unknown (its path changed).
 #include <climits>
 #include <cooperative_groups.h>
 
