@@ -61,6 +61,10 @@ namespace {
 constexpr unsigned kAll = 0xffffffffu;
 constexpr int kPatchBlock = 256;
 constexpr int32_t kBackoffMax = 64;
+// the search goes on in one block once a level has at most this many vertices
+constexpr int32_t kSoloFrontier = 256;
+// and gives up if a level widens past this again
+constexpr int32_t kSoloGiveUp = 8192;
 
 __device__ __forceinline__ int ceil_log2_i(int64_t x)
 {
@@ -200,8 +204,9 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_collect(PatchArgs a)
     // two levels later, when every thread has read it.
     int32_t lo = 0, end = *(volatile int32_t *)&g->lcnt[0];
     const int32_t nseeds = end;
-    bool bail = false;
-    for (int32_t level = 1;; level++) {
+    bool bail = false, solo = false;
+    int32_t level = 1;
+    for (;; level++) {
         if (end > a.acap) {
             bail = true;
             break;
@@ -209,6 +214,10 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_collect(PatchArgs a)
         if (lo == end) break;   // no vertex found in the last level: A is complete
         if (level > a.max_levels) {
             bail = true;
+            break;
+        }
+        if (end - lo <= kSoloFrontier) {   // every thread sees the same lo, end: a uniform decision
+            solo = true;
             break;
         }
         int32_t *lcount = &g->lcnt[level % 3];
@@ -227,17 +236,56 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_collect(PatchArgs a)
         end += *(volatile int32_t *)lcount;
     }
 
-    if (!bail) {
+    if (solo) {
+        // Narrow levels (the tails of the search, often long): block 0 goes on
+        // alone with block barriers, the other blocks are done.  Should a level
+        // widen past kSoloGiveUp again, the patch gives up (exact either way).
+        if (blockIdx.x != 0) return;
+        const int warps = blockDim.x >> 5, wid = threadIdx.x >> 5;
+        for (;; level++) {
+            if (end > a.acap || end - lo > kSoloGiveUp) {
+                bail = true;
+                break;
+            }
+            if (lo == end) break;
+            if (level > a.max_levels) {
+                bail = true;
+                break;
+            }
+            int32_t *lcount = &g->lcnt[level % 3];
+            if (leader) g->lcnt[(level + 1) % 3] = 0;   // last read two levels ago
+            const int64_t f = end - lo;
+            const int64_t k = f >= warps * 32 ? 32 : (f + warps - 1) / warps;
+            for (int64_t i0 = lo + wid * k; i0 < end; i0 += warps * k) {
+                const int64_t i = i0 + lane;
+                const bool valid = lane < k && i < end;
+                expand_children(a, valid, valid ? a.alist[i] : 0, i, end, lcount);
+            }
+            __syncthreads();
+            lo = end;
+            end += *(volatile int32_t *)lcount;
+            __syncthreads();   // every thread has read the count before it is reset
+        }
+        if (!bail) {
+            if (leader) {
+                g->acount = end;
+                g->nseeds = nseeds;
+            }
+            return;
+        }
+    } else if (!bail) {
         if (leader) {
             g->acount = end;
             g->nseeds = nseeds;
         }
         return;
     }
-    // give up: A's marks cleared, the full evaluation's gates opened
+    // give up: A's marks cleared, the full evaluation's gates opened (by the
+    // whole grid, or by block 0 alone after the narrow levels)
     const int32_t na = end < a.acap ? end : a.acap;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < na; i += (int64_t)gridDim.x * blockDim.x)
-        a.apos[a.alist[i]] = -1;
+    const int64_t t0 = solo ? threadIdx.x : (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t tn = solo ? blockDim.x : (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = t0; i < na; i += tn) a.apos[a.alist[i]] = -1;
     if (leader) {
         g->patch = 0;
         g->eval = 1;
