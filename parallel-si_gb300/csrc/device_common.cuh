@@ -72,7 +72,10 @@ __host__ __device__ __forceinline__ int key_infinite(int32_t k)
 // spread over the warp's lanes (their rev_off spans laid end to end), so one
 // round of rev_src loads usually covers them all, instead of one dependent
 // load per in-edge on those lanes while the rest of the warp waits.
-__device__ __forceinline__ void flag_in_neighbours(const ChangeTrack &t, int mode, int32_t v)
+// With rev (b, d) given, the lane's in-edges are rev_src[b, b + d) and
+// rev_off is not read.
+__device__ __forceinline__ void flag_in_neighbours(const ChangeTrack &t, int mode, int32_t v,
+                                                   const int2 *rev = nullptr)
 {
     if (!t.need || (t.quiet && *t.quiet)) return;
     if (!t.tie && mode == 1) mode = 0;
@@ -82,8 +85,13 @@ __device__ __forceinline__ void flag_in_neighbours(const ChangeTrack &t, int mod
     const int lane = threadIdx.x & 31;
     int32_t b = 0, d = 0;
     if (mode) {
-        b = t.rev_off[v];
-        d = t.rev_off[v + 1] - b;
+        if (rev) {
+            b = rev->x;
+            d = rev->y;
+        } else {
+            b = t.rev_off[v];
+            d = t.rev_off[v + 1] - b;
+        }
     }
     int32_t incl = d;   // inclusive prefix of d over the lanes
     for (int o = 1; o < 32; o <<= 1) {

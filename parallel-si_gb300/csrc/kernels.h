@@ -238,6 +238,7 @@ struct PatchArgs {
     int32_t *alist = nullptr;   // the vertices re-evaluated (acap entries)
     int32_t *apos = nullptr;    // per vertex: its position in alist, -1 if none (n entries, -1 between patches)
     int4 *rel = nullptr;                 // per position of alist: seed, path summary to it (acap)
+    int2 *arev = nullptr;                // per position of alist: the vertex's in-edge range (acap)
     int4 *sja = nullptr, *sjb = nullptr; // pointer-jumping entries of the seeds (acap each)
     int32_t acap = 0, ccap = 0, max_levels = 0;
     int64_t ucap = 0;           // capacity of ulist

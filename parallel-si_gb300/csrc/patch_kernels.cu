@@ -26,7 +26,8 @@
 //     by its own successor, with no atomics on the vertex; a warp spreads its
 //     vertices' in-edges over its lanes.  On the way down each vertex gets
 //     its seed and the summary of its path up to that seed (`rel`: seed
-//     index, vertices, top priority, its count), from its successor's.  If A
+//     index, vertices, top priority, its count), from its successor's, and
+//     its in-edge range (`arev`, read while it was tested).  If A
 //     outgrows its buffer or the levels their cap, the patch gives up: the
 //     full evaluation's gates open instead, and the next few evaluations do
 //     not try (doubling each time).
@@ -113,7 +114,10 @@ __global__ void k_patch_begin(PatchArgs a)
 // positions i of alist) laid end to end over the warp's lanes, 32 per round;
 // each lane tests its edge's source u for being a child of its x outside A,
 // appends it to alist at position end + (its slot counted in *lcount) and
-// gives it x's seed with the path summary extended by u.
+// gives it x's seed with the path summary extended by u.  A level is a chain
+// of dependent loads, so every load that does not need the test is issued
+// with it: u's successor, solved flag, position, priority and in-edge range
+// (stored with a child, so the next level starts from a coalesced read).
 __device__ __forceinline__ void expand_children(const PatchArgs &a, bool valid, int32_t x, int64_t i, int32_t end,
                                                 int32_t *lcount)
 {
@@ -121,8 +125,9 @@ __device__ __forceinline__ void expand_children(const PatchArgs &a, bool valid, 
     int32_t b = 0, d = 0;
     int4 r = make_int4(0, 0, -1, 0);
     if (valid) {
-        b = a.rev_off[x];
-        d = a.rev_off[x + 1] - b;
+        const int2 ev = a.arev[i];
+        b = ev.x;
+        d = ev.y;
         r = a.rel[i];
     }
     int32_t incl = d;
@@ -148,17 +153,23 @@ __device__ __forceinline__ void expand_children(const PatchArgs &a, bool valid, 
         rl.y = __shfl_sync(kAll, r.y, l);
         rl.z = __shfl_sync(kAll, r.z, l);
         rl.w = __shfl_sync(kAll, r.w, l);
-        int32_t u = -1, pu = 0;
+        int32_t u = -1, pu = 0, ub = 0, ue = 0;
         bool child = false;
         if (j < total) {
             u = a.rev_src[bl + (j - el)];
-            child = a.strat[u] == xl && !a.solved[u] && a.apos[u] == -1;
+            const int32_t su = a.strat[u];
+            const uint8_t so = a.solved[u];
+            const int32_t ap = a.apos[u];
             pu = a.pri[u];
+            ub = a.rev_off[u];
+            ue = a.rev_off[u + 1];
+            child = su == xl && !so && ap == -1;
         }
         const int32_t p = warp_reserve(child, lcount, end);
         if (child && p < a.acap) {
             a.alist[p] = u;
             a.apos[u] = p;
+            a.arev[p] = make_int2(ub, ue - ub);
             int32_t m = pu, c = 1;
             top1_merge(m, c, rl.z, rl.w);
             a.rel[p] = make_int4(rl.x, rl.y + 1, m, c);
@@ -192,6 +203,7 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_collect(PatchArgs a)
                 a.alist[p] = v;
                 a.apos[v] = p;
                 a.rel[p] = make_int4(p, 0, -1, 0);   // its own seed, empty path above it
+                a.arev[p] = make_int2(a.rev_off[v], a.rev_off[v + 1] - a.rev_off[v]);
             } else {
                 a.apos[v] = -1;
             }
@@ -375,32 +387,39 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_values(PatchArgs a)
         int32_t v = -1;
         bool changed = false, unreached = false;
         int mode = 0;
+        int2 ev = make_int2(0, 0);   // v's in-edge range, stored by the search
         if (i < na) {
             v = a.alist[i];
+            ev = a.arev[i];
             const int4 r = a.rel[i];
+            // v's own words, loaded before any store (which might alias them)
+            // so that they travel with the seed's value
+            const int32_t sv_strat = a.strat[v], sv_pri = a.pri[v];
+            const int32_t oldk = a.key ? a.key[v] : 0;
+            const bool watched = a.track.watch && a.track.watch[v];
             const int4 sv = out[r.x];
             int32_t k;
             if (sv.x >= 1) {
                 int32_t m = r.z, c = r.w;
                 top1_merge(m, c, sv.y, sv.z);
                 a.st[v] = r.y + sv.x;
-                a.node[v] = PathNode{a.strat[v], a.pri[v], m, c};
+                a.node[v] = PathNode{sv_strat, sv_pri, m, c};
                 k = finite_key(m, c);
             } else {
                 a.st[v] = sv.x;
                 k = (sv.x == ST_POS_INF) ? KEY_POS_INF : KEY_NEG_INF;
                 unreached = true;
             }
-            if (a.key && a.key[v] != k) {
+            if (a.key && oldk != k) {
                 a.key[v] = k;
                 changed = true;
             }
             // re-evaluated: a tied in-neighbour looks again even at an unchanged key
-            mode = changed ? 2 : (a.track.watch && a.track.watch[v] ? 1 : 0);
+            mode = changed ? 2 : (watched ? 1 : 0);
             if (a.skip) a.skip[v] = make_int4(SKIP_UNKNOWN, 0, 0, 0);   // its path changed: walks step here
             a.apos[v] = -1;
         }
-        flag_in_neighbours(a.track, mode, v);
+        flag_in_neighbours(a.track, mode, v, &ev);
         block_append(unreached, v, a.ulist, a.ucount);
     }
     if (tid == 0) {

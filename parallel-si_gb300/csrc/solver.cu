@@ -263,7 +263,7 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
             {(void **)&clist_, 4 * (size_t)ccap_},
             {(void **)&alist_, 4 * (size_t)acap_},
             {(void **)&apos_, 4 * (size_t)std::max<int64_t>(1, cap_n)},
-            {(void **)&pj_, 3 * sizeof(int4) * (size_t)acap_},
+            {(void **)&pj_, (3 * sizeof(int4) + sizeof(int2)) * (size_t)acap_},
         };
         for (const auto &a : patch) {
             cudaError_t e = device_alloc(a.ptr, a.bytes, stream_);
@@ -477,6 +477,7 @@ PatchArgs Solver::patch_args()
     a.rel = pj_;
     a.sja = pj_ ? pj_ + acap_ : nullptr;
     a.sjb = pj_ ? pj_ + 2 * (size_t)acap_ : nullptr;
+    a.arev = pj_ ? reinterpret_cast<int2 *>(pj_ + 3 * (size_t)acap_) : nullptr;
     a.acap = acap_;
     a.ccap = ccap_;
     a.max_levels = max_levels_;
