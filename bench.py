@@ -73,7 +73,7 @@ def workload_config(n, m=None, seed=1, family="single"):
         "l2": "inputs larger than L2 (game CSR + solver state ~1.3 GB at n=2^24), no flush",
         "parallelism": "replicas: one independent game per GPU",
         "evaluation": "incremental where few strategies changed (psi_options.incremental = auto: patches after "
-                      "steps that changed <= max(1024, n/64) strategies, else the full Euler-tour evaluation); "
+                      "steps that changed <= patch_limit strategies, else the full Euler-tour evaluation); "
                       "results identical to full evaluations",
     }
     if m is not None:
@@ -184,6 +184,39 @@ def hbm_peak():
             return float(json.load(f)["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         return FALLBACK_HBM_GBS, "fallback"
+
+
+def random_access_peak(local, array_bytes, reps=10):
+    """Measured bound for random 4-byte accesses on this GPU
+    (psi_measure_random_access): independent loads from uniformly random
+    positions of a device array of `array_bytes`, eight in flight per thread on
+    every SM, median of `reps` launches timed with CUDA events.  Each such
+    load moves a whole 32-byte sector (sector_GBps) unless L2 holds it.  The
+    evaluation's walks and the switch's key gathers are reads of this kind; a
+    phase is compared with the bound measured at the size of the array it
+    reads at random (so with the share of L2 hits that size allows)."""
+    import psi
+
+    r = psi.measure_random_access(local, int(array_bytes), reps)
+    r["array_bytes"] = int(array_bytes)
+    return r
+
+
+def random_accesses(phase, n, counters, n_even, n_odd, iters, brs):
+    """Random (data-dependent) 4-byte accesses per call of a phase, where the
+    phase is a chase or a gather: the sublist walk reads one successor per
+    tour node and writes one (sublist, prefix) entry per vertex; the switch
+    gathers the key of every compared successor and of each vertex's current
+    choice, loads a parent per walk step, and sets two dirty flags per
+    changed vertex."""
+    L = 2 * n + 2
+    if phase == "sublist":
+        return L + n
+    if phase == "switch":
+        sw_calls = max(1, counters["switches"])
+        player_vertices = brs * n_odd + iters * n_even
+        return (counters["sw_edges"] + player_vertices + counters["sw_loads"] + 2 * counters["sw_changed"]) / sw_calls
+    return None
 
 
 def traffic_per_launch(kernel, n):
@@ -303,10 +336,16 @@ def run_gb300(args, rank, world, local):
     owner, _, _, _ = game.csr()
     n_odd = int(owner.sum())
     n_even = game.n - n_odd
-    # the product path: psi_solve with default options (the whole solve_si
-    # loop as one CUDA graph, device-side loop control)
-    solver = psi.GPUList(game, device=local, sublist_len=args.sublist_len, graph=int(not args.host_loop),
-                         patch_limit=args.patch_limit)
+    # launch options: chosen by the autotuner (trial solves of this game,
+    # before the warm-up) unless --no-tune, then from the flags
+    tuning = None
+    knobs = dict(sublist_len=args.sublist_len, patch_limit=args.patch_limit, walk_block=args.walk_block)
+    if not args.no_tune:
+        o, tuning = psi.autotune(game, repeats=2, device=local, graph=int(not args.host_loop))
+        knobs = dict(sublist_len=o.sublist_len, patch_limit=o.patch_limit, walk_block=o.walk_block)
+    # the product path: psi_solve (the whole solve_si loop as one CUDA graph,
+    # device-side loop control)
+    solver = psi.GPUList(game, device=local, graph=int(not args.host_loop), **knobs)
 
     for _ in range(args.warmup):
         solver.solve()
@@ -335,8 +374,7 @@ def run_gb300(args, rank, world, local):
     if args.host_loop:
         phase_solver = solver
     else:
-        phase_solver = psi.GPUList(game, device=local, sublist_len=args.sublist_len, graph=0,
-                                   patch_limit=args.patch_limit)
+        phase_solver = psi.GPUList(game, device=local, graph=0, **knobs)
         phase_solver.solve()
         phase_solver.reset_times()
         for _ in range(args.steps):
@@ -345,7 +383,8 @@ def run_gb300(args, rank, world, local):
     counters = phase_solver.counters()
     if phase_solver is not solver:
         phase_solver.close()
-    nsub = (2 * game.n + 1 + args.sublist_len - 1) // args.sublist_len + 1
+    stride = knobs["sublist_len"]
+    nsub = (2 * game.n + 1 + stride - 1) // stride + 1
     full_evals = max(1, counters["evals"] - counters["patches"])
 
     def launches_of(p):
@@ -370,6 +409,29 @@ def run_gb300(args, rank, world, local):
             # what HBM actually moved per second (random 32-byte sectors count whole)
             roofline["traffic_GBps"] = traffic / (dom_ms / dom_calls / 1e3) / 1e9
             roofline["traffic_frac"] = roofline["traffic_GBps"] / peak
+    # the random-access bound beside the copy bound, measured at the size of
+    # the array each phase reads at random (the tour's successors for the
+    # sublist walk, the comparison keys for the switch) and at 1 GiB (DRAM)
+    rpeak = {"how": "psi_measure_random_access: independent 4-byte loads at uniformly random positions of a "
+                    "device array of the given size, 8 in flight per thread, every SM filled; median of 10 "
+                    "launches (CUDA events); sector_GBps counts 32 B per load",
+             "dram_1GiB": random_access_peak(local, 1 << 30),
+             "sublist": random_access_peak(local, 4 * (2 * game.n + 2)),
+             "switch": random_access_peak(local, 4 * game.n)}
+
+    def vs_random(p, ms_per_call):
+        k = random_accesses(p, game.n, counters, n_even, n_odd, iters, brs)
+        if k is None or not ms_per_call or p not in rpeak:
+            return None
+        g = k / (ms_per_call / 1e3) / 1e9
+        pk = rpeak[p]["G_per_s"]
+        return {"accesses_per_launch": k, "G_per_s": g, "peak_G_per_s": pk, "array_bytes": rpeak[p]["array_bytes"],
+                "frac": g / pk}
+
+    if roofline is not None:
+        ra = vs_random(dom, roofline["ms_per_launch"])
+        if ra:
+            roofline["random_access"] = ra
     lr = {}
     for p in ("sublist", "tour", "broadcast"):
         pm, pc = phases[p][0], launches_of(p)
@@ -377,6 +439,9 @@ def run_gb300(args, rank, world, local):
         if pc:
             sec = pm / pc / 1e3
             lr[p] = {"ms_per_call": pm / pc, "GBps": b / sec / 1e9, "frac": b / sec / 1e9 / peak}
+            ra = vs_random(p, pm / pc)
+            if ra:
+                lr[p]["random_access"] = ra
             # DRAM bytes the phase's kernels move per full evaluation (ncu): random
             # 4-byte accesses move whole 32-byte sectors
             t = [traffic_per_launch(k, game.n) for k in PHASE_KERNELS[p]]
@@ -398,7 +463,7 @@ def run_gb300(args, rank, world, local):
     e2e_iters = 0
     d2h = 0
     for _ in range(args.steps):
-        s2 = psi.GPUList.from_csr(*csr, device=local, sublist_len=args.sublist_len, patch_limit=args.patch_limit)
+        s2 = psi.GPUList.from_csr(*csr, device=local, **knobs)
         it, _ = s2.solve()
         w0 = s2.get_winning(0, out=out_w)
         strat = s2.get_strategy(out=out_s)
@@ -417,12 +482,12 @@ def run_gb300(args, rank, world, local):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
             "data": "synthetic", "config": dict(workload_config(game.n, game.m, args.seed, args.workload),
-                                                sublist_len=args.sublist_len, patch_limit=args.patch_limit,
+                                                **knobs, tuning=tuning,
                                                 iters_per_solve=iters // args.steps, brs_per_solve=brs // args.steps),
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
             "e2e": {"value": e2e_iters_all / e2e_max, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "list_ranking": lr,
+            "list_ranking": lr, "random_access_peak": rpeak,
             "phase_ms_per_solve": {k: v[0] / args.steps for k, v in phases.items()},
             "counters_per_solve": {k: v / args.steps for k, v in counters.items()},
         }
@@ -447,7 +512,18 @@ def run_batch(args, rank, world, local):
     sizes = psi.batch_sizes(args.batch_games, 100, 200000, args.seed)
     mine = psi.shard_games(sizes.astype(np.int64) + 1, world)[rank]
     games = [psi.Game.random(int(sizes[i]), 2, 8, int(sizes[i]), args.seed * 100003 + int(i)) for i in mine]
-    batch = psi.Batch(games, device=local)
+    # launch options from the autotuner, timed on every 8th game of this
+    # rank's share solved as one batch (before the warm-up), unless --no-tune
+    tuning = None
+    knobs = dict(sublist_len=args.sublist_len, patch_limit=args.patch_limit, walk_block=args.walk_block)
+    if not args.no_tune:
+        o, tuning = psi.autotune(games[::8], repeats=1, device=local)
+        knobs = dict(sublist_len=o.sublist_len, patch_limit=o.patch_limit, walk_block=o.walk_block)
+        # the sample's patch limit scales with the vertices of the whole share
+        total = sum(g.n for g in games)
+        sample = max(1, sum(g.n for g in games[::8]))
+        knobs["patch_limit"] = max(1024, int(o.patch_limit * total / sample)) if o.patch_limit else 0
+    batch = psi.Batch(games, device=local, **knobs)
     for _ in range(args.warmup):
         batch.solve()
     dist.barrier()
@@ -476,7 +552,8 @@ def run_batch(args, rank, world, local):
         "config": {"workload": f"{len(sizes)} random games, n_i log-uniform in [100,200000], out-degree U[2,8], "
                                f"priority U[0,n_i)", "total_vertices": nv, "total_edges": ne,
                    "max_iters": max_it, "max_brs": max_br,
-                   "parallelism": f"games sharded by footprint over {world} rank(s)"},
+                   "parallelism": f"games sharded by footprint over {world} rank(s)",
+                   **knobs, "tuning": tuning, "one_by_one_options": "defaults"},
         "one_by_one": {"games": int(n_solo), "games_per_s": n_solo / t_solo},
         "speedup_vs_one_by_one": (len(sizes) / t_batch) / (n_solo / t_solo),
         "counts_match_solo": exact,
@@ -598,7 +675,10 @@ def main():
     ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     ap.add_argument("--n", type=int, default=0, help="vertices (default 2^24; 2^23 for --workload longpath)")
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--sublist-len", type=int, default=64)
+    ap.add_argument("--sublist-len", type=int, default=64, help="with --no-tune")
+    ap.add_argument("--walk-block", type=int, default=0, help="with --no-tune (0: the library default)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the autotuner: sublist/walk/patch options from the flags")
     ap.add_argument("--patch-limit", type=int, default=0,
                     help="psi_options.patch_limit (0: the library default, max(1024, n/64))")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")

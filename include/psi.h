@@ -98,7 +98,8 @@ typedef struct {
                                 the same as a full evaluation's) */
     int32_t patch_limit;     /* PSI_INCR_AUTO: the most changed strategies after which a
                                 patch is tried (0, the default: max(1024, n/64)) */
-    int32_t reserved[1];
+    int32_t walk_block;      /* threads per block of the sublist walk (one thread per
+                                sublist): a multiple of 32 in [32, 1024]; 0, the default: 128 */
 } psi_options;
 
 /* incremental: PSI_INCR_AUTO (default) patches after steps that changed at
@@ -186,6 +187,21 @@ int psi_solver_unreached(psi_solver *s, int64_t *count);
 int psi_solver_counters(psi_solver *s, int64_t *out, int32_t k);
 /* Kernel launches issued by this library in this process so far. */
 int64_t psi_launch_count(void);
+/* The random-access bound for rooflines: times independent 4-byte loads
+ * from uniformly random positions of a device array of array_bytes (a
+ * multiple of 4 in [2^20, 2^34]; allocated and freed inside the call) on
+ * `device`,
+ * eight in flight per thread with every SM filled, about 2^27 loads per
+ * launch; reports the median of `reps` launches (after two untimed ones) as
+ * loads per second.  Each such load moves a whole 32-byte sector, so this is
+ * the ceiling for the data-dependent reads of the sublist walks, the
+ * root-summary walks and the switch's key gathers, beside the copy bandwidth
+ * that bounds streaming kernels; measured at the size of the array a kernel
+ * reads at random it includes the share of L2 hits that size allows (L2 is
+ * 129 MB on GB300).  No counterpart in the reference. */
+int psi_measure_random_access(int32_t device, int64_t array_bytes, int32_t reps, double *gathers_per_s,
+                              double *ms_per_launch, int64_t *gathers_per_launch);
+
 /* Page-locked host memory (cudaMallocHost), for callers that upload games and
  * read results back at full DMA speed: every psi_* call that takes or fills a
  * host array accepts it.  psi_host_free(NULL) does nothing. */
@@ -217,6 +233,37 @@ int psi_batch_solve(psi_batch *b, int32_t *iter_counts, int32_t *br_counts);
 /* Game-local results (vertex ids of the game, -1 = sink). */
 int psi_batch_get_strategy(psi_batch *b, int32_t game, int32_t *out);
 int psi_batch_get_winning(psi_batch *b, int32_t game, int32_t player, int32_t *out, int64_t cap, int64_t *count);
+
+/* ---------------------------------------------------------------- autotuner
+ * Chooses the options that only change the time of a solve, never its
+ * results -- sublist_len (the Helman-JaJa stride the reference fixes at 64,
+ * gpu_list_ranking.cu:19), walk_block (threads per block of the sublist walk,
+ * the reference's fixed launch shape) and patch_limit -- for a workload, by
+ * timing trial solves of that workload on the device: games[0] alone when
+ * count is 1 (psi_solve with base's graph setting), else all count games as
+ * one batch (psi_batch_solve).  Coordinate descent from the defaults over
+ * sublist_len {64,16,32,128,256}, walk_block {128,64,256,512} and
+ * patch_limit max(1024, vertices/d) for d in {64,16,32,128,256} (skipped when
+ * base->incremental is PSI_INCR_OFF); each candidate is one untimed solve and
+ * `repeats` timed ones scored by the least, and replaces the incumbent only
+ * when at least 2% faster.  *out = *base with the three fields chosen.  The
+ * choice is cached in the process by workload shape (device, number of
+ * games, size class of the total vertex count, mean out-degree) and a later
+ * call for the same shape returns it without timing (report->cached = 1),
+ * unless flags has PSI_TUNE_NO_CACHE.  Builds and frees one solver per
+ * candidate: run it before timing-sensitive work.  No counterpart in the
+ * reference. */
+typedef struct {
+    int32_t candidates;   /* option sets timed (0 when the choice came from the cache) */
+    int32_t solves;       /* solves run, each candidate's untimed first solve included */
+    int32_t cached;       /* 1: taken from this process's cache, nothing timed */
+    int32_t reserved;
+    double default_ms;    /* least time of one solve with the default stride, walk block, patch limit */
+    double best_ms;       /* least time of one solve with the chosen ones */
+} psi_tune_report;
+enum { PSI_TUNE_NO_CACHE = 1 };
+int psi_autotune(const psi_game *const *games, int32_t count, const psi_options *base, int32_t repeats,
+                 int32_t flags, psi_options *out, psi_tune_report *report);
 
 /* ------------------------------------------------------ solution certificate
  * Checks a solution independently of how it was computed (no counterpart in

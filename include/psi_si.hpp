@@ -208,6 +208,21 @@ inline int check_solution(const Game &g, const std::vector<int32_t> &strategy, c
     return r.status;
 }
 
+// Options for a workload (one game, or several solved as a Batch) chosen by
+// timing trial solves on the device (psi_autotune); base supplies the device
+// and the options that are not tuned (nullptr: the defaults).
+inline psi_options autotune(const std::vector<const Game *> &games, const psi_options *base = nullptr,
+                            int32_t repeats = 2, psi_tune_report *report = nullptr, int32_t flags = 0)
+{
+    std::vector<const psi_game *> hs;
+    for (const Game *g : games) hs.push_back(g->handle());
+    psi_options out;
+    psi_tune_report r;
+    check(psi_autotune(hs.data(), (int32_t)hs.size(), base, repeats, flags, &out, &r));
+    if (report) *report = r;
+    return out;
+}
+
 // Many games solved together (psi_batch_*); each ends with its solo results.
 class Batch {
 public:

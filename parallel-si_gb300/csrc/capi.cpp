@@ -15,6 +15,7 @@
 #include "psi_internal.h"
 #include "serve.h"
 #include "solver.h"
+#include "tune.h"
 
 struct psi_game {
     psi::HostGame g;
@@ -495,6 +496,31 @@ int psi_batch_get_winning(psi_batch *b, int32_t game, int32_t player, int32_t *o
     }
     if (count) *count = k;
     return PSI_OK;
+    PSI_GUARD_END
+}
+
+int psi_measure_random_access(int32_t device, int64_t array_bytes, int32_t reps, double *gathers_per_s,
+                              double *ms_per_launch, int64_t *gathers_per_launch)
+{
+    PSI_GUARD_BEGIN
+    return psi::measure_random_access(device, array_bytes, reps, gathers_per_s, ms_per_launch, gathers_per_launch);
+    PSI_GUARD_END
+}
+
+int psi_autotune(const psi_game *const *games, int32_t count, const psi_options *base, int32_t repeats,
+                 int32_t flags, psi_options *out, psi_tune_report *report)
+{
+    if (!games || count <= 0 || !out || !report) return psi::fail(PSI_ERR_INVALID, "null or empty argument");
+    PSI_GUARD_BEGIN
+    std::vector<const psi::HostGame *> gs;
+    for (int32_t k = 0; k < count; k++) {
+        if (!games[k]) return psi::fail(PSI_ERR_INVALID, "null game in workload");
+        gs.push_back(&games[k]->g);
+    }
+    psi_options o;
+    psi_options_default(&o);
+    if (base) o = *base;
+    return psi::autotune(gs, o, repeats, flags, out, report);
     PSI_GUARD_END
 }
 

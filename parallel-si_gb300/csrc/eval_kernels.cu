@@ -681,13 +681,14 @@ int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const ui
 }
 
 void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, int32_t stride, const int32_t *succ,
-                          int2 *vloc, int2 *red, uint32_t *err, const int32_t *gate)
+                          int2 *vloc, int2 *red, uint32_t *err, const int32_t *gate, int block)
 {
     count_launch();
     if ((stride & (stride - 1)) == 0)
-        k_walk_sublists<true><<<grid_for(nsub, 128), 128, 0, s>>>(nsub, n, L, stride, succ, vloc, red, err, gate);
+        k_walk_sublists<true><<<grid_for(nsub, block), block, 0, s>>>(nsub, n, L, stride, succ, vloc, red, err, gate);
     else
-        k_walk_sublists<false><<<grid_for(nsub, 128), 128, 0, s>>>(nsub, n, L, stride, succ, vloc, red, err, gate);
+        k_walk_sublists<false><<<grid_for(nsub, block), block, 0, s>>>(nsub, n, L, stride, succ, vloc, red, err,
+                                                                      gate);
 }
 
 int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, int2 *b, const int2 **fin,

@@ -122,8 +122,11 @@ int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const ui
                        int32_t *sinklist, int32_t *sinkcount, int32_t *dlist, int32_t *dcount,
                        const int32_t *gate = nullptr, const uint8_t *tie = nullptr, uint8_t *need = nullptr);
 // Sublist walks; heads are the nodes j*stride (j < nsub-1) and the list start.
+// One thread per sublist, `block` threads per block (a multiple of 32, <= 1024).
+constexpr int kWalkBlock = 128;
 void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, int32_t stride, const int32_t *succ,
-                          int2 *vloc, int2 *red, uint32_t *err, const int32_t *gate = nullptr);
+                          int2 *vloc, int2 *red, uint32_t *err, const int32_t *gate = nullptr,
+                          int block = kWalkBlock);
 // Ranks the reduced list red[0..nsub) (next, weight) by Wyllie pointer jumping
 // (cooperative launch; a, b: nsub entries each).  *fin is set to the buffer
 // that will hold, per item, (TOUR_END if the list start reaches it, else >= 0;

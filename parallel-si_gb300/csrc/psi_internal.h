@@ -22,6 +22,10 @@ int gen_longpath(int32_t n, int32_t pri_hi, uint64_t seed, int32_t *owner, int32
 int gen_batch_sizes(int32_t count, int32_t n_lo, int32_t n_hi, uint64_t seed, int32_t *sizes);
 uint64_t gen_game_seed(uint64_t seed, int32_t index);
 
+// psi_measure_random_access (measure.cu)
+int measure_random_access(int32_t device, int64_t array_bytes, int32_t reps, double *gathers_per_s,
+                          double *ms_per_launch, int64_t *gathers_per_launch);
+
 }  // namespace psi
 
 #endif

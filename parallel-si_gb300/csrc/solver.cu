@@ -37,6 +37,8 @@ int check_options(const psi_options &opt)
     if (opt.incremental < PSI_INCR_OFF || opt.incremental > PSI_INCR_ALWAYS)
         return fail(PSI_ERR_INVALID, "unknown incremental mode");
     if (opt.patch_limit < 0) return fail(PSI_ERR_INVALID, "patch_limit must be >= 0");
+    if (opt.walk_block != 0 && (opt.walk_block < 32 || opt.walk_block > 1024 || opt.walk_block % 32 != 0))
+        return fail(PSI_ERR_INVALID, "walk_block must be 0 or a multiple of 32 in [32, 1024]");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0) return fail(PSI_ERR_NO_DEVICE, "no CUDA device available");
@@ -60,6 +62,7 @@ int Solver::create(const CsrView &g, const psi_options &opt, Solver **out, bool 
     s->use_graph_ = opt.graph != 0;
     s->incremental_ = opt.incremental;
     s->patch_limit_ = opt.patch_limit;
+    s->walk_block_ = opt.walk_block ? opt.walk_block : kWalkBlock;
     rc = s->alloc_arrays(g.n, g.m);
     if (!rc) rc = s->upload_game(g, validate);
     if (rc) {
@@ -86,6 +89,7 @@ int Solver::create_arena(int64_t max_vertices, int64_t max_edges, int32_t slots,
     // admissions list their new vertices as changed ones: a patch evaluates them
     s->incremental_ = opt.incremental;
     s->patch_limit_ = opt.patch_limit;
+    s->walk_block_ = opt.walk_block ? opt.walk_block : kWalkBlock;
     rc = s->alloc_arrays(max_vertices, max_edges);
     if (!rc) rc = s->init_arena(slots);
     if (rc) {
@@ -133,6 +137,7 @@ int Solver::create_union(const std::vector<const HostGame *> &gs, const psi_opti
     s->use_graph_ = opt.graph != 0;
     s->incremental_ = opt.incremental;
     s->patch_limit_ = opt.patch_limit;
+    s->walk_block_ = opt.walk_block ? opt.walk_block : kWalkBlock;
     rc = s->alloc_arrays(n, m);
     if (!rc) rc = s->upload_union(gs, table, base->back());
     if (rc) {
@@ -539,7 +544,8 @@ int Solver::enqueue_full(bool timed)
     end(PH_TOUR);
     // 2. Helman-JaJa sublists, then the reduced list ranked on the device
     begin(PH_SUBLIST);
-    launch_walk_sublists(stream_, nsub_, n_, L_, stride_, succ_, vloc_, redA_, &dw_->err, &ctl_->eval);
+    launch_walk_sublists(stream_, nsub_, n_, L_, stride_, succ_, vloc_, redA_, &dw_->err, &ctl_->eval,
+                         walk_block_);
     end(PH_SUBLIST);
     begin(PH_REDUCED);
     const int2 *fin = nullptr;

@@ -199,6 +199,7 @@ private:
     // list, the re-evaluated set and its positions, the jump entries
     int32_t incremental_ = 1;   // psi_options.incremental
     int32_t patch_limit_ = 0;   // psi_options.patch_limit
+    int32_t walk_block_ = kWalkBlock;   // psi_options.walk_block (0 there: kWalkBlock)
     int32_t *clist_ = nullptr, *alist_ = nullptr, *apos_ = nullptr;
     int4 *pj_ = nullptr;
     int32_t ccap_ = 0, acap_ = 0, max_levels_ = 0;

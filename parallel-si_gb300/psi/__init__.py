@@ -21,7 +21,7 @@ def launch_count() -> int:
     """Kernel launches issued by the native library in this process."""
     return int(lib.psi_launch_count())
 
-__all__ = ["Game", "GPUList", "Batch", "Server", "PsiError", "Options", "solve_si", "batch_sizes", "shard_games", "check_solution", "default_options", "version"]
+__all__ = ["Game", "GPUList", "Batch", "Server", "PsiError", "Options", "solve_si", "batch_sizes", "shard_games", "check_solution", "default_options", "autotune", "measure_random_access", "version"]
 
 
 def version() -> str:
@@ -306,6 +306,37 @@ def batch_sizes(count: int, n_lo: int, n_hi: int, seed: int = 1) -> np.ndarray:
     out = np.empty(count, np.int32)
     check(lib.psi_generate_batch_sizes(count, n_lo, n_hi, C.c_uint64(seed), ptr(out)))
     return out
+
+
+def measure_random_access(device: int = 0, array_bytes: int = 1 << 30, reps: int = 10) -> dict:
+    """The random-access bound (psi_measure_random_access): independent
+    4-byte loads per second from random positions of a device array."""
+    g = C.c_double()
+    ms = C.c_double()
+    k = C.c_int64()
+    check(lib.psi_measure_random_access(int(device), int(array_bytes), int(reps), C.byref(g), C.byref(ms),
+                                        C.byref(k)))
+    return {"G_per_s": g.value / 1e9, "sector_GBps": g.value * 32 / 1e9, "ms": ms.value, "loads": k.value}
+
+
+def autotune(games, repeats: int = 2, no_cache: bool = False, options: Optional[Options] = None, **kw):
+    """Options for a workload chosen by timing trial solves on the device
+    (psi_autotune): sublist_len, walk_block and patch_limit, which change the
+    time of a solve and never its results.  `games` is one Game (solved alone)
+    or a list of Games (solved as one Batch).  The other options come from
+    `options` or the keywords.  Returns (Options, report dict)."""
+    from ._lib import TuneReport
+    gs = [games] if isinstance(games, Game) else list(games)
+    base = options if options is not None else default_options(**kw)
+    handles = (C.c_void_p * len(gs))(*[g._h.value for g in gs])
+    out = Options()
+    r = TuneReport()
+    check(lib.psi_autotune(C.cast(handles, C.c_void_p), len(gs), C.byref(base), int(repeats), 1 if no_cache else 0,
+                           C.byref(out), C.byref(r)))
+    rep = {"candidates": r.candidates, "solves": r.solves, "cached": bool(r.cached), "default_ms": r.default_ms,
+           "best_ms": r.best_ms, "sublist_len": out.sublist_len, "walk_block": out.walk_block,
+           "patch_limit": out.patch_limit}
+    return out, rep
 
 
 CHECK_STATUS = {0: "ok", 1: "bad strategy", 2: "not closed", 3: "not a trap", 4: "bad cycle", 5: "incomplete"}

@@ -38,6 +38,11 @@ class CheckReport(C.Structure):
     _fields_ = [("status", C.c_int32), ("reserved", C.c_int32), ("vertex", C.c_int64), ("edge_visits", C.c_int64)]
 
 
+class TuneReport(C.Structure):
+    _fields_ = [("candidates", C.c_int32), ("solves", C.c_int32), ("cached", C.c_int32), ("reserved", C.c_int32),
+                ("default_ms", C.c_double), ("best_ms", C.c_double)]
+
+
 class Options(C.Structure):
     _fields_ = [
         ("device", C.c_int32),
@@ -47,7 +52,7 @@ class Options(C.Structure):
         ("graph", C.c_int32),
         ("incremental", C.c_int32),
         ("patch_limit", C.c_int32),
-        ("reserved", C.c_int32 * 1),
+        ("walk_block", C.c_int32),
     ]
 
 
@@ -114,6 +119,10 @@ _SIGS = {
     "psi_batch_get_strategy": ([_vp, C.c_int32, _vp], C.c_int),
     "psi_batch_get_winning": ([_vp, C.c_int32, C.c_int32, _vp, C.c_int64, _i64p], C.c_int),
     "psi_check_solution": ([_vp, _vp, _vp, C.c_int64, C.POINTER(CheckReport)], C.c_int),
+    "psi_measure_random_access": ([C.c_int32, C.c_int64, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                   _i64p], C.c_int),
+    "psi_autotune": ([_vp, C.c_int32, C.POINTER(Options), C.c_int32, C.c_int32, C.POINTER(Options),
+                      C.POINTER(TuneReport)], C.c_int),
     "psi_server_create": ([C.c_int64, C.c_int64, C.c_int32, C.c_int32, C.POINTER(Options), _pp], C.c_int),
     "psi_server_destroy": ([_vp], None),
     "psi_server_submit": ([_vp, _vp, _i64p], C.c_int),
