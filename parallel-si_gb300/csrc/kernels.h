@@ -181,9 +181,10 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
                    int32_t *list_count = nullptr, ChangeList changes = ChangeList(), uint8_t *tie = nullptr,
                    uint8_t *watch = nullptr, const int4 *skip = nullptr);
 // ---- batches: per-game accounting of solve_si (state[g] = brs, iters,
-// odd_done, done; gcount[g] = strict improvements of the last switch step)
+// odd_done, done; gcount[g] = strict improvements of the last switch step);
+// with gate, only when *gate is set
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state,
-                          unsigned long long *gcount);
+                          unsigned long long *gcount, const int32_t *gate = nullptr);
 // ---- serving arena (serve_kernels.cu)
 // Places the games of one admission, uploaded as a packed union (game k owns
 // union vertices [ub[k], ub[k+1]); u_roff/u_rsrc: the union's reverse CSR), at

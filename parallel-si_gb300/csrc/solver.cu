@@ -819,7 +819,18 @@ int Solver::solve(int32_t reset, int32_t *iters, int32_t *brs, int64_t max_evals
 // (launch_batch_account): the union's loops end when no game switches.
 int Solver::solve_batch(int32_t *iters, int32_t *brs)
 {
-    if (!games_) return fail(PSI_ERR_STATE, "not a batch");
+    if (!games_ || arena_) return fail(PSI_ERR_STATE, "not a batch");
+    if (use_graph_) {   // the default: the whole loop as one graph launch
+        std::vector<int4> st;
+        int rc = solve_batch_graph(st);
+        if (rc) return rc;
+        for (int32_t k = 0; k < games_; k++) {
+            brs[k] = st[k].x;
+            iters[k] = st[k].y;
+            if (!st[k].w) return fail(PSI_ERR_STATE, "batch loop ended with an unfinished game");
+        }
+        return PSI_OK;
+    }
     int rc = init_strat();
     if (rc) return rc;
     PSI_CUDA_TRY(cudaMemsetAsync(gstate_, 0, 16 * (size_t)games_, stream_));

@@ -101,7 +101,8 @@ public:
     // Batches (create_union): the solver's game is a disjoint union of games,
     // game g owning vertices [base[g], base[g+1]).  solve_batch runs solve_si
     // over the union and returns each game's own iteration and evaluation
-    // counts.
+    // counts: as one graph launch (psi_options.graph, the default) or through
+    // the host-driven loop.
     int solve_batch(int32_t *iters, int32_t *brs);
     int32_t batch_games() const { return games_; }
 
@@ -214,7 +215,9 @@ private:
         int32_t cnt[3];             // active-list counters of the cycle kernel
     };
     Words *dw_ = nullptr, *hw_ = nullptr;
-    // graph-driven solve loop
+    // graph-driven solve loop (solver_graph.cu)
+    int run_graph(bool reset, int64_t max_evals, GraphCtl *out, int4 *gstate_out);
+    int solve_batch_graph(std::vector<int4> &state);
     bool use_graph_ = false, graph_reset_ = false;
     GraphCtl *ctl_ = nullptr;
     cudaGraph_t graph_ = nullptr;

@@ -121,27 +121,37 @@ int Solver::enqueue_step(cudaGraph_t body, cudaGraphConditionalHandle loop, bool
     if (rc) return abort_capture(rc);
     PSI_CUDA_TRY(cudaStreamEndCapture(stream_, &g));
 
-    // (C)
+    // (C); a batch also advances every game's own solve_si counts
+    // (k_batch_account, at the points where the host loop calls it), and its
+    // switch steps add each game's strict improvements to gcount_
+    const bool batch = games_ > 0 && !arena_;
     PSI_CUDA_TRY(cudaStreamBeginCaptureToGraph(stream_, body, &ifnode, nullptr, 1, mode));
     count_launch();
     k_ctl_evaluated<<<1, 1, 0, stream_>>>(ctl_);
+    if (batch) launch_batch_account(stream_, games_, 0, gstate_, gcount_);
     // Odd: mark_solved(1), switch(1)
     launch_mark_solved(stream_, &dw_->ucount, ulist_, 1, st_, solved_, dirty_, nullptr, nullptr, nullptr,
                        &ctl_->mfrom[1], &ctl_->mdone);
     e = cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_);
     if (e != cudaSuccess) return abort_capture(fail(PSI_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e)));
     int32_t *todo = reinterpret_cast<int32_t *>(jB_);   // free until the next cycle pass
-    launch_switch(stream_, np_ - np0_, plist_ + np0_, 1, off_, tgt_, strat_, st_, key_, node_, dw_->sw, nullptr,
-                  nullptr, nullptr, dirty_, &dw_->err, nullptr, need_, todo, &dw_->cnt[2], changes(), tie_, watch_, skip_);
+    unsigned long long *gc = batch ? gcount_ : nullptr;
+    launch_switch(stream_, np_ - np0_, plist_ + np0_, 1, off_, tgt_, strat_, st_, key_, node_, dw_->sw,
+                  batch ? game_of_ : nullptr, gc, nullptr, dirty_, &dw_->err, nullptr, need_, todo, &dw_->cnt[2],
+                  changes(), tie_, watch_, skip_);
+    if (batch) launch_batch_account(stream_, games_, 1, gstate_, gcount_);
     count_launch();
     k_ctl_odd<<<1, 1, 0, stream_>>>(ctl_, dw_->sw);
     // Even, when Odd made no strict improvement: mark_solved(0), switch(0)
     launch_mark_solved(stream_, &dw_->ucount, ulist_, 0, st_, solved_, dirty_, nullptr, nullptr, &ctl_->even,
                        &ctl_->mfrom[0], &ctl_->mdone);
+    if (batch) launch_batch_account(stream_, games_, 2, gstate_, gcount_, &ctl_->even);
     e = cudaMemsetAsync(dw_->sw, 0, sizeof(dw_->sw), stream_);
     if (e != cudaSuccess) return abort_capture(fail(PSI_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e)));
-    launch_switch(stream_, np0_, plist_, 0, off_, tgt_, strat_, st_, key_, node_, dw_->sw, nullptr, nullptr, nullptr,
-                  dirty_, &dw_->err, &ctl_->even, need_, todo, &dw_->cnt[2], changes(), tie_, watch_, skip_);
+    launch_switch(stream_, np0_, plist_, 0, off_, tgt_, strat_, st_, key_, node_, dw_->sw,
+                  batch ? game_of_ : nullptr, gc, nullptr, dirty_, &dw_->err, &ctl_->even, need_, todo,
+                  &dw_->cnt[2], changes(), tie_, watch_, skip_);
+    if (batch) launch_batch_account(stream_, games_, 3, gstate_, gcount_, &ctl_->even);
     count_launch();
     k_ctl_even<<<1, 1, 0, stream_>>>(ctl_, dw_->sw, loop, reset ? 1 : 0, kEvalGuard);
     e = cudaGetLastError();
@@ -180,14 +190,16 @@ int Solver::build_graph(bool reset)
     return PSI_OK;
 }
 
-// solve_si as one graph launch; the same results and counts as solve().
-int Solver::solve_graph(int32_t reset, int32_t *iters, int32_t *brs, int64_t max_evals)
+// One graph launch of the solve loop from init_strat; *out receives the
+// loop's control words at the end.  With gstate_out (a batch), the per-game
+// states are read back in the same synchronisation.
+int Solver::run_graph(bool reset, int64_t max_evals, GraphCtl *out, int4 *gstate_out)
 {
     int rc = init_strat();
     if (rc) return rc;
     const unsigned long long patches_before = hw_->patch[0];   // as of init_strat's synchronisation
-    if (!graph_exec_ || graph_reset_ != (reset != 0)) {
-        rc = build_graph(reset != 0);
+    if (!graph_exec_ || graph_reset_ != reset) {
+        rc = build_graph(reset);
         if (rc) return rc;
     }
     GraphCtl init;
@@ -197,24 +209,48 @@ int Solver::solve_graph(int32_t reset, int32_t *iters, int32_t *brs, int64_t max
     init.max_evals = max_evals > 0 && max_evals < INT32_MAX ? (int32_t)max_evals : 0;
     PSI_CUDA_TRY(cudaMemcpyAsync(ctl_, &init, sizeof init, cudaMemcpyHostToDevice, stream_));
     PSI_CUDA_TRY(cudaGraphLaunch(graph_exec_, stream_));
-    GraphCtl out;
-    PSI_CUDA_TRY(cudaMemcpyAsync(&out, ctl_, sizeof out, cudaMemcpyDeviceToHost, stream_));
+    PSI_CUDA_TRY(cudaMemcpyAsync(out, ctl_, sizeof *out, cudaMemcpyDeviceToHost, stream_));
+    if (gstate_out)
+        PSI_CUDA_TRY(cudaMemcpyAsync(gstate_out, gstate_, sizeof(int4) * (size_t)games_, cudaMemcpyDeviceToHost,
+                                     stream_));
     rc = sync_and_check("solve (graph)");
     if (rc) return rc;
-    *iters = out.iters;
-    *brs = out.brs;
     // every pass launches each kernel of the body once, those of the full
     // evaluation only when it is not a patch
     const long long patched = (long long)(hw_->patch[0] - patches_before);
-    add_launches((graph_step_launches_ - graph_full_launches_) * out.brs +
-                 graph_full_launches_ * (out.brs - patched));
-    times_.evals += out.brs;
-    times_.switches += out.brs + out.iters;
+    add_launches((graph_step_launches_ - graph_full_launches_) * out->brs +
+                 graph_full_launches_ * (out->brs - patched));
+    times_.evals += out->brs;
+    times_.switches += out->brs + out->iters;
     val_ready_ = true;
     tour_valid_ = true;
-    if (out.stop == GraphCtl::kEvalCap) return fail(PSI_ERR_LIMIT, "evaluation cap reached");
-    if (out.stop != GraphCtl::kConverged) return fail(PSI_ERR_LIMIT, "graph solve loop stopped by its guard");
+    if (out->stop == GraphCtl::kEvalCap) return fail(PSI_ERR_LIMIT, "evaluation cap reached");
+    if (out->stop != GraphCtl::kConverged) return fail(PSI_ERR_LIMIT, "graph solve loop stopped by its guard");
     return PSI_OK;
+}
+
+// solve_si as one graph launch; the same results and counts as solve().
+int Solver::solve_graph(int32_t reset, int32_t *iters, int32_t *brs, int64_t max_evals)
+{
+    GraphCtl out;
+    int rc = run_graph(reset != 0, max_evals, &out, nullptr);
+    if (rc) return rc;
+    *iters = out.iters;
+    *brs = out.brs;
+    return PSI_OK;
+}
+
+// A batch's solve_si loops as one graph launch: the union's loop ends when no
+// game switches (a device-side decision, as for one game); every game's own
+// counts come from its state in gstate_.  The same results and counts as
+// the host-driven solve_batch.
+int Solver::solve_batch_graph(std::vector<int4> &state)
+{
+    PSI_CUDA_TRY(cudaMemsetAsync(gstate_, 0, sizeof(int4) * (size_t)games_, stream_));
+    PSI_CUDA_TRY(cudaMemsetAsync(gcount_, 0, sizeof(unsigned long long) * (size_t)games_, stream_));
+    state.assign((size_t)games_, int4{});
+    GraphCtl out;
+    return run_graph(false, 0, &out, state.data());
 }
 
 }  // namespace psi

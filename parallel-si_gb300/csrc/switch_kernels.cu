@@ -355,8 +355,9 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
 //   event 3: after switch(Even) -> a game whose Even made no improvement is done; the others
 //                                  re-enter their best-response loop
 __global__ void k_batch_account(int32_t games, int32_t event, int4 *__restrict__ state,
-                                unsigned long long *__restrict__ gcount)
+                                unsigned long long *__restrict__ gcount, const int32_t *__restrict__ gate)
 {
+    if (gate && !*gate) return;   // graph-driven loop: Even's events only when Even moves
     int32_t g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= games) return;
     int4 s = state[g];
@@ -441,11 +442,12 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
                                   gmask, dirty, err, gate, need, changes, tie, watch, skip);
 }
 
-void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state, unsigned long long *gcount)
+void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state, unsigned long long *gcount,
+                          const int32_t *gate)
 {
     if (games <= 0) return;
     count_launch();
-    k_batch_account<<<grid_for(games), kBlock, 0, s>>>(games, event, state, gcount);
+    k_batch_account<<<grid_for(games), kBlock, 0, s>>>(games, event, state, gcount, gate);
 }
 
 void launch_materialize(cudaStream_t s, int32_t v0, int32_t count, int32_t d, const int32_t *st,

@@ -88,3 +88,24 @@ def test_batch_of_mixed_families_and_tiny_games_matches_oracle():
         o.close()
     single = psi.Batch([games[2]])
     assert tuple(single.solve()[0]) == (it[2],)
+
+
+@pytest.mark.gpu
+def test_batch_graph_loop_matches_host_loop():
+    """The default batch solve is one CUDA graph launch (device-side loop
+    control and per-game accounting); the host-driven loop (graph=0) must
+    give every game the same counts, strategy and winning sets."""
+    games = c4_games(30, 30, 20000, 13) + [psi.Game.longpath(700, 32, 4), psi.Game.random(2, 1, 1, 2, 5)]
+    g = psi.Batch(games)
+    h = psi.Batch(games, graph=0)
+    it_g, br_g = g.solve()
+    it_h, br_h = h.solve()
+    assert np.array_equal(it_g, it_h) and np.array_equal(br_g, br_h)
+    for k in range(len(games)):
+        assert np.array_equal(g.get_strategy(k), h.get_strategy(k)), f"game {k}"
+        assert np.array_equal(g.get_winning(k, 0), h.get_winning(k, 0)), f"game {k}"
+    # a second graph solve starts from fresh per-game states
+    it2, br2 = g.solve()
+    assert np.array_equal(it2, it_g) and np.array_equal(br2, br_g)
+    g.close()
+    h.close()
