@@ -193,7 +193,8 @@ int64_t psi_launch_count(void);
  * `device`,
  * eight in flight per thread with every SM filled, about 2^27 loads per
  * launch; reports the median of `reps` launches (after two untimed ones) as
- * loads per second.  Each such load moves a whole 32-byte sector, so this is
+ * loads per second; the calling thread's current device is restored on
+ * return.  Each such load moves a whole 32-byte sector, so this is
  * the ceiling for the data-dependent reads of the sublist walks, the
  * root-summary walks and the switch's key gathers, beside the copy bandwidth
  * that bounds streaming kernels; measured at the size of the array a kernel
@@ -248,11 +249,12 @@ int psi_batch_get_winning(psi_batch *b, int32_t game, int32_t player, int32_t *o
  * `repeats` timed ones scored by the least, and replaces the incumbent only
  * when at least 2% faster.  *out = *base with the three fields chosen.  The
  * choice is cached in the process by workload shape (device, number of
- * games, size class of the total vertex count, mean out-degree) and a later
- * call for the same shape returns it without timing (report->cached = 1),
- * unless flags has PSI_TUNE_NO_CACHE.  Builds and frees one solver per
- * candidate: run it before timing-sensitive work.  No counterpart in the
- * reference. */
+ * games, size class of the total vertex count, mean out-degree, graph,
+ * incremental) and a later call for the same shape returns it without
+ * timing (report->cached = 1), unless flags has PSI_TUNE_NO_CACHE.  Builds
+ * and frees one solver per candidate (a candidate that runs out of device
+ * memory is skipped): run it before timing-sensitive work.  No counterpart
+ * in the reference. */
 typedef struct {
     int32_t candidates;   /* option sets timed (0 when the choice came from the cache) */
     int32_t solves;       /* solves run, each candidate's untimed first solve included */

@@ -61,6 +61,9 @@ __global__ void __launch_bounds__(kGatherBlock) k_random_gather(const int32_t *_
     sink[tid] = acc;
 }
 
+int measure_on_current(int32_t device, int64_t array_bytes, int32_t reps, double *gathers_per_s,
+                       double *ms_per_launch, int64_t *gathers_per_launch);
+
 }  // namespace
 
 int measure_random_access(int32_t device, int64_t array_bytes, int32_t reps, double *gathers_per_s,
@@ -72,7 +75,19 @@ int measure_random_access(int32_t device, int64_t array_bytes, int32_t reps, dou
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(PSI_ERR_NO_DEVICE, "no CUDA device available");
     if (device < 0 || device >= ndev) return fail(PSI_ERR_INVALID, "device ordinal out of range");
+    int prev = 0;
+    PSI_CUDA_TRY(cudaGetDevice(&prev));
     PSI_CUDA_TRY(cudaSetDevice(device));
+    const int rc = measure_on_current(device, array_bytes, reps, gathers_per_s, ms_per_launch, gathers_per_launch);
+    cudaSetDevice(prev);   // the caller's current device, as it was
+    return rc;
+}
+
+namespace {
+
+int measure_on_current(int32_t device, int64_t array_bytes, int32_t reps, double *gathers_per_s,
+                       double *ms_per_launch, int64_t *gathers_per_launch)
+{
     int sms = 0, per_sm = 0;
     PSI_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
     PSI_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_random_gather, kGatherBlock, 0));
@@ -124,5 +139,7 @@ int measure_random_access(int32_t device, int64_t array_bytes, int32_t reps, dou
     if (gathers_per_launch) *gathers_per_launch = loads;
     return PSI_OK;
 }
+
+}  // namespace
 
 }  // namespace psi

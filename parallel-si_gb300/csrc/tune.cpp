@@ -16,8 +16,10 @@
 // by the least.  A candidate replaces the incumbent only when it is at least
 // 2% faster, so timing noise does not move the choice.  Choices are cached in
 // the process by workload shape (device, number of games, size class of the
-// total vertex count, mean out-degree): a later call for a workload of the
-// same shape returns the cached choice without timing anything.
+// total vertex count, mean out-degree, graph loop, incremental mode): a
+// later call for a workload of the same shape returns the cached choice
+// without timing anything.  A candidate that runs out of device memory is
+// skipped (the defaults are always timed first).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -57,7 +59,8 @@ struct Choice {
     double default_ms, best_ms;
 };
 
-using Key = std::tuple<int32_t, int32_t, int32_t, int32_t>;   // device, games class, size class, degree x4
+// device, games class, size class, mean degree x4, graph loop, incremental mode
+using Key = std::tuple<int32_t, int32_t, int32_t, int32_t, int32_t, int32_t>;
 
 std::mutex g_mu;
 std::map<Key, Choice> g_cache;
@@ -116,7 +119,8 @@ int autotune(const std::vector<const HostGame *> &gs, const psi_options &base, i
         m += g->m;
     }
     const Key key{base.device, bit_length((int64_t)gs.size() - 1), bit_length(n),
-                  n > 0 ? (int32_t)std::lround(4.0 * (double)m / (double)n) : 0};
+                  n > 0 ? (int32_t)std::lround(4.0 * (double)m / (double)n) : 0, base.graph != 0 ? 1 : 0,
+                  base.incremental};
     const bool patches = base.incremental != PSI_INCR_OFF;
     auto finish = [&](const Choice &c) {
         *out = base;
@@ -156,6 +160,7 @@ int autotune(const std::vector<const HostGame *> &gs, const psi_options &base, i
             c.*field = v;
             double ms = 0.0;
             int e = time_candidate(gs, options_of(c), repeats, &ms, &rep->solves);
+            if (e == PSI_ERR_NOMEM) continue;   // this candidate does not fit beside the caller's data
             if (e) return e;
             rep->candidates++;
             if (ms < 0.98 * cur.best_ms) {

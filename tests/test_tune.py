@@ -118,3 +118,15 @@ def test_batch_tuning_keeps_every_game_exact():
         assert np.array_equal(b.get_winning(k, 0), ref.get_winning(k, 0)), f"game {k}"
     b.close()
     ref.close()
+
+
+@pytest.mark.gpu
+def test_cache_tells_loop_and_incremental_modes_apart():
+    g = psi.Game.random(4000, 2, 5, 4000, 26)
+    _, rep = psi.autotune(g, repeats=1, no_cache=True)
+    assert not rep["cached"]
+    assert psi.autotune(g, repeats=1)[1]["cached"]
+    # the host-driven loop and full evaluations only time differently: tuned apart
+    assert not psi.autotune(g, repeats=1, graph=0)[1]["cached"]
+    assert not psi.autotune(g, repeats=1, incremental=0)[1]["cached"]
+    assert psi.autotune(g, repeats=1, graph=0)[1]["cached"]
