@@ -618,7 +618,18 @@ def run_serve(args, rank, world, local):
     sizes = psi.batch_sizes(args.serve_games, args.serve_lo, args.serve_hi, args.seed)
     mine = psi.shard_games(sizes.astype(np.int64) + 1, world)[rank]
     games = [psi.Game.random(int(sizes[i]), 2, 8, int(sizes[i]), args.seed * 100003 + int(i)) for i in mine]
-    srv = psi.Server(args.arena_vertices, 8 * args.arena_vertices, args.serve_slots, device=local)
+    # launch options from the autotuner, timed on every 8th game of this
+    # rank's share solved as one batch, unless --no-tune; the patch limit is
+    # carried over as its fraction of the vertices (the arena's, here)
+    tuning = None
+    knobs = dict(sublist_len=args.sublist_len, patch_limit=args.patch_limit, walk_block=args.walk_block)
+    if not args.no_tune:
+        o, tuning = psi.autotune(games[::8], repeats=1, device=local)
+        sample = sum(g.n for g in games[::8])
+        div = int(round(sample / o.patch_limit)) if o.patch_limit > 1024 else 0
+        knobs = dict(sublist_len=o.sublist_len, walk_block=o.walk_block,
+                     patch_limit=max(1024, args.arena_vertices // div) if div in (16, 32, 64, 128, 256) else 0)
+    srv = psi.Server(args.arena_vertices, 8 * args.arena_vertices, args.serve_slots, device=local, **knobs)
     warm = games[: max(4, len(games) // 16)]
     for _ in range(args.warmup):
         serve_once(srv, warm, np.zeros(len(warm)))
@@ -654,7 +665,8 @@ def run_serve(args, rank, world, local):
                    "arena_vertices": args.arena_vertices,
                    "arena_edges": 8 * args.arena_vertices, "max_games": args.serve_slots,
                    "total_vertices": int(sizes.astype(np.int64).sum()),
-                   "parallelism": f"games sharded by footprint over {world} rank(s), one server each"},
+                   "parallelism": f"games sharded by footprint over {world} rank(s), one server each",
+                   **knobs, "tuning": tuning},
         "saturated": {"games_per_s": sat, "p50_ms": dist.max(1000 * float(np.percentile(lat, 50))),
                       "p99_ms": dist.max(1000 * float(np.percentile(lat, 99))), "steps": int(dist.max(steps)),
                       "mean_resident_games": dist.sum(mres)},
