@@ -628,7 +628,7 @@ def run_serve(args, rank, world, local):
         sample = sum(g.n for g in games[::8])
         div = int(round(sample / o.patch_limit)) if o.patch_limit > 1024 else 0
         knobs = dict(sublist_len=o.sublist_len, walk_block=o.walk_block,
-                     patch_limit=max(1024, args.arena_vertices // div) if div in (16, 32, 64, 128, 256) else 0)
+                     patch_limit=max(1024, args.arena_vertices // div) if div in (8, 16, 32, 64, 128, 256) else 0)
     srv = psi.Server(args.arena_vertices, 8 * args.arena_vertices, args.serve_slots, device=local, **knobs)
     warm = games[: max(4, len(games) // 16)]
     for _ in range(args.warmup):

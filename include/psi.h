@@ -244,7 +244,7 @@ int psi_batch_get_winning(psi_batch *b, int32_t game, int32_t player, int32_t *o
  * count is 1 (psi_solve with base's graph setting), else all count games as
  * one batch (psi_batch_solve).  Coordinate descent from the defaults over
  * sublist_len {64,16,32,128,256}, walk_block {128,64,256,512} and
- * patch_limit max(1024, vertices/d) for d in {64,16,32,128,256} (skipped when
+ * patch_limit max(1024, vertices/d) for d in {64,8,16,32,128,256} (skipped when
  * base->incremental is PSI_INCR_OFF); each candidate is one untimed solve and
  * `repeats` timed ones scored by the least, and replaces the incumbent only
  * when at least 2% faster.  *out = *base with the three fields chosen.  The

@@ -45,10 +45,11 @@ const std::vector<int32_t> &tune_walk_blocks()
     return v;
 }
 
-// patch_limit = max(1024, vertices / divisor); 64 is the solver's default
+// patch_limit = max(1024, vertices / divisor); 64 is the solver's default.
+// Beyond vertices/8 a patch gives way to a full evaluation anyway.
 const std::vector<int32_t> &tune_patch_divisors()
 {
-    static const std::vector<int32_t> v = {64, 16, 32, 128, 256};
+    static const std::vector<int32_t> v = {64, 8, 16, 32, 128, 256};
     return v;
 }
 

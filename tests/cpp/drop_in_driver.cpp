@@ -5,6 +5,9 @@
 //   drop_in_driver solve <game.gm>   -> "time iters brs" then the W0 size
 //   drop_in_driver serve <game.gm>   -> the same game through Batch and Server:
 //                                       "iters brs" of each and the certificate status
+//   drop_in_driver tune <game.gm>    -> options from psi::autotune, then solve_si with
+//                                       them: "sublist_len walk_block patch_limit" then
+//                                       "iters brs" 
 #include <chrono>
 #include <cstdio>
 #include <cstring>
@@ -16,7 +19,7 @@
 int main(int argc, char **argv)
 {
     if (argc != 3) {
-        std::printf("usage: %s parse|solve game.gm\n", argv[0]);
+        std::printf("usage: %s parse|solve|serve|tune game.gm\n", argv[0]);
         return 1;
     }
     try {
@@ -39,6 +42,15 @@ int main(int argc, char **argv)
             std::vector<int32_t> strat, inf;
             srv.take(t, strat, inf);
             std::printf("%d %d\n%d %d\n%d\n", bi[0], bb[0], si_, sb, psi::check_solution(g, strat, inf));
+            return 0;
+        }
+        if (std::strcmp(argv[1], "tune") == 0) {
+            psi_tune_report rep;
+            const psi_options o = psi::autotune({&g}, nullptr, 1, &rep);
+            psi::GPUList tuned(g, &o);
+            int it = 0, br = 0;
+            psi::solve_si(tuned, &br, &it, false);
+            std::printf("%d %d %d\n%d %d\n", o.sublist_len, o.walk_block, o.patch_limit, it, br);
             return 0;
         }
         psi::GPUList si(g);

@@ -64,3 +64,16 @@ def test_cpp_batch_server_and_check(driver, tmp_path):
     assert tuple(map(int, lines[0].split())) == it_br    # batch
     assert tuple(map(int, lines[1].split())) == it_br    # server
     assert int(lines[2]) == 0                            # PSI_CHECK_OK
+
+
+@pytest.mark.gpu
+def test_cpp_autotune_then_solve(driver, tmp_path):
+    g = make("c2", 4000, 19)
+    o = oracle.Oracle(*g.csr())
+    it_br = o.solve()
+    o.close()
+    out = subprocess.run([driver, "tune", write_game(tmp_path, g)], capture_output=True, text=True, check=True)
+    lines = out.stdout.split("\n")
+    sub, walk, limit = map(int, lines[0].split())
+    assert sub in (16, 32, 64, 128, 256) and walk in (64, 128, 256, 512) and limit >= 1024
+    assert tuple(map(int, lines[1].split())) == it_br

@@ -15,7 +15,7 @@ from psi._lib import PSI_ERR_INVALID, PSI_ERR_NO_DEVICE, PSI_OK, Options, TuneRe
 
 SUBLIST = {16, 32, 64, 128, 256}
 WALK = {64, 128, 256, 512}
-DIVISORS = (16, 32, 64, 128, 256)
+DIVISORS = (8, 16, 32, 64, 128, 256)
 
 
 def _call(games, count=None, repeats=2, flags=0, base=None):
@@ -68,7 +68,7 @@ def test_tuned_options_solve_identically_and_are_cached():
     o, rep = psi.autotune(g, repeats=2, no_cache=True)
     assert o.sublist_len in SUBLIST and o.walk_block in WALK
     assert o.patch_limit in {max(1024, g.n // d) for d in DIVISORS}
-    assert not rep["cached"] and rep["candidates"] == 1 + 4 + 3 + 4
+    assert not rep["cached"] and rep["candidates"] == 1 + 4 + 3 + 5
     assert rep["solves"] == 3 * rep["candidates"]
     assert 0 < rep["best_ms"] <= rep["default_ms"]
     assert o.graph == 1 and o.incremental == psi.default_options().incremental
