@@ -130,3 +130,15 @@ def test_cache_tells_loop_and_incremental_modes_apart():
     assert not psi.autotune(g, repeats=1, graph=0)[1]["cached"]
     assert not psi.autotune(g, repeats=1, incremental=0)[1]["cached"]
     assert psi.autotune(g, repeats=1, graph=0)[1]["cached"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("text", ["parity -1;\n", "parity 0;\n0 3 0 0;\n", "parity 1;\n0 2 1 1;\n1 1 0 0;\n"])
+def test_tuning_the_smallest_games(text):
+    """The empty game and one- or two-vertex games (self-loops) tune and then
+    solve exactly as with the defaults."""
+    g = psi.Game.parse_text(text)
+    o, rep = psi.autotune(g, repeats=1, no_cache=True)
+    assert rep["candidates"] >= 1 and o.sublist_len in SUBLIST
+    if g.n:
+        assert _same(_solve(g, o), _solve(g, psi.default_options()))
