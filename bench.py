@@ -11,6 +11,14 @@ stream).  e2e repeats the solve through the C ABI from page-locked host buffers
 (psi_host_alloc): upload of the game, the solve, and the read-back of the
 winning set and strategy are inside the timed region.  Prints one JSON line (rank 0).
 
+Before its warm-up the bench lets psi_autotune choose the sublist stride, the
+sublist walk's block size and the patch limit by timing trial solves of the
+same workload (--no-tune takes them from the flags); none of them changes a
+result.  After its timed regions it measures the random-access bound
+(psi_measure_random_access) at the size of the arrays the sublist walk and the
+switch read at random, and reports both kernels against it beside the
+copy-bandwidth roofline.
+
 --impl reference times the reference algorithm's CPU implementation instead:
 the oracle (a C restatement of the reference's CPUParity), single thread, on a
 bounded sample of the same workload (the dense n*(max_pri+1) valuation table of
