@@ -1,0 +1,52 @@
+"""bench.py's output contract on CPU: the reference arm's JSON line (rank 0,
+one process) and the per-launch byte and random-access formulas the roofline
+figures are computed from."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+
+
+def test_reference_arm_prints_one_complete_line():
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "3"], env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    lines = [x for x in r.stdout.splitlines() if x.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == bench.UNIT
+    assert d["higher_is_better"] is True and d["value"] > 0
+    cb = d["cpu_baseline"]
+    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    assert "workload" in d["config"]
+
+
+def test_phase_byte_formulas():
+    n, nsub = 1 << 24, ((2 * (1 << 24) + 1) + 63) // 64 + 1
+    L = 2 * n + 2
+    assert bench.phase_bytes("sublist", n, 0, nsub, None, 1, 0, 0, 0, 0) == 4 * L + 8 * n + 8 * nsub
+    assert bench.phase_bytes("tour", n, 0, nsub, None, 1, 0, 0, 0, 0) == 14 * n
+    assert bench.phase_bytes("broadcast", n, 0, nsub, None, 1, 0, 0, 0, 0) == 69 * n
+    rounds = (nsub - 1).bit_length() + 1
+    assert bench.phase_bytes("reduced", n, 0, nsub, None, 1, 0, 0, 0, 0) == 24 * nsub * rounds
+    c = {"switches": 2, "sw_edges": 1000, "sw_loads": 10, "sw_changed": 7}
+    # one Odd step of 300 vertices and one Even step of 200: (16*500 + 8*1000 + 8*10 + 6*7) / 2
+    assert bench.phase_bytes("switch", n, 0, nsub, c, 2, 200, 300, 1, 1) == (16 * 500 + 8000 + 80 + 42) / 2
+
+
+def test_random_access_formulas():
+    n = 1000
+    assert bench.random_accesses("sublist", n, None, 0, 0, 0, 0) == (2 * n + 2) + n
+    c = {"switches": 2, "sw_edges": 1000, "sw_loads": 10, "sw_changed": 7}
+    assert bench.random_accesses("switch", n, c, 200, 300, 1, 1) == (1000 + 500 + 10 + 14) / 2
+    assert bench.random_accesses("tour", n, c, 200, 300, 1, 1) is None
