@@ -121,3 +121,38 @@ def test_game_from_csr_reports_the_first_bad_vertex():
     owner[2_500_000] = 1
     g = psi.Game.from_csr(owner, pri, off, tg)
     assert (g.n, g.m, g.max_pri) == (n, n, 1)
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The ctypes mirrors of psi_options, psi_tune_report and psi_check_report
+    have the header's field offsets and sizes (compiled with the host C
+    compiler)."""
+    import shutil
+
+    from psi._lib import CheckReport, Options, TuneReport
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    structs = {"psi_options": Options, "psi_tune_report": TuneReport, "psi_check_report": CheckReport}
+    body = []
+    for cname, py in structs.items():
+        body.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            body.append(f'printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stddef.h>\n#include <stdio.h>\n#include \"psi.h\"\nint main(void) {\n"
+                   + "\n".join(body) + "\nreturn 0;\n}\n")
+    exe = tmp_path / "layout"
+    import subprocess
+    subprocess.run([cc, "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    seen = 0
+    for line in out:
+        if not line:
+            continue
+        cname, what, val = line.split()
+        py = structs[cname]
+        expect = C.sizeof(py) if what == "size" else getattr(py, what).offset
+        assert int(val) == expect, line
+        seen += 1
+    assert seen == sum(len(p._fields_) + 1 for p in structs.values())
