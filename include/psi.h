@@ -18,6 +18,7 @@
 #ifndef PSI_H
 #define PSI_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus

@@ -156,3 +156,24 @@ def test_struct_layouts_match_the_header(tmp_path):
         assert int(val) == expect, line
         seen += 1
     assert seen == sum(len(p._fields_) + 1 for p in structs.values())
+
+
+def test_headers_compile_standalone_with_strict_warnings(tmp_path):
+    """include/psi.h is a self-contained C99 header and include/psi_si.hpp a
+    self-contained C++17 header: each compiles as the first include of a
+    translation unit with -Wall -Wextra -Werror -pedantic."""
+    import shutil
+    import subprocess
+
+    inc = os.path.join(ROOT, "include")
+    cc, cxx = shutil.which("gcc"), shutil.which("g++")
+    if cc is None or cxx is None:
+        pytest.skip("no host compilers")
+    c = tmp_path / "h.c"
+    c.write_text('#include "psi.h"\nint main(void) { return PSI_OK; }\n')
+    subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I" + inc, "-c", str(c), "-o",
+                    str(tmp_path / "h.o")], check=True)
+    cpp = tmp_path / "h.cpp"
+    cpp.write_text('#include "psi_si.hpp"\nint main() { return PSI_OK; }\n')
+    subprocess.run([cxx, "-std=c++17", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I" + inc,
+                    "-I/usr/local/cuda/include", "-c", str(cpp), "-o", str(tmp_path / "hpp.o")], check=True)
