@@ -243,8 +243,7 @@ def traffic_per_launch(kernel, n):
 
 def phase_bytes(phase, n, m, nsub, counters, calls, n_even, n_odd, iters, brs):
     """Algorithmic bytes per call of a timed phase: every array element the
-    phase must touch, once, at its size (the per-unit figures are in the
-    design notes)."""
+    phase must touch, once, at its size."""
     L = 2 * n + 2
     if phase == "switch":
         # per vertex of the player: plist, strategy, offsets, key of the current

@@ -157,7 +157,12 @@ int psi_get_valuation(psi_solver *s, int32_t v0, int32_t count, int32_t *out);
  * response (evaluate, mark_solved(1), switch(1) until no switch), then
  * mark_solved(0) and switch(0), until Even makes no switch.  reset != 0 is the
  * "cpu-reset" variant (main.cpp:27-28).  max_evals > 0 caps the number of
- * evaluations (PSI_ERR_LIMIT when reached); 0 means no cap. */
+ * evaluations (PSI_ERR_LIMIT when reached); 0 means no cap.  The graph-driven
+ * loop (psi_options.graph) runs on the device and ends by itself: when a
+ * kernel reports a step cap or a malformed strategy through the device error
+ * word (after that pass, PSI_ERR_LIMIT), and at a runaway guard of
+ * min(2^20, max(2^14, 64*(n+64))) evaluations (PSI_ERR_LIMIT; solves that
+ * need more use graph = 0). */
 int psi_solve(psi_solver *s, int32_t reset, int32_t *iter_count, int32_t *br_count, int64_t max_evals);
 
 /* Device time spent in evaluations and switch steps since creation or the last
@@ -180,6 +185,15 @@ int psi_solver_info(psi_solver *s, int32_t *n, int64_t *m, int32_t *max_pri);
 int psi_solver_stream(psi_solver *s, void **stream);
 /* Number of non-solved vertices the sink did not reach in the last evaluation. */
 int psi_solver_unreached(psi_solver *s, int64_t *count);
+/* Test hook for the device-side error path (no counterpart in the
+ * reference).  From the next psi_solve on, a graph-driven solve sets `bits`
+ * in the solver's device error word right after evaluation `after_evals`
+ * (0 turns the hook off), exactly as a kernel does when it hits one of its
+ * step caps.  The solve loop must then stop at the end of that pass and
+ * psi_solve return PSI_ERR_LIMIT, with psi_solver_times counting only the
+ * evaluations that ran.  Nothing faults on the device: only a word in
+ * device memory is set.  The host-driven loop (graph = 0) ignores it. */
+int psi_solver_debug_inject_error(psi_solver *s, int32_t after_evals, uint32_t bits);
 /* Work counters since the last reset, in this order: evaluations, switch
  * steps, compared edges, parent/priority loads of the comparison walks,
  * vertices whose strategy changed, unreached vertices (summed over full
@@ -361,7 +375,10 @@ int psi_server_info(psi_server *s, int32_t *resident, int32_t *queued, int64_t *
  * holds on each device it uses, until exit.  Hence the size limit: n may be at
  * most PSI_NOALLOC_MAX_VERTICES, larger n returns PSI_ERR_TOO_LARGE.
  * The first call on a device looks up that array's device address (once per
- * device); make that first call before any stream capture.  All calls share
+ * device); make that first call before any stream capture.  The address is
+ * kept for the life of the process: after cudaDeviceReset, or anything else
+ * that destroys the device's primary context, it is stale, and this entry
+ * point must not be called on that device again in the same process.  All calls share
  * the one array, which keeps the previous call's contents (the call clears
  * what must start at zero): calls that overlap on the GPU -- from two host
  * threads, or on two streams -- race and must not be issued. */

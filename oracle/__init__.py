@@ -17,14 +17,20 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "libpsi_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libpsi_ref.so")
-# Where the build recipe and the fixture test read the reference's sources
-# (absent on machines that only run the prebuilt libraries).
-REF_DIR = os.environ.get("REF_DIR", "/root/reference")
+# the reference's 10-vertex fixture game, placed beside REF_LIB by the recipe
+REF_FIXTURE = os.path.join(HERE, "_ref", "test2.gm")
+# Where the reference's sources are, when the caller names them; otherwise
+# the build recipe (build_ref.sh) looks in its own default place and builds
+# only the restatement if they are not there.
+REF_DIR = os.environ.get("REF_DIR")
 
 
-def build(ref_dir: str = REF_DIR) -> None:
-    """Compile the oracle (and the reference driver when ref_dir exists)."""
-    env = dict(os.environ, REF_DIR=ref_dir)
+def build(ref_dir: str | None = REF_DIR) -> None:
+    """Compile the oracle (and the reference driver when the reference's
+    sources are present)."""
+    env = dict(os.environ)
+    if ref_dir:
+        env["REF_DIR"] = ref_dir
     subprocess.run(["sh", os.path.join(HERE, "build_ref.sh")], check=True, env=env)
 
 
@@ -63,6 +69,37 @@ def _oracle_lib():
         L.oracle_get_vals.argtypes = [vp, C.c_int, C.c_int, vp]
         L.oracle_get_vals.restype = None
         L.oracle_solve.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int64]
+        # path-valuation restatement (psi_sparse.c)
+        L.sparse_create.restype = vp
+        L.sparse_create.argtypes = [C.c_int, vp, vp, vp, vp, C.c_int]
+        for f in ("sparse_destroy", "sparse_init_strat", "sparse_reset_opponent_strategy",
+                  "sparse_compute_valuation"):
+            getattr(L, f).argtypes = [vp]
+            getattr(L, f).restype = None
+        L.sparse_max_pri.argtypes = [vp]
+        L.sparse_threads.argtypes = [vp]
+        L.sparse_mark_solved.argtypes = [vp, C.c_int]
+        L.sparse_mark_solved.restype = None
+        L.sparse_switch_strategy.argtypes = [vp, C.c_int]
+        L.sparse_switch_strategy.restype = C.c_int64
+        L.sparse_get_winning.argtypes = [vp, C.c_int, vp]
+        L.sparse_get_winning.restype = C.c_int64
+        L.sparse_compare.argtypes = [vp, C.c_int, C.c_int]
+        for f in ("sparse_get_strategy", "sparse_set_strategy", "sparse_get_infinite", "sparse_get_solved"):
+            getattr(L, f).argtypes = [vp, vp]
+            getattr(L, f).restype = None
+        L.sparse_get_summary.argtypes = [vp, vp, vp, vp]
+        L.sparse_get_summary.restype = None
+        L.sparse_get_vals.argtypes = [vp, C.c_int, C.c_int, vp]
+        L.sparse_get_vals.restype = None
+        L.sparse_solve.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int64]
+        # workload generator (psi_gen.c)
+        L.oracle_gen_random_edges.restype = C.c_int64
+        L.oracle_gen_random_edges.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64, vp]
+        L.oracle_gen_random_fill.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_uint64, vp, vp, vp, vp]
+        L.oracle_gen_longpath_edges.restype = C.c_int64
+        L.oracle_gen_longpath_edges.argtypes = [C.c_int]
+        L.oracle_gen_longpath.argtypes = [C.c_int, C.c_int, C.c_uint64, vp, vp, vp, vp]
         _olib = L
     return _olib
 
@@ -185,6 +222,122 @@ class Oracle:
             self.close()
         except Exception:
             pass
+
+
+class Sparse(Oracle):
+    """The path-valuation restatement of CPUParity (psi_sparse.c): the same
+    StrategyImprovement methods and results as Oracle, in O(n) memory, with
+    the evaluation and the switch step on `threads` host threads (<= 0: every
+    online core)."""
+
+    def __init__(self, owner, priority, offsets, targets, threads: int = 0):
+        self.L = _oracle_lib()
+        self._keep = [np.ascontiguousarray(a, dtype=np.int32) for a in (owner, priority, offsets, targets)]
+        self.n = len(self._keep[0])
+        self.h = self.L.sparse_create(self.n, *[_ptr(a) for a in self._keep], int(threads))
+        if not self.h:
+            raise MemoryError("sparse_create failed")
+        self.max_pri = self.L.sparse_max_pri(self.h)
+        self.threads = self.L.sparse_threads(self.h)
+        self._keep = None    # the solver holds its own copies
+
+    def init_strat(self):
+        self.L.sparse_init_strat(self.h)
+
+    def compute_valuation(self):
+        self.L.sparse_compute_valuation(self.h)
+
+    compute_first_val = compute_valuation
+
+    def mark_solved(self, p):
+        self.L.sparse_mark_solved(self.h, p)
+
+    def switch_strategy(self, p):
+        return self.L.sparse_switch_strategy(self.h, p)
+
+    def reset_opponent_strategy(self):
+        self.L.sparse_reset_opponent_strategy(self.h)
+
+    def get_winning(self, p):
+        out = np.empty(self.n, np.int32)
+        k = self.L.sparse_get_winning(self.h, p, _ptr(out))
+        return out[:k]
+
+    def get_strategy(self):
+        out = np.empty(self.n, np.int32)
+        self.L.sparse_get_strategy(self.h, _ptr(out))
+        return out
+
+    def set_strategy(self, s):
+        s = np.ascontiguousarray(s, dtype=np.int32)
+        self.L.sparse_set_strategy(self.h, _ptr(s))
+
+    def get_infinite(self):
+        out = np.empty(self.n, np.int32)
+        self.L.sparse_get_infinite(self.h, _ptr(out))
+        return out
+
+    def get_solved(self):
+        out = np.empty(self.n, np.int32)
+        self.L.sparse_get_solved(self.h, _ptr(out))
+        return out
+
+    def get_summary(self):
+        """(path length, top priority, its count) per vertex; (0, -1, 0) where infinite."""
+        d, t, c = (np.empty(self.n, np.int32) for _ in range(3))
+        self.L.sparse_get_summary(self.h, _ptr(d), _ptr(t), _ptr(c))
+        return d, t, c
+
+    def get_valuation(self, v0=0, count=None):
+        count = self.n - v0 if count is None else count
+        out = np.empty((count, self.max_pri + 1), np.int32)
+        self.L.sparse_get_vals(self.h, v0, count, _ptr(out))
+        return out
+
+    def compare(self, v, u):
+        return self.L.sparse_compare(self.h, v, u)
+
+    def solve(self, reset=False, max_evals=0):
+        it = C.c_int()
+        br = C.c_int()
+        rc = self.L.sparse_solve(self.h, int(reset), C.byref(it), C.byref(br), max_evals)
+        if rc != 0:
+            raise RuntimeError("oracle evaluation cap reached")
+        return it.value, br.value
+
+    def close(self):
+        if self.h:
+            self.L.sparse_destroy(self.h)
+            self.h = None
+
+
+def random_game(n, deg_lo, deg_hi, pri_hi=None, seed=1):
+    """CSR (owner, priority, offsets, targets) of the seeded random game, made
+    on the CPU without the product library (psi_gen.c); the same arrays as
+    psi.Game.random(n, deg_lo, deg_hi, pri_hi, seed).csr()."""
+    L = _oracle_lib()
+    pri_hi = n if pri_hi is None else pri_hi
+    off = np.empty(n + 1, np.int32)
+    m = L.oracle_gen_random_edges(n, deg_lo, deg_hi, seed, _ptr(off))
+    if m < 0:
+        raise ValueError("bad random-game arguments")
+    ow, pr, tg = np.empty(n, np.int32), np.empty(n, np.int32), np.empty(max(m, 1), np.int32)
+    if L.oracle_gen_random_fill(n, deg_lo, deg_hi, pri_hi, seed, _ptr(off), _ptr(ow), _ptr(pr), _ptr(tg)) != 0:
+        raise ValueError("bad random-game arguments")
+    return ow, pr, off, tg[:m]
+
+
+def longpath_game(n, pri_hi=1024, seed=1):
+    """CSR of the seeded long-path game (psi_gen.c); the same arrays as
+    psi.Game.longpath(n, pri_hi, seed).csr()."""
+    L = _oracle_lib()
+    m = L.oracle_gen_longpath_edges(n)
+    if m < 0:
+        raise ValueError("bad long-path arguments")
+    ow, pr, off, tg = np.empty(n, np.int32), np.empty(n, np.int32), np.empty(n + 1, np.int32), np.empty(m, np.int32)
+    if L.oracle_gen_longpath(n, pri_hi, seed, _ptr(ow), _ptr(pr), _ptr(off), _ptr(tg)) != 0:
+        raise ValueError("bad long-path arguments")
+    return ow, pr, off, tg
 
 
 class RefSolver:

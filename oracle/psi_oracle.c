@@ -95,11 +95,17 @@ void oracle_destroy(oracle_t *o)
 
 int oracle_max_pri(const oracle_t *o) { return o->max_pri; }
 
-/* cpu_parity.cpp:276-286 */
+/* cpu_parity.cpp:276-286.  The reference's solver object serves one solve
+ * (its init_strat appends to strat); starting a solve here also clears what
+ * a previous solve on the same object left in solved[] and infinite[], so
+ * every solve runs as on a fresh CPUParity (cpu_parity.cpp:20-33). */
 void oracle_init_strat(oracle_t *o)
 {
-    for (int v = 0; v < o->n; v++)
+    for (int v = 0; v < o->n; v++) {
         o->strat[v] = (o->owner[v] == 0) ? -1 : o->targets[o->offsets[v]];
+        o->solved[v] = 0;
+        o->infinite[v] = 0;
+    }
 }
 
 /* cpu_parity.cpp:300-307 */

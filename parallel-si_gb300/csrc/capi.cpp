@@ -388,6 +388,14 @@ int psi_solver_unreached(psi_solver *s, int64_t *count)
     return PSI_OK;
 }
 
+int psi_solver_debug_inject_error(psi_solver *s, int32_t after_evals, uint32_t bits)
+{
+    if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null argument");
+    if (after_evals < 0) return psi::fail(PSI_ERR_INVALID, "after_evals must be >= 0");
+    s->s->debug_inject_error(after_evals, bits);
+    return PSI_OK;
+}
+
 int psi_solver_reset_times(psi_solver *s)
 {
     if (!s || !s->s) return psi::fail(PSI_ERR_INVALID, "null solver");

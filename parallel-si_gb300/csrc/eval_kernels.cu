@@ -592,15 +592,21 @@ __global__ void k_mark_solved(const int32_t *__restrict__ ucount, const int32_t 
 // Grid for the grid-stride kernels: enough blocks to fill the device a few
 // times over, not one block per 256 items (a kernel whose gate is closed then
 // costs a small launch).
-unsigned capped_grid(int64_t items)
+std::atomic<int> g_sms[kMaxCachedDevices];
+
+int device_sms()
 {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
+    return per_device(g_sms, [] {
+        int dev = 0, sms = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
-    }
+        return sms > 0 ? sms : 1;
+    });
+}
+
+unsigned capped_grid(int64_t items)
+{
+    const int sms = device_sms();
     unsigned g = grid_for(items);
     unsigned cap = 16u * (unsigned)sms;
     return g < cap ? g : cap;
@@ -608,17 +614,12 @@ unsigned capped_grid(int64_t items)
 
 int device_blocks(const void *kernel, int block)
 {
-    static int cached_dev = -1, cached_sms = 0;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev != cached_dev) {
-        cudaDeviceGetAttribute(&cached_sms, cudaDevAttrMultiProcessorCount, dev);
-        cached_dev = dev;
-    }
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
-    return (cached_sms > 0 ? cached_sms : 1) * (per_sm > 0 ? per_sm : 1);
+    return device_sms() * (per_sm > 0 ? per_sm : 1);
 }
+
+std::atomic<int> g_rank_blocks[kMaxCachedDevices], g_cycle_blocks[kMaxCachedDevices];
 
 }  // namespace
 
@@ -694,13 +695,7 @@ void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, in
 int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, int2 *b, const int2 **fin,
                         const int32_t *gate)
 {
-    static int blocks = 0, blocks_dev = -1;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev != blocks_dev) {
-        blocks = device_blocks((const void *)k_rank_reduced, kBlock);
-        blocks_dev = dev;
-    }
+    const int blocks = per_device(g_rank_blocks, [] { return device_blocks((const void *)k_rank_reduced, kBlock); });
     int64_t need = ceil_div(nsub, kBlock);
     int grid = (int)(need < blocks ? need : blocks);
     int rounds = 0;
@@ -733,13 +728,7 @@ int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, c
                   const int32_t *pri, const uint8_t *solved, int32_t *st, int32_t *key, int2 *ja, int2 *jb,
                   int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err, ChangeTrack track, const int32_t *gate)
 {
-    static int blocks = 0, blocks_dev = -1;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev != blocks_dev) {
-        blocks = device_blocks((const void *)k_cycles, kBlock);
-        blocks_dev = dev;
-    }
+    const int blocks = per_device(g_cycle_blocks, [] { return device_blocks((const void *)k_cycles, kBlock); });
     void *args[] = {(void *)&ucount, (void *)&ulist, (void *)&strat, (void *)&pri, (void *)&solved,
                     (void *)&st, (void *)&key, (void *)&ja, (void *)&jb, (void *)&la, (void *)&lb, (void *)&cnt,
                     (void *)&err, (void *)&track, (void *)&gate};

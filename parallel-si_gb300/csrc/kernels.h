@@ -3,6 +3,7 @@
 #ifndef PSI_KERNELS_H
 #define PSI_KERNELS_H
 
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -69,6 +70,26 @@ struct ChangeList {
 // device (pool.cu); release with cudaFreeAsync on a stream.  Freed blocks
 // stay cached in the pool for later allocations of the process.
 cudaError_t device_alloc(void **p, size_t bytes, cudaStream_t s);
+
+// A launch-shape figure (resident blocks of a cooperative kernel, SM count)
+// cached per CUDA device ordinal of the calling thread's current device:
+// `slot` holds one entry per ordinal, 0 until computed.  Threads that drive
+// solvers on different devices each read their own device's entry; two
+// threads racing on one entry both compute the same value.  Ordinals beyond
+// the table are computed on every call.
+constexpr int kMaxCachedDevices = 64;
+template <class F>
+int per_device(std::atomic<int> (&slot)[kMaxCachedDevices], F compute)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxCachedDevices) return compute();
+    int v = slot[dev].load(std::memory_order_relaxed);
+    if (v <= 0) {
+        v = compute();
+        slot[dev].store(v, std::memory_order_relaxed);
+    }
+    return v;
+}
 
 // Process-wide count of kernel launches issued by this library.
 void count_launch();

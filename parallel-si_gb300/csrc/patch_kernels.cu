@@ -431,13 +431,10 @@ __global__ void __launch_bounds__(kPatchBlock) k_patch_values(PatchArgs a)
 
 int patch_blocks(const void *kernel)
 {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
-    }
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPatchBlock, 0);
     if (per_sm <= 0) per_sm = 1;
@@ -446,6 +443,8 @@ int patch_blocks(const void *kernel)
     // sees (1 to 4 blocks per SM measured within 1% of each other)
     return sms * (per_sm < 2 ? per_sm : 2);
 }
+
+std::atomic<int> g_collect_blocks[kMaxCachedDevices], g_values_blocks[kMaxCachedDevices];
 
 }  // namespace
 
@@ -463,8 +462,7 @@ void launch_patch_begin(cudaStream_t s, const PatchArgs &a)
 
 int launch_patch_collect(cudaStream_t s, const PatchArgs &a)
 {
-    static int blocks = 0;
-    if (blocks == 0) blocks = patch_blocks((const void *)k_patch_collect);
+    const int blocks = per_device(g_collect_blocks, [] { return patch_blocks((const void *)k_patch_collect); });
     void *args[] = {(void *)&a};
     count_launch();
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_patch_collect, dim3(blocks), dim3(kPatchBlock), args,
@@ -474,8 +472,7 @@ int launch_patch_collect(cudaStream_t s, const PatchArgs &a)
 
 int launch_patch_values(cudaStream_t s, const PatchArgs &a)
 {
-    static int blocks = 0;
-    if (blocks == 0) blocks = patch_blocks((const void *)k_patch_values);
+    const int blocks = per_device(g_values_blocks, [] { return patch_blocks((const void *)k_patch_values); });
     void *args[] = {(void *)&a};
     count_launch();
     cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_patch_values, dim3(blocks), dim3(kPatchBlock), args,

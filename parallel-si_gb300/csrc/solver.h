@@ -38,12 +38,18 @@ inline int32_t status_infinite(int32_t st) { return st == -2 ? 1 : (st == -1 ? -
 // Control words on the device: the evaluation's gates (kernels.h), and those of
 // the graph-driven solve loop (solver_graph.cu).
 struct GraphCtl : EvalGates {
-    enum { kRunning = 0, kConverged = 1, kEvalCap = 2, kRunaway = 3 };
+    // kDeviceError: a kernel of the last pass set a bit of the device error
+    // word (a step cap, a malformed strategy); the loop ends after that pass
+    enum { kRunning = 0, kConverged = 1, kEvalCap = 2, kRunaway = 3, kDeviceError = 4 };
     int32_t even = 0;    // gate: Even's mark_solved and switch run in this step
     int32_t reset = 0;   // gate: Odd's strategy is reset before the next evaluation
     int32_t quiet = 0;   // every need flag is set: the next evaluation's key changes flag nothing
     int32_t patch_on = 0;   // evaluations after the first may be patches (psi_options.incremental)
     int32_t brs = 0, iters = 0, stop = kRunning, max_evals = 0;
+    // test hook (psi_solver_debug_inject_error): after evaluation inject_at
+    // (> 0) the control kernel sets inject_bits in the device error word
+    int32_t inject_at = 0;
+    uint32_t inject_bits = 0;
 };
 
 class Solver {
@@ -85,6 +91,14 @@ public:
     // The same loop as one CUDA graph launch (solver_graph.cu).
     int solve_graph(int32_t reset, int32_t *iters, int32_t *brs, int64_t max_evals);
     bool use_graph() const { return use_graph_; }
+    // Test hook: the next graph solves set `bits` in the device error word
+    // after evaluation `after_evals` (0: off), as a kernel that hits a step
+    // cap does; the loop must end after that pass with PSI_ERR_LIMIT.
+    void debug_inject_error(int32_t after_evals, uint32_t bits)
+    {
+        inject_at_ = after_evals;
+        inject_bits_ = bits;
+    }
 
     int32_t n() const { return n_; }
     int64_t m() const { return m_; }
@@ -219,6 +233,8 @@ private:
     int run_graph(bool reset, int64_t max_evals, GraphCtl *out, int4 *gstate_out);
     int solve_batch_graph(std::vector<int4> &state);
     bool use_graph_ = false, graph_reset_ = false;
+    int32_t inject_at_ = 0;
+    uint32_t inject_bits_ = 0;
     GraphCtl *ctl_ = nullptr;
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t graph_exec_ = nullptr;

@@ -24,7 +24,7 @@ namespace {
 
 // after an evaluation: the tour is valid for updates (and the next
 // evaluation may be a patch), one more evaluation
-__global__ void k_ctl_evaluated(GraphCtl *c)
+__global__ void k_ctl_evaluated(GraphCtl *c, uint32_t *err)
 {
     c->full = 0;
     c->incr = 1;
@@ -32,15 +32,23 @@ __global__ void k_ctl_evaluated(GraphCtl *c)
     c->reset = 0;
     c->quiet = 0;
     c->brs++;
+    if (c->inject_at > 0 && c->brs == c->inject_at) atomicOr(err, c->inject_bits);
 }
 
 // after Odd's switch: Even moves in this step iff Odd made no strict improvement
 __global__ void k_ctl_odd(GraphCtl *c, const unsigned long long *sw) { c->even = (sw[3] == 0) ? 1 : 0; }
 
-// after Even's (gated) switch: iteration count, termination, reset, caps
-__global__ void k_ctl_even(GraphCtl *c, const unsigned long long *sw, cudaGraphConditionalHandle loop,
-                           int32_t reset_variant, int32_t guard)
+// after Even's (gated) switch: iteration count, termination, reset, caps.
+// A set bit of the device error word ends the loop after this pass: the
+// state it left may be inconsistent, and later passes must not build on it.
+__global__ void k_ctl_even(GraphCtl *c, const unsigned long long *sw, const uint32_t *err,
+                           cudaGraphConditionalHandle loop, int32_t reset_variant, int32_t guard)
 {
+    if (*(volatile const uint32_t *)err) {
+        c->stop = GraphCtl::kDeviceError;
+        cudaGraphSetConditional(loop, 0);
+        return;
+    }
     bool go = true;
     if (c->even) {
         c->iters++;
@@ -65,9 +73,15 @@ __global__ void k_ctl_even(GraphCtl *c, const unsigned long long *sw, cudaGraphC
     if (!go) cudaGraphSetConditional(loop, 0);
 }
 
-// A solve that needs this many evaluations is treated as a fault (the loop
-// runs on the device and must end by itself).
-constexpr int32_t kEvalGuard = 1 << 20;
+// A solve that needs more evaluations than this is treated as a runaway (the
+// loop runs on the device and must end by itself): 64 per vertex plus a
+// margin, between 2^14 and 2^20.  Random games of 2^24 vertices need under
+// 100; a caller expecting more passes max_evals or uses the host loop.
+inline int32_t eval_guard(int64_t n)
+{
+    const int64_t g = 64 * (n + 64);
+    return (int32_t)(g < (1 << 14) ? (1 << 14) : (g > (1 << 20) ? (1 << 20) : g));
+}
 
 }  // namespace
 
@@ -127,7 +141,7 @@ int Solver::enqueue_step(cudaGraph_t body, cudaGraphConditionalHandle loop, bool
     const bool batch = games_ > 0 && !arena_;
     PSI_CUDA_TRY(cudaStreamBeginCaptureToGraph(stream_, body, &ifnode, nullptr, 1, mode));
     count_launch();
-    k_ctl_evaluated<<<1, 1, 0, stream_>>>(ctl_);
+    k_ctl_evaluated<<<1, 1, 0, stream_>>>(ctl_, &dw_->err);
     if (batch) launch_batch_account(stream_, games_, 0, gstate_, gcount_);
     // Odd: mark_solved(1), switch(1)
     launch_mark_solved(stream_, &dw_->ucount, ulist_, 1, st_, solved_, dirty_, nullptr, nullptr, nullptr,
@@ -153,7 +167,7 @@ int Solver::enqueue_step(cudaGraph_t body, cudaGraphConditionalHandle loop, bool
                   &dw_->cnt[2], changes(), tie_, watch_, skip_);
     if (batch) launch_batch_account(stream_, games_, 3, gstate_, gcount_, &ctl_->even);
     count_launch();
-    k_ctl_even<<<1, 1, 0, stream_>>>(ctl_, dw_->sw, loop, reset ? 1 : 0, kEvalGuard);
+    k_ctl_even<<<1, 1, 0, stream_>>>(ctl_, dw_->sw, &dw_->err, loop, reset ? 1 : 0, eval_guard(n_));
     e = cudaGetLastError();
     if (e != cudaSuccess) return abort_capture(fail(PSI_ERR_CUDA, std::string("step launch: ") + cudaGetErrorString(e)));
     PSI_CUDA_TRY(cudaStreamEndCapture(stream_, &g));
@@ -207,14 +221,17 @@ int Solver::run_graph(bool reset, int64_t max_evals, GraphCtl *out, int4 *gstate
     init.quiet = 1;  // and every need flag is set
     init.patch_on = incremental_ != PSI_INCR_OFF ? 1 : 0;
     init.max_evals = max_evals > 0 && max_evals < INT32_MAX ? (int32_t)max_evals : 0;
+    init.inject_at = inject_at_;
+    init.inject_bits = inject_bits_;
     PSI_CUDA_TRY(cudaMemcpyAsync(ctl_, &init, sizeof init, cudaMemcpyHostToDevice, stream_));
     PSI_CUDA_TRY(cudaGraphLaunch(graph_exec_, stream_));
     PSI_CUDA_TRY(cudaMemcpyAsync(out, ctl_, sizeof *out, cudaMemcpyDeviceToHost, stream_));
     if (gstate_out)
         PSI_CUDA_TRY(cudaMemcpyAsync(gstate_out, gstate_, sizeof(int4) * (size_t)games_, cudaMemcpyDeviceToHost,
                                      stream_));
+    // the counts of the passes that ran are kept even when a pass failed
     rc = sync_and_check("solve (graph)");
-    if (rc) return rc;
+    if (rc && rc != PSI_ERR_LIMIT) return rc;
     // every pass launches each kernel of the body once, those of the full
     // evaluation only when it is not a patch
     const long long patched = (long long)(hw_->patch[0] - patches_before);
@@ -222,9 +239,15 @@ int Solver::run_graph(bool reset, int64_t max_evals, GraphCtl *out, int4 *gstate
                  graph_full_launches_ * (out->brs - patched));
     times_.evals += out->brs;
     times_.switches += out->brs + out->iters;
+    if (rc) {   // the device error word was set: the state is not trusted
+        val_ready_ = false;
+        tour_valid_ = false;
+        return rc;
+    }
     val_ready_ = true;
     tour_valid_ = true;
     if (out->stop == GraphCtl::kEvalCap) return fail(PSI_ERR_LIMIT, "evaluation cap reached");
+    if (out->stop == GraphCtl::kDeviceError) return fail(PSI_ERR_LIMIT, "graph solve loop stopped by a device error");
     if (out->stop != GraphCtl::kConverged) return fail(PSI_ERR_LIMIT, "graph solve loop stopped by its guard");
     return PSI_OK;
 }

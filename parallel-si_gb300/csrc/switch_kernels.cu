@@ -402,6 +402,8 @@ __global__ void k_materialize(int32_t v0, int32_t count, int32_t d, const int32_
     }
 }
 
+std::atomic<int> g_switch_blocks[kMaxCachedDevices];
+
 int switch_grid()
 {
     int dev = 0, sms = 0, per_sm = 0;
@@ -422,8 +424,7 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
                    const int4 *skip)
 {
     if (np <= 0) return;
-    static int blocks = 0;   // resident blocks on the device (same device for the process's solvers)
-    if (blocks == 0) blocks = switch_grid();
+    const int blocks = per_device(g_switch_blocks, switch_grid);   // four waves of resident blocks
     unsigned g = grid_for(np);
     g = g < (unsigned)blocks ? g : (unsigned)blocks;
     const int32_t *items = plist, *count = nullptr;

@@ -104,6 +104,7 @@ _SIGS = {
     "psi_solver_phase_times": ([_vp, C.POINTER(C.c_double), _i64p, C.c_int32], C.c_int),
     "psi_solver_stream": ([_vp, _pp], C.c_int),
     "psi_solver_unreached": ([_vp, _i64p], C.c_int),
+    "psi_solver_debug_inject_error": ([_vp, C.c_int32, C.c_uint32], C.c_int),
     "psi_solver_counters": ([_vp, _i64p, C.c_int32], C.c_int),
     "psi_launch_count": ([], C.c_int64),
     "psi_host_alloc": ([C.c_size_t, _pp], C.c_int),

@@ -48,7 +48,7 @@ def test_oracle_matches_reference_golden(case):
 
 def test_ring10_is_the_reference_fixture_game():
     """The ring10 family is the reference's own test2.gm fixture, built in code."""
-    path = os.path.join(oracle.REF_DIR, "test2.gm")
+    path = oracle.REF_FIXTURE
     if not os.path.exists(path) or not oracle.ref_available():
         pytest.skip("reference tree not present")
     ref = oracle.RefSolver(open(path).read())

@@ -17,7 +17,7 @@ import numpy as np
 import pytest
 
 import psi
-from psi._lib import PSI_ERR_TOO_LARGE, lib
+from psi._lib import PSI_ERR_INVALID, PSI_ERR_TOO_LARGE, lib
 
 pytestmark = pytest.mark.gpu
 
@@ -79,6 +79,65 @@ def test_noalloc_matches_solver_twice(family):
         got = noalloc_status(torch, game, strat)
         want = solver_status(game, strat)
         assert np.array_equal(got, want), f"mismatch at {np.nonzero(got != want)[0][:10]}"
+
+
+def _cuda(torch):
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    torch.cuda.set_device(0)
+
+
+def test_noalloc_at_capacity_then_small():
+    """A game of exactly PSI_NOALLOC_MAX_VERTICES vertices (every slot of the
+    scratch layout at its largest), then a small game: the second call must
+    not see anything the first left behind."""
+    torch = pytest.importorskip("torch")
+    _cuda(torch)
+    rng = np.random.default_rng(11)
+    big = psi.Game.random(NOALLOC_MAX_VERTICES, 2, 5, 64, seed=81)      # few priorities: small dense rows
+    small = psi.Game.random(3000, 2, 5, 3000, seed=82)
+    for game in (big, small, big):
+        strat = random_strategy(game, rng)
+        got = noalloc_status(torch, game, strat)
+        want = solver_status(game, strat)
+        assert np.array_equal(got, want), f"n={game.n}: mismatch at {np.nonzero(got != want)[0][:10]}"
+
+
+def test_noalloc_long_path_at_capacity():
+    """The long-path family at full capacity: one tour of depth ~n."""
+    torch = pytest.importorskip("torch")
+    _cuda(torch)
+    game = psi.Game.longpath(NOALLOC_MAX_VERTICES, 16, seed=83)
+    owner, _, off, tg = game.csr()
+    strat = tg[off[:-1]].astype(np.int32)            # v -> v+1 along the chain (the last: its back-edge)
+    assert owner[game.n - 2] == 0
+    strat[game.n - 2] = -1                           # an Even vertex at the end leaves for the sink
+    got = noalloc_status(torch, game, strat)
+    assert got.max() >= game.n - 1                   # the path from vertex 0 spans the whole chain
+    want = solver_status(game, strat)
+    assert np.array_equal(got, want), f"mismatch at {np.nonzero(got != want)[0][:10]}"
+
+
+def test_noalloc_rejects_out_of_range_strategy():
+    """A strategy entry >= n (or < -1) is reported as PSI_ERR_INVALID; the
+    kernels treat the entry as the sink while they run, so every access stays
+    inside the caller's arrays and the scratch, and the next call is clean."""
+    torch = pytest.importorskip("torch")
+    _cuda(torch)
+    game = psi.Game.random(2000, 2, 5, 2000, seed=84)
+    rng = np.random.default_rng(12)
+    for bad in (game.n, game.n + 1000, -7):
+        strat = random_strategy(game, rng)
+        strat[123] = bad
+        dev = torch.device("cuda", 0)
+        d_strat = torch.tensor(strat, dtype=torch.int32, device=dev)
+        d_pri = torch.tensor(game.csr()[1], dtype=torch.int32, device=dev)
+        d_out = torch.zeros(game.n, dtype=torch.int32, device=dev)
+        rc = lib.psi_evaluate_strategy_noalloc(game.n, d_strat.data_ptr(), d_pri.data_ptr(), d_out.data_ptr(), None)
+        assert rc == PSI_ERR_INVALID, rc
+        assert "out of range" in lib.psi_last_error().decode()
+    strat = random_strategy(game, rng)
+    assert np.array_equal(noalloc_status(torch, game, strat), solver_status(game, strat))
 
 
 def test_noalloc_rejects_games_beyond_its_capacity():
