@@ -17,12 +17,20 @@ same workload (--no-tune takes them from the flags); none of them changes a
 result.  After its timed regions it measures the random-access bound
 (psi_measure_random_access) at the size of the arrays the sublist walk and the
 switch read at random, and reports both kernels against it beside the
-copy-bandwidth roofline.
+copy-bandwidth roofline.  On one GPU the line also carries, unless --no-extras:
+the n = 10,000 random game (out-degree U[2,10]) on the GPU beside the dense
+restatement of the reference's CPUParity on the host ("c1"); the 2^23 long-path
+game ("longpath"); 4,096 mixed-size games batched against one-by-one solves
+("batch"); and the continuous-batching server under saturated and Poisson load
+("serve").
 
---impl reference times the reference algorithm's CPU implementation instead:
-the oracle (a C restatement of the reference's CPUParity), single thread, on a
-bounded sample of the same workload (the dense n*(max_pri+1) valuation table of
-CPUParity does not fit at n = 2^24).
+--impl reference times the reference algorithm's CPU implementation instead,
+without loading the CUDA library: the games come from the oracle's own
+generator (byte-identical to the library's), and the solver is the exact
+path-valuation restatement of CPUParity on every host core (the dense
+n*(max_pri+1) rows of CPUParity itself would take 2^48 ints at n = 2^24).  Each
+of its steps is one SI iteration of a solve_si sequence of the same game, the
+solve restarting from init_strat when it converges.
 """
 from __future__ import annotations
 
@@ -47,7 +55,7 @@ UNIT = "SI iters/s"
 N_DEFAULT = 1 << 24
 LONGPATH_N = 1 << 23
 DEG_LO, DEG_HI = 2, 5
-CPU_SAMPLE_N = 1 << 15          # bounded sample for the CPU reference algorithm
+C1_N, C1_DEG = 10000, (2, 10)   # the reference CPU path's own full-size configuration
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 TRAFFIC_PATH = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
@@ -57,36 +65,50 @@ LONGPATH_PRI = 1024            # long-path games: priority U[0,1024)
 
 
 def make_game(psi, family, n, seed):
-    """The single game a step solves: the random headline game or the long-path game."""
+    """The single game a step solves: the random headline game, the long-path
+    game, or the reference CPU path's own n = 10,000 case."""
     if family == "longpath":
         return psi.Game.longpath(n, LONGPATH_PRI, seed)
+    if family == "c1":
+        return psi.Game.random(n, C1_DEG[0], C1_DEG[1], n, seed)
     return psi.Game.random(n, DEG_LO, DEG_HI, n, seed)
 
 
 def workload_config(n, m=None, seed=1, family="single"):
-    if family == "longpath":
+    if family == "c1":
+        text = (f"single random parity game, n={n}: owner uniform, priority uniform in [0,n), out-degree uniform "
+                f"in [{C1_DEG[0]},{C1_DEG[1]}], distinct non-self successors (the reference CPU path's full-size "
+                f"case)")
+    elif family == "longpath":
         text = (f"long-path parity game, n={n} (2^{n.bit_length() - 1}): chain v_i -> v_(i+1) plus one back-edge "
                 f"per vertex to a uniformly random earlier vertex, owner alternating, priority uniform in "
                 f"[0,{LONGPATH_PRI})")
     else:
         text = (f"single random parity game, n={n} (2^{n.bit_length() - 1}): owner uniform, priority uniform in "
                 f"[0,n), out-degree uniform in [{DEG_LO},{DEG_HI}], distinct non-self successors")
+    # the workload only, the same for both arms; how each arm solves it is in
+    # its line's "method" (this arm) or "cpu_baseline" (the reference arm)
     cfg = {
         "workload": text,
         "n": n,
         "seed": seed,
-        "step": "one full solve_si (init_strat to convergence) through psi_solve, game resident in HBM",
-        "solve_loop": "one CUDA graph per solve (device-side loop control); per-phase times for the roofline "
-                      "from the same kernels in the host-driven loop",
-        "l2": "inputs larger than L2 (game CSR + solver state ~1.3 GB at n=2^24), no flush",
-        "parallelism": "replicas: one independent game per GPU",
-        "evaluation": "incremental where few strategies changed (psi_options.incremental = auto: patches after "
-                      "steps that changed <= patch_limit strategies, else the full Euler-tour evaluation); "
-                      "results identical to full evaluations",
+        "parallelism": "replicas: one independent game per GPU (the reference arm: rank 0's game on the host)",
+        "l2": ("inputs larger than L2 (game CSR + solver state ~1.3 GB at n=2^24), no flush" if n >= (1 << 20)
+               else "game and solver state fit in L2; every solve rewrites its state from init_strat"),
     }
     if m is not None:
         cfg["m"] = m
     return cfg
+
+
+METHOD = {
+    "step": "one full solve_si (init_strat to convergence) through psi_solve, game resident in HBM",
+    "solve_loop": "one CUDA graph per solve (device-side loop control); per-phase times for the roofline from the "
+                  "same kernels in the host-driven loop",
+    "evaluation": "incremental where few strategies changed (psi_options.incremental = auto: patches after steps "
+                  "that changed <= patch_limit strategies, else the full Euler-tour evaluation); results identical "
+                  "to full evaluations",
+}
 
 
 # ------------------------------------------------------------------ helpers
@@ -280,56 +302,175 @@ PHASE_KERNELS = {"sublist": ("k_walk_sublists",), "tour": ("k_dirty_list", "k_to
 FULL_EVAL_PHASES = ("sublist", "tour", "broadcast", "reduced", "cycles")
 
 
-def cpu_baseline_sample(solves=3, seed=1, family="single"):
-    """The oracle (C restatement of CPUParity), single thread, on the bounded
-    sample: `solves` full solves of the n=2^15 game of the same distribution."""
+# ------------------------------------------------------------------ CPU legs
+# Everything here runs the oracle (test infrastructure, the reference's
+# algorithm restated) and never the CUDA library.
+def cpu_game(family, n, seed):
+    """CSR arrays of the workload game from the oracle's generator (the same
+    bytes as the library's generator gives)."""
     import oracle
-    import psi
 
-    g = make_game(psi, family, CPU_SAMPLE_N, seed)
-    o = oracle.Oracle(*g.csr())
+    if family == "longpath":
+        return oracle.longpath_game(n, LONGPATH_PRI, seed)
+    if family == "c1":
+        return oracle.random_game(n, C1_DEG[0], C1_DEG[1], n, seed)
+    return oracle.random_game(n, DEG_LO, DEG_HI, n, seed)
+
+
+def cpu_threads():
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+
+
+class IterationStepper:
+    """SI iterations of a solve_si sequence (main.cpp:20-55) on a CPU solver:
+    step() runs one iteration -- Odd's best response (evaluate, mark_solved(1),
+    switch(1) until no switch), then mark_solved(0) and Even's switch -- and
+    a converged solve starts over from init_strat on the next step."""
+
+    def __init__(self, solver):
+        self.s = solver
+        self.fresh = True
+        self.evals = 0
+        self.solves = 0
+
+    def step(self):
+        s = self.s
+        if self.fresh:
+            s.init_strat()
+            self.fresh = False
+        while True:
+            s.compute_valuation()
+            self.evals += 1
+            s.mark_solved(1)
+            if s.switch_strategy(1) == 0:
+                break
+        s.mark_solved(0)
+        if s.switch_strategy(0) == 0:
+            self.fresh = True
+            self.solves += 1
+
+
+def cpu_baseline_full(family, n, seed):
+    """The bounded CPU sample of the headline workload: one full solve_si of
+    the same game by the path-valuation restatement of CPUParity on every host
+    core (SI iterations over the wall time of the solve)."""
+    import oracle
+
+    csr = cpu_game(family, n, seed)
+    o = oracle.Sparse(*csr, threads=cpu_threads())
     t0 = time.perf_counter()
-    iters = 0
+    it, br = o.solve()
+    dt = time.perf_counter() - t0
+    threads = o.threads
+    o.close()
+    return {"value": it / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"one full solve_si of the same n={n} game (seed {seed}): {it} iterations, {br} evaluations, "
+                      f"{dt:.1f} s, by the exact path-valuation restatement of the reference's CPUParity on "
+                      f"{threads} host threads (CPUParity's dense rows would need n*(max_pri+1) ints)"}
+
+
+def cpu_c1(seed, solves=3):
+    """The reference CPU path's own full-size case (n = 10,000, out-degree
+    U[2,10]): the dense restatement of CPUParity, one thread as the reference
+    runs it, `solves` full solves of one game; and every host core solving
+    its own C1 game (seeds seed, seed+1, ...) at once, games per second."""
+    import threading
+
+    import oracle
+
+    csr = cpu_game("c1", C1_N, seed)
+    o = oracle.Oracle(*csr)
+    t0 = time.perf_counter()
+    iters = brs = 0
     for _ in range(solves):
-        it, _ = o.solve()
+        it, br = o.solve()
         iters += it
+        brs += br
     dt = time.perf_counter() - t0
     o.close()
-    return {"value": iters / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{solves} full solves of the n=2^15 game of the same distribution (seed {seed}); "
-                      f"{dt:.1f} s; the reference's CPUParity keeps n*(max_pri+1) ints and cannot hold the "
-                      f"full-size game"}
+    one = {"si_iters_per_s": iters / dt, "solve_ms": 1000 * dt / solves, "iters": iters // solves,
+           "brs": brs // solves, "cores": 1,
+           "how": f"{solves} full solves, dense restatement of CPUParity (psi_oracle.c), one thread"}
+    # all cores: one dense solver per thread, each on its own seed (ctypes
+    # releases the GIL during the C call); bounded by host memory (400 MB each)
+    t = max(1, min(cpu_threads(), 16))
+    solvers = [oracle.Oracle(*cpu_game("c1", C1_N, seed + k)) for k in range(t)]
+    res = [None] * t
+
+    def work(k):
+        res[k] = solvers[k].solve()
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(t)]
+    t0 = time.perf_counter()
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    dt = time.perf_counter() - t0
+    for o2 in solvers:
+        o2.close()
+    allc = {"games_per_s": t / dt, "si_iters_per_s": sum(r[0] for r in res) / dt, "cores": t,
+            "how": f"{t} C1 games (seeds {seed}..{seed + t - 1}) solved at once, one dense solver per thread"}
+    return {"one_core": one, "all_cores": allc}
 
 
 # ------------------------------------------------------------------ arms
 def run_reference(args, rank, world):
+    """The reference arm: the reference algorithm's CPU implementation on the
+    host cores, on this arm's workload, with no CUDA library loaded."""
     if rank != 0:
         return 0
     import oracle
-    import psi
 
-    g = make_game(psi, args.workload, CPU_SAMPLE_N, args.seed)
-    o = oracle.Oracle(*g.csr())
-    for _ in range(args.warmup):
-        o.solve()
-    t0 = time.perf_counter()
-    iters = 0
-    for _ in range(args.steps):
-        it, _ = o.solve()
-        iters += it
-    dt = time.perf_counter() - t0
+    base = {"impl": "reference", "metric": METRIC, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32", "data": "synthetic"}
+    if args.workload in ("batch", "serve"):
+        print(json.dumps(dict(base, unavailable="the reference solves one game per process run and has no batched "
+                                                "or served form; the batch line reports one-by-one solves beside "
+                                                "the batch")), flush=True)
+        return 0
+    n = C1_N if args.workload == "c1" else args.n
+    csr = cpu_game(args.workload, n, args.seed)
+    if args.workload == "c1":
+        # the reference's own CPU-runnable case: dense CPUParity restated, one
+        # thread, each step one full solve
+        o = oracle.Oracle(*csr)
+        for _ in range(args.warmup):
+            o.solve()
+        t0 = time.perf_counter()
+        iters = 0
+        for _ in range(args.steps):
+            it, _ = o.solve()
+            iters += it
+        dt = time.perf_counter() - t0
+        cores, kind = 1, "port"
+        sample = (f"each step: one full solve of the n={n} game (seed {args.seed}) by the dense restatement of "
+                  f"the reference CPUParity (psi_oracle.c), one thread")
+    else:
+        o = oracle.Sparse(*csr, threads=cpu_threads())
+        cores, kind = o.threads, "port"
+        # warm-up: evaluations of the initial strategy (pages the arrays in)
+        o.init_strat()
+        for _ in range(args.warmup):
+            o.compute_valuation()
+        stepper = IterationStepper(o)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            stepper.step()
+        dt = time.perf_counter() - t0
+        iters = args.steps
+        sample = (f"each step: the next SI iteration (Odd's best response, then Even's switch) of a solve_si "
+                  f"sequence of the same n={n} game (seed {args.seed}), restarting from init_strat at convergence "
+                  f"({stepper.solves} solve(s) completed, {stepper.evals} evaluations in {args.steps} steps), by "
+                  f"the exact path-valuation restatement of the reference's CPUParity on {cores} host threads; "
+                  f"warm-up steps: evaluations of the initial strategy")
+    o.close()
     value = iters / dt
-    sample = (f"each step: one full solve of the n=2^15 game of the same distribution (seed {args.seed}) by "
-              f"the oracle (C restatement of the reference CPUParity, single thread; the reference's dense "
-              f"valuation table cannot hold the full-size game)")
-    line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": workload_config(args.n, seed=args.seed, family=args.workload),
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
+    line = dict(base, value=value, ms_per_step=1000 * dt / args.steps,
+                config=workload_config(n, int(csr[2][-1]), args.seed, args.workload),
+                cpu_baseline={"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
+                e2e={"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0})
     print(json.dumps(line), flush=True)
     return 0
 
@@ -481,30 +622,119 @@ def run_gb300(args, rank, world, local):
     e2e_max = dist.max(e2e_s)
     e2e_iters_all = dist.sum(e2e_iters)
 
-    cpu = (cpu_baseline_sample(seed=args.seed, family=args.workload) if (rank == 0 and world == 1 and not args.no_cpu)
+    cpu = (cpu_baseline_full(args.workload, game.n, args.seed) if (rank == 0 and world == 1 and not args.no_cpu)
            else None)
+    if cpu:
+        cpu["speedup"] = (iters_all / (ms_max / 1e3)) / cpu["value"]
+        cpu["e2e_speedup"] = (e2e_iters_all / e2e_max) / cpu["value"]
+    config = workload_config(game.n, game.m, args.seed, args.workload)
+    extras = {}
+    if world == 1 and args.workload == "single" and not args.no_extras:
+        del game, phase_solver, csr   # the 2^24 game's memory goes before the other workloads
+        extras = run_extras(args, dist, rank, world, local)
     if rank == 0:
         line = {
             "metric": METRIC, "value": iters_all / (ms_max / 1e3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic", "config": dict(workload_config(game.n, game.m, args.seed, args.workload),
-                                                **knobs, tuning=tuning,
-                                                iters_per_solve=iters // args.steps, brs_per_solve=brs // args.steps),
+            "data": "synthetic", "config": config,
+            "method": dict(METHOD, **knobs, tuning=tuning, iters_per_solve=iters // args.steps,
+                           brs_per_solve=brs // args.steps),
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
             "e2e": {"value": e2e_iters_all / e2e_max, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "list_ranking": lr, "random_access_peak": rpeak,
             "phase_ms_per_solve": {k: v[0] / args.steps for k, v in phases.items()},
             "counters_per_solve": {k: v / args.steps for k, v in counters.items()},
+            **extras,
         }
         print(json.dumps(line), flush=True)
     dist.close()
     return 0
 
 
+def gpu_solve_rate(psi, game, local, steps, warmup, tune=True):
+    """SI iterations per second of K solves of one game on the GPU (device
+    time, CUDA events on the solver stream; the game resident), and the same
+    end to end through the C ABI from page-locked host buffers (upload,
+    solve, read-back of the winning set and strategy)."""
+    knobs, tuning = {}, None
+    if tune:
+        o, tuning = psi.autotune(game, repeats=2, device=local)
+        knobs = dict(sublist_len=o.sublist_len, patch_limit=o.patch_limit, walk_block=o.walk_block)
+    s = psi.GPUList(game, device=local, **knobs)
+    for _ in range(warmup):
+        s.solve()
+    s.timer_begin()
+    iters = brs = 0
+    for _ in range(steps):
+        it, br = s.solve()
+        iters += it
+        brs += br
+    ms = s.timer_end()
+    s.close()
+    csr = []
+    for a in game.csr():
+        h = psi.pinned(len(a))
+        h[:] = a
+        csr.append(h)
+    out_w, out_s = psi.pinned(game.n), psi.pinned(game.n)
+    t0 = time.perf_counter()
+    e2e_iters = 0
+    for _ in range(steps):
+        s2 = psi.GPUList.from_csr(*csr, device=local, **knobs)
+        it, _ = s2.solve()
+        s2.get_winning(0, out=out_w)
+        s2.get_strategy(out=out_s)
+        s2.close()
+        e2e_iters += it
+    e2e_s = time.perf_counter() - t0
+    return {"value": iters / (ms / 1e3), "unit": UNIT, "ms_per_solve": ms / steps, "iters": iters // steps,
+            "brs": brs // steps, "steps": steps, "warmup": warmup,
+            "e2e": {"value": e2e_iters / e2e_s, "unit": UNIT, "ms_per_solve": 1000 * e2e_s / steps},
+            "options": dict(knobs, tuning=tuning)}
+
+
+def run_extras(args, dist, rank, world, local):
+    """The other measured configurations, compact, for the one-GPU line: the
+    reference CPU path's own n = 10,000 case on the GPU beside the dense
+    CPUParity restatement on the host, the 2^23 long-path game, 4,096 games
+    batched against one-by-one, and the continuous-batching server."""
+    import psi
+
+    out = {}
+    g = make_game(psi, "c1", C1_N, args.seed)
+    gpu = gpu_solve_rate(psi, g, local, steps=20, warmup=3)
+    cpu = cpu_c1(args.seed)
+    out["c1"] = {"config": workload_config(g.n, g.m, args.seed, "c1"), "gpu": gpu, "cpu_reference_port": cpu,
+                 "speedup_vs_one_core": gpu["value"] / cpu["one_core"]["si_iters_per_s"],
+                 "e2e_speedup_vs_one_core": gpu["e2e"]["value"] / cpu["one_core"]["si_iters_per_s"]}
+    del g
+    g = make_game(psi, "longpath", LONGPATH_N, args.seed)
+    out["longpath"] = dict(gpu_solve_rate(psi, g, local, steps=5, warmup=2),
+                           config=workload_config(g.n, g.m, args.seed, "longpath"))
+    del g
+    b = batch_measure(args, dist, rank, world, local, steps=3, warmup=1)
+    out["batch"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "config", "one_by_one",
+                                      "speedup_vs_one_by_one", "counts_match_solo")}
+    sv = serve_measure(args, dist, rank, world, local, warmup=1)
+    out["serve"] = {k: sv[k] for k in ("value", "unit", "config", "saturated", "poisson", "counts_match_solo",
+                                       "solo_checked")}
+    return out
+
+
 def run_batch(args, rank, world, local):
-    """Batched workload (not the headline line): `--batch-games` random games
+    """The batched workload as its own line (see batch_measure)."""
+    dist = Dist(world, local)
+    line = batch_measure(args, dist, rank, world, local, args.steps, args.warmup)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+    return 0
+
+
+def batch_measure(args, dist, rank, world, local, steps, warmup):
+    """Batched workload: `--batch-games` random games
     with sizes log-uniform in [100, 200000], out-degree U[2,8], priority
     U[0,n_i), solved together (psi_batch_solve) against the same kind of games
     solved one at a time on the same GPU (every `--solo-stride`-th game, each
@@ -515,7 +745,6 @@ def run_batch(args, rank, world, local):
     over ranks."""
     import psi
 
-    dist = Dist(world, local)
     sizes = psi.batch_sizes(args.batch_games, 100, 200000, args.seed)
     mine = psi.shard_games(sizes.astype(np.int64) + 1, world)[rank]
     games = [psi.Game.random(int(sizes[i]), 2, 8, int(sizes[i]), args.seed * 100003 + int(i)) for i in mine]
@@ -531,14 +760,14 @@ def run_batch(args, rank, world, local):
         sample = max(1, sum(g.n for g in games[::8]))
         knobs["patch_limit"] = max(1024, int(o.patch_limit * total / sample)) if o.patch_limit else 0
     batch = psi.Batch(games, device=local, **knobs)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         batch.solve()
     dist.barrier()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         it, br = batch.solve()
     dist.barrier()
-    t_batch = dist.max((time.perf_counter() - t0) / args.steps)
+    t_batch = dist.max((time.perf_counter() - t0) / steps)
     solo_idx = list(range(0, len(games), args.solo_stride))
     solvers = [psi.GPUList(games[k], device=local) for k in solo_idx]
     for s in solvers[:8]:
@@ -554,7 +783,7 @@ def run_batch(args, rank, world, local):
     max_it, max_br = int(dist.max(int(it.max()))), int(dist.max(int(br.max())))
     line = {
         "metric": "games/s (batched)", "value": len(sizes) / t_batch, "unit": "games/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t_batch, "higher_is_better": True,
+        "steps": steps, "warmup": warmup, "ms_per_step": 1000 * t_batch, "higher_is_better": True,
         "scaling": "strong", "dtype": "int32", "data": "synthetic",
         "config": {"workload": f"{len(sizes)} random games, n_i log-uniform in [100,200000], out-degree U[2,8], "
                                f"priority U[0,n_i)", "total_vertices": nv, "total_edges": ne,
@@ -565,10 +794,10 @@ def run_batch(args, rank, world, local):
         "speedup_vs_one_by_one": (len(sizes) / t_batch) / (n_solo / t_solo),
         "counts_match_solo": exact,
     }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    dist.close()
-    return 0
+    batch.close()
+    for s in solvers:
+        s.close()
+    return line
 
 
 def serve_once(srv, games, arrivals):
@@ -607,7 +836,17 @@ def serve_once(srv, games, arrivals):
 
 
 def run_serve(args, rank, world, local):
-    """Serving workload (not the headline line): `--serve-games` random games
+    """The serving workload as its own line (see serve_measure)."""
+    dist = Dist(world, local)
+    line = serve_measure(args, dist, rank, world, local, args.warmup)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+    return 0
+
+
+def serve_measure(args, dist, rank, world, local, warmup):
+    """Serving workload: `--serve-games` random games
     (sizes log-uniform in [--serve-lo, --serve-hi], default [10^3, 2*10^6],
     out-degree U[2,8], priority U[0,n_i)) arrive at one continuous-batching
     server (psi_server_*) whose arena holds `--arena-vertices` vertex slots.
@@ -621,7 +860,6 @@ def run_serve(args, rank, world, local):
     rank's."""
     import psi
 
-    dist = Dist(world, local)
     sizes = psi.batch_sizes(args.serve_games, args.serve_lo, args.serve_hi, args.seed)
     mine = psi.shard_games(sizes.astype(np.int64) + 1, world)[rank]
     games = [psi.Game.random(int(sizes[i]), 2, 8, int(sizes[i]), args.seed * 100003 + int(i)) for i in mine]
@@ -638,7 +876,7 @@ def run_serve(args, rank, world, local):
                      patch_limit=max(1024, args.arena_vertices // div) if div in (8, 16, 32, 64, 128, 256) else 0)
     srv = psi.Server(args.arena_vertices, 8 * args.arena_vertices, args.serve_slots, device=local, **knobs)
     warm = games[: max(4, len(games) // 16)]
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         serve_once(srv, warm, np.zeros(len(warm)))
     dist.barrier()
     el, lat, counts, steps, mres = serve_once(srv, games, np.zeros(len(games)))
@@ -665,7 +903,7 @@ def run_serve(args, rank, world, local):
     exact = dist.sum(bad) == 0
     line = {
         "metric": "games/s (served, saturated)", "value": sat, "unit": "games/s", "n_gpus": world,
-        "steps": 1, "warmup": args.warmup, "ms_per_step": 1000 * el, "higher_is_better": True,
+        "steps": 1, "warmup": warmup, "ms_per_step": 1000 * el, "higher_is_better": True,
         "scaling": "strong", "dtype": "int32", "data": "synthetic",
         "config": {"workload": f"{len(sizes)} random games served, n_i log-uniform in [{args.serve_lo},"
                                f"{args.serve_hi}], out-degree U[2,8], priority U[0,n_i)",
@@ -680,10 +918,8 @@ def run_serve(args, rank, world, local):
         "poisson": loads,
         "counts_match_solo": exact, "solo_checked": int(dist.sum(len(solo_idx))),
     }
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    dist.close()
-    return 0
+    srv.close()
+    return line
 
 
 def main():
@@ -703,10 +939,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--host-loop", action="store_true",
                     help="time the host-driven solve loop instead of the default one-graph solve")
-    ap.add_argument("--workload", choices=("single", "longpath", "batch", "serve"), default="single",
-                    help="single: the 2^24 game (headline); longpath: the 2^23 long-path game; batch: many "
-                         "mixed-size games solved together; serve: the same kind of games arriving at a "
-                         "continuous-batching server")
+    ap.add_argument("--workload", choices=("single", "longpath", "c1", "batch", "serve"), default="single",
+                    help="single: the 2^24 game (headline); longpath: the 2^23 long-path game; c1: the n=10,000 "
+                         "random game of the reference CPU path; batch: many mixed-size games solved together; "
+                         "serve: the same kind of games arriving at a continuous-batching server")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline line only: skip the c1, longpath, batch and serve sub-objects")
     ap.add_argument("--batch-games", type=int, default=4096)
     ap.add_argument("--solo-stride", type=int, default=16)
     ap.add_argument("--serve-games", type=int, default=256)
@@ -716,7 +954,7 @@ def main():
     ap.add_argument("--arena-vertices", type=int, default=1 << 25)
     args = ap.parse_args()
     if args.n <= 0:
-        args.n = LONGPATH_N if args.workload == "longpath" else N_DEFAULT
+        args.n = {"longpath": LONGPATH_N, "c1": C1_N}.get(args.workload, N_DEFAULT)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     rank, world, local = dist_env()

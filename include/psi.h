@@ -101,7 +101,15 @@ typedef struct {
                                 patch is tried (0, the default: max(1024, n/64)) */
     int32_t walk_block;      /* threads per block of the sublist walk (one thread per
                                 sublist): a multiple of 32 in [32, 1024]; 0, the default: 128 */
+    int32_t switch_kernel;   /* PSI_SWITCH_*: how the all-switches step maps vertices to threads
+                                (the same results either way) */
 } psi_options;
+
+/* switch_kernel: PSI_SWITCH_WARP (default) -- a warp takes 32 vertices and
+ * lays their successor lists end to end, one successor per lane per round,
+ * the per-vertex choice by a segmented warp scan; PSI_SWITCH_THREAD -- one
+ * thread per vertex walking its own successor list. */
+enum { PSI_SWITCH_WARP = 0, PSI_SWITCH_THREAD = 1 };
 
 /* incremental: PSI_INCR_AUTO (default) patches after steps that changed at
  * most patch_limit strategies, giving up for a full evaluation when more
@@ -152,6 +160,13 @@ int psi_get_solved(psi_solver *s, int32_t *out);
  * the reference's layout (cpu_parity.h:17, gpu_parity.cu:61-106); rows of
  * infinite vertices are zero. */
 int psi_get_valuation(psi_solver *s, int32_t v0, int32_t count, int32_t *out);
+
+/* The valuations of the last evaluation in path form (no counterpart in the
+ * reference, whose valuations are the dense rows above): per vertex, the
+ * length of its strategy path to the sink, the highest priority on that path
+ * and how many of the path's vertices carry it; (0, -1, 0) where the
+ * valuation is infinite.  n ints each; any pointer may be NULL. */
+int psi_get_path_summary(psi_solver *s, int32_t *depth, int32_t *top, int32_t *count);
 
 /* solve_si (main.cpp:20-55, gpumain.cpp:18-53): init_strat, then Odd's best
  * response (evaluate, mark_solved(1), switch(1) until no switch), then

@@ -287,6 +287,11 @@ int psi_get_valuation(psi_solver *s, int32_t v0, int32_t count, int32_t *out)
     PSI_SOLVER_CALL(s->s->get_valuation(v0, count, out));
 }
 
+int psi_get_path_summary(psi_solver *s, int32_t *depth, int32_t *top, int32_t *count)
+{
+    PSI_SOLVER_CALL(s->s->get_path_summary(depth, top, count));
+}
+
 int psi_solve(psi_solver *s, int32_t reset, int32_t *iter_count, int32_t *br_count, int64_t max_evals)
 {
     if (!iter_count || !br_count) return psi::fail(PSI_ERR_INVALID, "null output");

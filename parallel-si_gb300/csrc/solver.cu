@@ -39,6 +39,8 @@ int check_options(const psi_options &opt)
     if (opt.patch_limit < 0) return fail(PSI_ERR_INVALID, "patch_limit must be >= 0");
     if (opt.walk_block != 0 && (opt.walk_block < 32 || opt.walk_block > 1024 || opt.walk_block % 32 != 0))
         return fail(PSI_ERR_INVALID, "walk_block must be 0 or a multiple of 32 in [32, 1024]");
+    if (opt.switch_kernel != PSI_SWITCH_WARP && opt.switch_kernel != PSI_SWITCH_THREAD)
+        return fail(PSI_ERR_INVALID, "unknown switch_kernel");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0) return fail(PSI_ERR_NO_DEVICE, "no CUDA device available");
@@ -63,6 +65,7 @@ int Solver::create(const CsrView &g, const psi_options &opt, Solver **out, bool 
     s->incremental_ = opt.incremental;
     s->patch_limit_ = opt.patch_limit;
     s->walk_block_ = opt.walk_block ? opt.walk_block : kWalkBlock;
+    s->switch_warp_ = opt.switch_kernel == PSI_SWITCH_WARP;
     rc = s->alloc_arrays(g.n, g.m);
     if (!rc) rc = s->upload_game(g, validate);
     if (rc) {
@@ -90,6 +93,7 @@ int Solver::create_arena(int64_t max_vertices, int64_t max_edges, int32_t slots,
     s->incremental_ = opt.incremental;
     s->patch_limit_ = opt.patch_limit;
     s->walk_block_ = opt.walk_block ? opt.walk_block : kWalkBlock;
+    s->switch_warp_ = opt.switch_kernel == PSI_SWITCH_WARP;
     rc = s->alloc_arrays(max_vertices, max_edges);
     if (!rc) rc = s->init_arena(slots);
     if (rc) {
@@ -138,6 +142,7 @@ int Solver::create_union(const std::vector<const HostGame *> &gs, const psi_opti
     s->incremental_ = opt.incremental;
     s->patch_limit_ = opt.patch_limit;
     s->walk_block_ = opt.walk_block ? opt.walk_block : kWalkBlock;
+    s->switch_warp_ = opt.switch_kernel == PSI_SWITCH_WARP;
     rc = s->alloc_arrays(n, m);
     if (!rc) rc = s->upload_union(gs, table, base->back());
     if (rc) {
@@ -623,7 +628,8 @@ int Solver::switch_strategy(int32_t player, int64_t *switched)
     const int32_t *pl = plist_ + (player == 0 ? 0 : np0_);
     // jB_ is free until the next cycle pass: it holds the list of vertices to examine
     launch_switch(stream_, np, pl, player, off_, tgt_, strat_, st_, key_, node_, dw_->sw, game_of_, gcount_, gmask_,
-                  dirty_, &dw_->err, nullptr, need_, reinterpret_cast<int32_t *>(jB_), &dw_->cnt[2], changes(), tie_, watch_, skip_);
+                  dirty_, &dw_->err, nullptr, need_, reinterpret_cast<int32_t *>(jB_), &dw_->cnt[2], changes(), tie_,
+                  watch_, skip_, switch_warp_);
     phase_end(PH_SWITCH);
     rc = sync_and_check("switch_strategy");
     if (rc) return rc;
@@ -723,6 +729,25 @@ int Solver::get_solved(int32_t *out)
     PSI_CUDA_TRY(cudaMemcpyAsync(s.data(), solved_, n_, cudaMemcpyDeviceToHost, stream_));
     PSI_CUDA_TRY(cudaStreamSynchronize(stream_));
     for (int32_t v = 0; v < n_; v++) out[v] = s[v];
+    return PSI_OK;
+}
+
+int Solver::get_path_summary(int32_t *depth, int32_t *top, int32_t *count)
+{
+    if (!val_ready_) return fail(PSI_ERR_STATE, "get_path_summary before compute_valuation");
+    int rc = set_device();
+    if (rc) return rc;
+    std::vector<int32_t> st(n_);
+    std::vector<PathNode> nd(n_);
+    PSI_CUDA_TRY(cudaMemcpyAsync(st.data(), st_, 4 * (size_t)n_, cudaMemcpyDeviceToHost, stream_));
+    PSI_CUDA_TRY(cudaMemcpyAsync(nd.data(), node_, sizeof(PathNode) * (size_t)n_, cudaMemcpyDeviceToHost, stream_));
+    PSI_CUDA_TRY(cudaStreamSynchronize(stream_));
+    for (int32_t v = 0; v < n_; v++) {
+        const bool fin = st[v] >= 1;
+        if (depth) depth[v] = fin ? st[v] : 0;
+        if (top) top[v] = fin ? nd[v].rmax : -1;
+        if (count) count[v] = fin ? nd[v].rcnt : 0;
+    }
     return PSI_OK;
 }
 

@@ -86,6 +86,9 @@ public:
     int get_infinite(int32_t *out);
     int get_solved(int32_t *out);
     int get_depth(int32_t *out);
+    // Per vertex after the last evaluation: path length to the sink, top
+    // priority on the path and its count ((0, -1, 0) where infinite).
+    int get_path_summary(int32_t *depth, int32_t *top, int32_t *count);
     int get_valuation(int32_t v0, int32_t count, int32_t *out);
     int solve(int32_t reset, int32_t *iters, int32_t *brs, int64_t max_evals);
     // The same loop as one CUDA graph launch (solver_graph.cu).
@@ -215,6 +218,7 @@ private:
     int32_t incremental_ = 1;   // psi_options.incremental
     int32_t patch_limit_ = 0;   // psi_options.patch_limit
     int32_t walk_block_ = kWalkBlock;   // psi_options.walk_block (0 there: kWalkBlock)
+    bool switch_warp_ = true;           // psi_options.switch_kernel == PSI_SWITCH_WARP
     int32_t *clist_ = nullptr, *alist_ = nullptr, *apos_ = nullptr;
     int4 *pj_ = nullptr;
     int32_t ccap_ = 0, acap_ = 0, max_levels_ = 0;

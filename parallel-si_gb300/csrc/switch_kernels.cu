@@ -341,6 +341,216 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
     }
 }
 
+// ---- warp-cooperative all-switches
+// A warp takes 32 entries of the list at a time (one vertex per lane) and
+// lays their successor lists end to end; every lane then gathers one
+// successor and its key per round of 32 edges, whatever the degrees.  The
+// switch rule is a prefix maximum: with score = key for Even and -key for Odd
+// (a strict improvement for the owner is a strictly larger score), the running
+// choice before successor j is the first vertex attaining the maximum score
+// over the incumbent and the successors before j; j is a strict improvement
+// (a move) iff its score exceeds that maximum.  A segmented warp scan (one
+// segment per vertex, max with the earlier element winning ties, the
+// incumbent as the carry into the first round) gives every lane that running
+// choice, so the moves of a vertex are the improving lanes of its segment and
+// its final choice is the scan's last value.  Equal scores of distinct finite
+// vertices mean that the keys cannot tell: such a vertex is redone by its
+// lane with the exact comparisons (summaries, then walks), as in k_switch.
+struct ScoreArg {
+    int32_t sc, u;
+};
+
+// the earlier element wins ties (first strict maximum)
+__device__ __forceinline__ ScoreArg first_max(ScoreArg a, ScoreArg b) { return (a.sc >= b.sc) ? a : b; }
+
+__global__ void __launch_bounds__(kBlock) k_switch_warp(int32_t np, const int32_t *__restrict__ plist,
+                                                        const int32_t *__restrict__ count, int32_t player,
+                                                        const int32_t *__restrict__ off,
+                                                        const int32_t *__restrict__ tgt, int32_t *__restrict__ strat,
+                                                        const int32_t *__restrict__ st,
+                                                        const int32_t *__restrict__ key,
+                                                        const PathNode *__restrict__ node,
+                                                        unsigned long long *__restrict__ stats,
+                                                        const int32_t *__restrict__ game_of,
+                                                        unsigned long long *__restrict__ gcount,
+                                                        const int32_t *__restrict__ gmask,
+                                                        uint8_t *__restrict__ dirty, uint32_t *__restrict__ err,
+                                                        const int32_t *__restrict__ gate, uint8_t *__restrict__ need,
+                                                        ChangeList changes, uint8_t *__restrict__ tie_out,
+                                                        uint8_t *__restrict__ watch, const int4 *__restrict__ skip)
+{
+    if (gate && !*gate) return;
+    if (count) np = *count;
+    constexpr unsigned kAll = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int32_t sgn = (player == 0) ? 1 : -1;   // score = sgn * key
+    int32_t t_edges = 0, t_loads = 0, t_changed = 0, t_moves = 0;
+    for (int64_t g0 = warp * 32; g0 < np; g0 += nwarps * 32) {
+        // this lane's vertex
+        const int64_t i = g0 + lane;
+        int32_t v = -1, cur0 = -1, e0 = 0, deg = 0;
+        if (i < np) {
+            v = __ldcs(&plist[i]);
+            if (gmask && !gmask[game_of[v]]) v = -1;
+        }
+        if (v >= 0) {
+            cur0 = strat[v];
+            e0 = __ldcs(&off[v]);
+            deg = __ldcs(&off[v + 1]) - e0;
+        }
+        const int32_t kc0 = (cur0 >= 0) ? key[cur0] : 0;
+        // successor lists end to end: base = exclusive prefix of the degrees
+        int32_t incl = deg;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(kAll, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int32_t base = incl - deg;
+        const int32_t total = __shfl_sync(kAll, incl, 31);
+        // per vertex (held by its lane): running choice, moves, tie, exact
+        ScoreArg run = {sgn * kc0, cur0};
+        int32_t moves = 0;
+        bool tie = false, exact = false;
+        for (int32_t c = 0; c < total; c += 32) {
+            const int32_t t = c + lane;
+            const bool valid = t < total;
+            // the lane whose segment holds edge t: the last lane with base <= t
+            int32_t seg = 0;
+#pragma unroll
+            for (int step = 16; step; step >>= 1) {
+                const int32_t b = __shfl_sync(kAll, base, seg + step);
+                if (b <= t) seg += step;
+            }
+            const int32_t sb = __shfl_sync(kAll, base, seg), se0 = __shfl_sync(kAll, e0, seg);
+            int32_t u = -1, k = 0;
+            if (valid) {
+                u = __ldcs(&tgt[se0 + (t - sb)]);
+                k = key[u];
+            }
+            ScoreArg x = {valid ? sgn * k : INT_MIN, u};
+            // segmented inclusive scan (segments are runs of equal seg)
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int32_t osc = __shfl_up_sync(kAll, x.sc, o), ou = __shfl_up_sync(kAll, x.u, o);
+                const int32_t oseg = __shfl_up_sync(kAll, seg, o);
+                if (lane >= o && oseg == seg && osc >= x.sc) {
+                    x.sc = osc;
+                    x.u = ou;
+                }
+            }
+            // the running choice before this edge: the segment's carry, then
+            // the inclusive value of the previous lane of the same segment
+            const ScoreArg carry = {__shfl_sync(kAll, run.sc, seg), __shfl_sync(kAll, run.u, seg)};
+            const int32_t psc = __shfl_up_sync(kAll, x.sc, 1), pu = __shfl_up_sync(kAll, x.u, 1);
+            const int32_t pseg = __shfl_up_sync(kAll, seg, 1);
+            const bool first = (lane == 0) || (pseg != seg);
+            const ScoreArg excl = first ? carry : first_max(carry, ScoreArg{psc, pu});
+            const int32_t sc = valid ? sgn * k : INT_MIN;
+            const bool rec = valid && sc > excl.sc;
+            const bool eqd = valid && sc == excl.sc && u != excl.u;
+            const bool exd = eqd && !key_infinite(k);
+            const unsigned recm = __ballot_sync(kAll, rec), eqm = __ballot_sync(kAll, eqd);
+            const unsigned exm = __ballot_sync(kAll, exd);
+            const ScoreArg last = first_max(carry, x);   // inclusive, with the carry
+            // each vertex lane collects its segment's lanes of this round
+            const int32_t lo = base - c, hi = base + deg - c;   // [lo, hi) of this round's lanes
+            int32_t lastlane = 0;
+            unsigned segm = 0;
+            if (deg > 0 && hi > 0 && lo < 32) {
+                const int32_t a = lo > 0 ? lo : 0, b = hi < 32 ? hi : 32;
+                segm = (b - a == 32) ? kAll : (((1u << (b - a)) - 1u) << a);
+                lastlane = b - 1;
+            }
+            const int32_t lsc = __shfl_sync(kAll, last.sc, lastlane), lu = __shfl_sync(kAll, last.u, lastlane);
+            if (segm) {
+                const unsigned r = recm & segm;
+                moves += __popc(r);
+                if (r) {
+                    const int top = 31 - __clz(r);
+                    tie = (top < 31) && ((eqm & segm) >> (top + 1)) != 0;
+                } else {
+                    tie = tie || (eqm & segm) != 0;
+                }
+                exact = exact || (exm & segm) != 0;
+                run.sc = lsc;
+                run.u = lu;
+            }
+        }
+        int32_t cur = run.u;
+        int32_t ext = sgn * run.sc;   // the best key (the owner's view), as a key
+        if (v >= 0 && exact) {
+            // the keys cannot order two distinct finite vertices: redo this
+            // vertex with the exact comparisons, successor by successor
+            cur = cur0;
+            int32_t kc = kc0;
+            moves = 0;
+            ext = kc0;
+            int32_t ext_v = cur0;
+            tie = false;
+            for (int32_t e = e0; e < e0 + deg; e++) {
+                const int32_t uu = tgt[e], ku = key[uu];
+                if ((player == 0) ? ku > ext : ku < ext) {
+                    ext = ku;
+                    ext_v = uu;
+                    tie = false;
+                } else if (ku == ext && uu != ext_v) {
+                    tie = true;
+                }
+                int cmp;
+                if (ku != kc) cmp = ku > kc ? 1 : -1;
+                else if (uu == cur || key_infinite(ku)) cmp = 0;
+                else cmp = compare_equal_keys(node, skip, st, uu, cur, t_loads, err);
+                if ((player == 0 && cmp > 0) || (player == 1 && cmp < 0)) {
+                    cur = uu;
+                    kc = ku;
+                    moves++;
+                }
+            }
+        }
+        if (v >= 0) {
+            t_edges += deg;
+            const bool sticky = tie && ext != 0 && !key_infinite(ext);
+            if (tie_out) {
+                need[v] = 0;
+                tie_out[v] = sticky ? 1 : 0;
+                if (sticky && watch)   // the successors the tie rests on
+                    for (int32_t e = e0; e < e0 + deg; e++) {
+                        const int32_t uu = tgt[e];
+                        if (key[uu] == ext) watch[uu] = 1;
+                    }
+            } else if (need) {
+                need[v] = sticky ? 1 : 0;
+            }
+            if (moves) {   // strict improvements never return to cur0: cur != cur0
+                strat[v] = cur;
+                if (cur0 >= 0) dirty[cur0] = 1;
+                if (cur >= 0) dirty[cur] = 1;
+                if (game_of) atomicAdd(&gcount[game_of[v]], (unsigned long long)moves);
+                t_changed++;
+                t_moves += moves;
+            }
+        }
+        if (changes.list) {   // warp-collective (coalesced lanes)
+            if (v >= 0 && moves) note_change(changes, v);
+        }
+    }
+    typedef cub::BlockReduce<longlong4, kBlock> Reduce;
+    __shared__ typename Reduce::TempStorage tmp;
+    longlong4 mine = make_longlong4(t_edges, t_loads, t_changed, t_moves);
+    longlong4 tot = Reduce(tmp).Reduce(mine, [](const longlong4 &x, const longlong4 &y) {
+        return make_longlong4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w);
+    });
+    if (threadIdx.x == 0) {
+        if (tot.x) atomicAdd(&stats[0], (unsigned long long)tot.x);
+        if (tot.y) atomicAdd(&stats[1], (unsigned long long)tot.y);
+        if (tot.z) atomicAdd(&stats[2], (unsigned long long)tot.z);
+        if (tot.w) atomicAdd(&stats[3], (unsigned long long)tot.w);
+    }
+}
+
 // Per-game accounting of the solve_si loop (main.cpp:20-55) run over a batch
 // of games packed as one disjoint union.  Paths never leave their game, so a
 // game's strategies and valuations evolve exactly as in a solo solve; a game
@@ -421,7 +631,7 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
                    unsigned long long *stats, const int32_t *game_of, unsigned long long *gcount,
                    const int32_t *gmask, uint8_t *dirty, uint32_t *err, const int32_t *gate, uint8_t *need,
                    int32_t *list, int32_t *list_count, ChangeList changes, uint8_t *tie, uint8_t *watch,
-                   const int4 *skip)
+                   const int4 *skip, bool warp)
 {
     if (np <= 0) return;
     const int blocks = per_device(g_switch_blocks, switch_grid);   // four waves of resident blocks
@@ -439,8 +649,12 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
         count = list_count;
     }
     count_launch();
-    k_switch<<<g, kBlock, 0, s>>>(np, items, count, player, off, tgt, strat, st, key, node, stats, game_of, gcount,
-                                  gmask, dirty, err, gate, need, changes, tie, watch, skip);
+    if (warp)
+        k_switch_warp<<<g, kBlock, 0, s>>>(np, items, count, player, off, tgt, strat, st, key, node, stats, game_of,
+                                           gcount, gmask, dirty, err, gate, need, changes, tie, watch, skip);
+    else
+        k_switch<<<g, kBlock, 0, s>>>(np, items, count, player, off, tgt, strat, st, key, node, stats, game_of,
+                                      gcount, gmask, dirty, err, gate, need, changes, tie, watch, skip);
 }
 
 void launch_batch_account(cudaStream_t s, int32_t games, int32_t event, int4 *state, unsigned long long *gcount,

@@ -239,6 +239,14 @@ class GPUList:
         check(lib.psi_get_valuation(self._h, v0, count, ptr(out)))
         return out
 
+    def get_summary(self):
+        """(path length to the sink, top priority on the path, its count) per
+        vertex after the last evaluation; (0, -1, 0) where the valuation is
+        infinite (psi_get_path_summary)."""
+        d, t, c = (np.empty(self.n, np.int32) for _ in range(3))
+        check(lib.psi_get_path_summary(self._h, ptr(d), ptr(t), ptr(c)))
+        return d, t, c
+
     def solve(self, reset: bool = False, max_evals: int = 0):
         it = C.c_int32()
         br = C.c_int32()

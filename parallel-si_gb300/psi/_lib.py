@@ -53,6 +53,7 @@ class Options(C.Structure):
         ("incremental", C.c_int32),
         ("patch_limit", C.c_int32),
         ("walk_block", C.c_int32),
+        ("switch_kernel", C.c_int32),
     ]
 
 
@@ -98,6 +99,7 @@ _SIGS = {
     "psi_get_infinite": ([_vp, _vp], C.c_int),
     "psi_get_solved": ([_vp, _vp], C.c_int),
     "psi_get_valuation": ([_vp, C.c_int32, C.c_int32, _vp], C.c_int),
+    "psi_get_path_summary": ([_vp, _vp, _vp, _vp], C.c_int),
     "psi_solve": ([_vp, C.c_int32, _i32p, _i32p, C.c_int64], C.c_int),
     "psi_solver_times": ([_vp, C.POINTER(C.c_double), C.POINTER(C.c_double), _i64p, _i64p], C.c_int),
     "psi_solver_reset_times": ([_vp], C.c_int),

@@ -26,8 +26,17 @@ def compare_states(a, b, where):
         assert bad.size == 0, f"{where}: valuations differ at vertices {bad[:10]}"
 
 
-def lockstep(x, y, reset=False, rows=True, max_evals=100000):
-    """Drive x and y together; returns (iters, brs)."""
+def compare_summaries(x, y, where):
+    """Path-form valuations (path length, top priority, its count per vertex)
+    of two solvers that both have get_summary()."""
+    for name, a, b in zip(("path lengths", "top priorities", "top counts"), x.get_summary(), y.get_summary()):
+        assert np.array_equal(a, b), f"{where}: {name} differ at {np.nonzero(a != b)[0][:10]}"
+
+
+def lockstep(x, y, reset=False, rows=True, max_evals=100000, summary=False):
+    """Drive x and y together; returns (iters, brs).  rows: compare the dense
+    valuation rows after every evaluation; summary: compare the path-form
+    summaries instead (for games whose dense rows would not fit)."""
     x.init_strat()
     y.init_strat()
     assert np.array_equal(x.get_strategy(), y.get_strategy()), "init_strat differs"
@@ -46,6 +55,8 @@ def lockstep(x, y, reset=False, rows=True, max_evals=100000):
                 y.compute_valuation()
             brs += 1
             compare_states(state_digest(x, rows), state_digest(y, rows), f"evaluation {brs}")
+            if summary:
+                compare_summaries(x, y, f"evaluation {brs}")
             x.mark_solved(1)
             y.mark_solved(1)
             a = x.switch_strategy(1)

@@ -78,7 +78,7 @@ def test_pinned_host_memory_needs_a_device():
 def test_invalid_options_rejected_before_device_use():
     g = psi.Game.random(100, 2, 4, 100, 1)
     for bad in (dict(sublist_len=1), dict(valuation_mode=7), dict(walk_block=48), dict(walk_block=2048),
-                dict(walk_block=-32)):
+                dict(walk_block=-32), dict(switch_kernel=2), dict(switch_kernel=-1)):
         o = psi.default_options(**bad)
         h = C.c_void_p()
         rc = lib.psi_solver_create(g._h, C.byref(o), C.byref(h))

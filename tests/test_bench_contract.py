@@ -12,14 +12,33 @@ sys.path.insert(0, ROOT)
 import bench  # noqa: E402
 
 
-def test_reference_arm_prints_one_complete_line():
+# runs the reference arm in-process, then reports whether the product package
+# or its CUDA library was loaded on the way
+_PROBE = """
+import json, runpy, sys
+sys.argv = ["bench.py"] + sys.argv[1:]
+try:
+    runpy.run_path(sys.argv[0], run_name="__main__")
+except SystemExit:
+    pass
+maps = open("/proc/self/maps").read()
+print(json.dumps({"psi_imported": "psi" in sys.modules, "libpsi_mapped": "libpsi_gb300" in maps}))
+"""
+
+
+def _reference_arm(*extra):
     env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
-    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
-                        "--warmup", "3"], env=env, capture_output=True, text=True, timeout=600)
+    r = subprocess.run([sys.executable, "-c", _PROBE, "--impl", "reference", *extra], cwd=ROOT, env=env,
+                       capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
     lines = [x for x in r.stdout.splitlines() if x.strip()]
-    assert len(lines) == 1
-    d = json.loads(lines[0])
+    assert len(lines) == 2, r.stdout
+    return json.loads(lines[0]), json.loads(lines[1])
+
+
+def test_reference_arm_prints_one_complete_line():
+    d, probe = _reference_arm("--n", "65536", "--steps", "2", "--warmup", "3")
+    assert probe == {"psi_imported": False, "libpsi_mapped": False}, "the reference arm must not load the product"
     for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
               "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
         assert k in d, k
@@ -29,6 +48,14 @@ def test_reference_arm_prints_one_complete_line():
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert "workload" in d["config"]
+    # the same workload description as this arm's own line
+    assert d["config"] == bench.workload_config(65536, d["config"]["m"], 1, "single")
+
+
+def test_reference_arm_c1_is_the_dense_restatement_on_one_thread():
+    d, probe = _reference_arm("--workload", "c1", "--steps", "1", "--warmup", "3")
+    assert not probe["psi_imported"] and not probe["libpsi_mapped"]
+    assert d["config"]["n"] == 10000 and d["cpu_baseline"]["cores"] == 1 and d["value"] > 0
 
 
 def test_phase_byte_formulas():

@@ -45,6 +45,27 @@ def test_gpu_lockstep_with_oracle(fam, n, seed, reset):
     lockstep(gpu, ref, reset=reset, rows=(n * (g.max_pri + 1) <= 2e8))
 
 
+@pytest.mark.parametrize("fam,n,seed,reset", [("c2", 4000, 61, False), ("smallpri", 3000, 62, True),
+                                               ("c1", 10000, 63, False), ("c3", 5000, 64, False)])
+def test_gpu_thread_per_vertex_switch_matches_oracle(fam, n, seed, reset):
+    """The thread-per-vertex switch kernel (psi_options.switch_kernel) gives
+    what the default warp-cooperative one gives: the oracle's steps."""
+    g = make(fam, n, seed)
+    gpu = psi.GPUList(g, switch_kernel=1)
+    ref = oracle.Oracle(*g.csr())
+    lockstep(gpu, ref, reset=reset, rows=(n * (g.max_pri + 1) <= 2e8))
+
+
+def test_gpu_switch_kernels_agree_on_high_degree_vertices():
+    """Vertices whose successor lists span several rounds of 32 edges, and
+    lists shared unevenly over a warp: a random game with out-degree up to
+    200 and few priorities (many equal keys), warp and thread kernels in
+    lockstep with the oracle."""
+    g = psi.Game.random(3000, 1, 200, 12, seed=65)
+    for kernel in (0, 1):
+        lockstep(psi.GPUList(g, switch_kernel=kernel), oracle.Oracle(*g.csr()))
+
+
 @pytest.mark.parametrize("stride", [2, 3, 17, 64, 500])
 def test_gpu_sublist_stride_does_not_change_results(stride):
     g = make("c2", 3000, 41)

@@ -25,8 +25,9 @@ FAMILIES = [("c1", 3000, 1), ("c2", 4000, 2), ("c3", 2000, 3), ("c4", 3000, 4), 
 
 def test_options_layout_and_default():
     from psi._lib import Options
-    assert C.sizeof(Options) == 32
+    assert C.sizeof(Options) == 36
     assert psi.default_options().incremental == AUTO
+    assert psi.default_options().switch_kernel == 0   # PSI_SWITCH_WARP
 
 
 def test_unknown_incremental_mode_is_rejected_before_device_use():
