@@ -23,4 +23,6 @@ if [ -f "$REF_DIR/cpu_parity.cpp" ] && [ -f "$REF_DIR/game.cpp" ]; then
         "$REF_DIR/game.cpp" "$REF_DIR/cpu_parity.cpp" "$HERE/ref_driver.cpp"
     # the reference's own 10-vertex fixture, for the test that pins the ring10 family
     if [ -f "$REF_DIR/test2.gm" ]; then cp "$REF_DIR/test2.gm" "$HERE/_ref/test2.gm"; fi
+    # where the sources lie, for the test that compiles the reference-side adapter
+    echo "$REF_DIR" > "$HERE/_ref/REF_DIR"
 fi
