@@ -280,7 +280,15 @@ def phase_bytes(phase, n, m, nsub, counters, calls, n_even, n_odd, iters, brs):
     if phase == "sublist":
         return 4 * L + 8 * n + 8 * nsub          # successor per node, (sublist, prefix) per vertex, reduced list
     if phase == "tour":
-        return 14 * n                             # dirty flags, vloc reset, sink-list scan (strategy, solved)
+        # per vertex: dirty flag, vloc reset (8 B), sink-list scan (strategy, solved);
+        # per (re)linked parent: its list entry, solved flag, in-list bounds and the
+        # closing successor write (17 B); per in-neighbour entry scanned: the entry
+        # and the neighbour's strategy (8 B); per child linked: a successor write (4 B)
+        if not counters or "tour_parents" not in counters:
+            return 14 * n
+        full = max(1, calls)
+        return 14 * n + (17 * counters["tour_parents"] + 8 * counters["tour_entries"]
+                         + 4 * counters["tour_children"]) / full
     if phase == "broadcast":
         # broadcast: vloc, solved, strategy, priority in; status, PathNode out (37 B);
         # root-path summaries: status and PathNode in, summary and key out (32 B)

@@ -213,7 +213,9 @@ int psi_solver_debug_inject_error(psi_solver *s, int32_t after_evals, uint32_t b
  * steps, compared edges, parent/priority loads of the comparison walks,
  * vertices whose strategy changed, unreached vertices (summed over full
  * evaluations), pointer-jumping rounds, incremental evaluations (patches),
- * vertices the patches re-evaluated.  Writes min(k, 9) values. */
+ * vertices the patches re-evaluated, and of the Euler-tour build and upkeep:
+ * parents whose child lists were (re)linked, in-neighbour entries they
+ * scanned, children they linked.  Writes min(k, 12) values. */
 int psi_solver_counters(psi_solver *s, int64_t *out, int32_t k);
 /* Kernel launches issued by this library in this process so far. */
 int64_t psi_launch_count(void);

@@ -336,8 +336,8 @@ int psi_solver_counters(psi_solver *s, int64_t *out, int32_t k)
 {
     if (!s || !s->s || !out) return psi::fail(PSI_ERR_INVALID, "null argument");
     const psi::SolverTimes &t = s->s->times();
-    const int64_t vals[] = {t.evals,     t.switches,    t.sw_edges, t.sw_loads, t.sw_changed,
-                            t.unreached, t.jump_rounds, t.patches,  t.patched};
+    const int64_t vals[] = {t.evals,     t.switches,    t.sw_edges, t.sw_loads,     t.sw_changed,   t.unreached,
+                            t.jump_rounds, t.patches, t.patched,  t.tour_parents, t.tour_entries, t.tour_children};
     for (int32_t i = 0; i < k && i < (int32_t)(sizeof vals / sizeof vals[0]); i++) out[i] = vals[i];
     return PSI_OK;
 }

@@ -106,6 +106,27 @@ __global__ void k_tour_init(int32_t n, int32_t *__restrict__ succ, int2 *__restr
     }
 }
 
+// Work counters of the tour kernels, one set of atomics per block:
+// stats[0] += parents linked, [1] += in-neighbour entries scanned, [2] +=
+// children linked (stats == nullptr: none).  Every thread of the block calls it.
+__device__ __forceinline__ void add_relink_stats(unsigned long long *stats, int32_t parents, int32_t entries,
+                                                 int32_t children)
+{
+    if (!stats) return;
+    __shared__ unsigned long long acc[3];
+    if (threadIdx.x == 0) acc[0] = acc[1] = acc[2] = 0;
+    __syncthreads();
+    if (parents) atomicAdd(&acc[0], (unsigned long long)parents);
+    if (entries) atomicAdd(&acc[1], (unsigned long long)entries);
+    if (children) atomicAdd(&acc[2], (unsigned long long)children);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (acc[0]) atomicAdd(&stats[0], acc[0]);
+        if (acc[1]) atomicAdd(&stats[1], acc[1]);
+        if (acc[2]) atomicAdd(&stats[2], acc[2]);
+    }
+}
+
 // Thread p: (a) if p is a live child of the sink, append it to the sink list;
 // (b) if p is live, link its children, found among its distinct in-neighbours
 // rev_src[rev_off[p] .. rev_off[p+1]), as
@@ -117,9 +138,11 @@ __global__ void k_tour_init(int32_t n, int32_t *__restrict__ succ, int2 *__restr
 __global__ void k_tour_link(int32_t n, const int32_t *__restrict__ strat, const uint8_t *__restrict__ solved,
                             const int32_t *__restrict__ rev_off, const int32_t *__restrict__ rev_src,
                             int32_t *__restrict__ succ, int32_t *__restrict__ sinklist,
-                            int32_t *__restrict__ sinkcount, const int32_t *__restrict__ gate)
+                            int32_t *__restrict__ sinkcount, const int32_t *__restrict__ gate,
+                            unsigned long long *__restrict__ stats)
 {
     if (gate && !*gate) return;
+    int32_t t_parents = 0, t_entries = 0, t_children = 0;
     // grid-stride with block-uniform passes (block_append needs every thread)
     for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < n; b0 += (int64_t)gridDim.x * blockDim.x) {
         const int32_t p = (int32_t)(b0 + threadIdx.x);
@@ -127,16 +150,20 @@ __global__ void k_tour_link(int32_t n, const int32_t *__restrict__ strat, const 
         block_append(live && strat[p] < 0, p, sinklist, sinkcount);
         if (!live) continue;
         int32_t prev = -1;
-        const int32_t e1 = rev_off[p + 1];
-        for (int32_t e = rev_off[p]; e < e1; e++) {
+        const int32_t e0 = rev_off[p], e1 = rev_off[p + 1];
+        t_parents++;
+        t_entries += e1 - e0;
+        for (int32_t e = e0; e < e1; e++) {
             int32_t u = rev_src[e];
             if (strat[u] != p) continue;
             if (prev < 0) succ[2 * (int64_t)p + 1] = 2 * u + 1;
             else succ[2 * (int64_t)prev] = 2 * u + 1;
             prev = u;
+            t_children++;
         }
         if (prev >= 0) succ[2 * (int64_t)prev] = 2 * p;
     }
+    add_relink_stats(stats, t_parents, t_entries, t_children);
 }
 
 // Incremental tour maintenance.  Between evaluations the tour lists persist
@@ -177,18 +204,23 @@ __global__ void k_dirty_list(int32_t n, uint8_t *__restrict__ dirty, int32_t *__
 __global__ void k_tour_relink(const int32_t *__restrict__ list, const int32_t *__restrict__ count,
                               const int32_t *__restrict__ strat, const uint8_t *__restrict__ solved,
                               const int32_t *__restrict__ rev_off, const int32_t *__restrict__ rev_src,
-                              int32_t *__restrict__ succ, const int32_t *__restrict__ gate)
+                              int32_t *__restrict__ succ, const int32_t *__restrict__ gate,
+                              unsigned long long *__restrict__ stats)
 {
     if (gate && !*gate) return;
     const int32_t k = *count;
+    int32_t t_parents = 0, t_entries = 0, t_children = 0;
     for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k; i += gridDim.x * blockDim.x) {
         const int32_t p = list[i];
         const bool live = !solved[p];
         int32_t prev = -1;
-        const int32_t e1 = rev_off[p + 1];
-        for (int32_t e = rev_off[p]; e < e1; e++) {
+        const int32_t e0 = rev_off[p], e1 = rev_off[p + 1];
+        t_parents++;
+        t_entries += e1 - e0;
+        for (int32_t e = e0; e < e1; e++) {
             int32_t u = rev_src[e];
             if (strat[u] != p) continue;
+            t_children++;
             if (!live) {
                 succ[2 * (int64_t)u] = 2 * u + 1;
                 continue;
@@ -200,6 +232,7 @@ __global__ void k_tour_relink(const int32_t *__restrict__ list, const int32_t *_
         if (prev >= 0) succ[2 * (int64_t)prev] = 2 * p;
         else succ[2 * (int64_t)p + 1] = 2 * p;
     }
+    add_relink_stats(stats, t_parents, t_entries, t_children);
 }
 
 // The sink's live children (the full build collects them in k_tour_link).
@@ -648,13 +681,13 @@ void launch_reset_odd(cudaStream_t s, int32_t n, const int8_t *owner, const int3
 void launch_tour_build(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
                        const int32_t *rev_off, const int32_t *rev_src, int32_t *succ, int2 *vloc,
                        int32_t *sinklist, int32_t *sinkcount, uint8_t *dirty, const int32_t *gate,
-                       const uint8_t *tie, uint8_t *need)
+                       const uint8_t *tie, uint8_t *need, unsigned long long *stats)
 {
     count_launch();
     k_tour_init<<<capped_grid((int64_t)n + 1), kBlock, 0, s>>>(n, succ, vloc, dirty, gate, tie, need);
     count_launch();
     k_tour_link<<<capped_grid(n), kBlock, 0, s>>>(n, strat, solved, rev_off, rev_src, succ, sinklist, sinkcount,
-                                                  gate);
+                                                  gate, stats);
     count_launch();
     unsigned g = grid_for(n);
     k_sink_chain<<<g < 1216u ? g : 1216u, kBlock, 0, s>>>(n, sinklist, sinkcount, succ, gate);
@@ -663,7 +696,7 @@ void launch_tour_build(cudaStream_t s, int32_t n, const int32_t *strat, const ui
 int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
                        const int32_t *rev_off, const int32_t *rev_src, uint8_t *dirty, int32_t *succ, int2 *vloc,
                        int32_t *sinklist, int32_t *sinkcount, int32_t *dlist, int32_t *dcount,
-                       const int32_t *gate, const uint8_t *tie, uint8_t *need)
+                       const int32_t *gate, const uint8_t *tie, uint8_t *need, unsigned long long *stats)
 {
     cudaError_t e = cudaMemsetAsync(dcount, 0, sizeof(int32_t), s);
     if (e != cudaSuccess) return (int)e;
@@ -673,7 +706,7 @@ int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const ui
     count_launch();
     unsigned g = grid_for(n);
     g = g < 1216u ? g : 1216u;
-    k_tour_relink<<<g, kBlock, 0, s>>>(dlist, dcount, strat, solved, rev_off, rev_src, succ, gate);
+    k_tour_relink<<<g, kBlock, 0, s>>>(dlist, dcount, strat, solved, rev_off, rev_src, succ, gate, stats);
     count_launch();
     k_sink_list<<<capped_grid(ceil_div(n, kScanPer)), kBlock, 0, s>>>(n, strat, solved, sinklist, sinkcount, gate);
     count_launch();

@@ -132,16 +132,19 @@ void launch_reset_odd(cudaStream_t s, int32_t n, const int8_t *owner, const int3
 void launch_tour_build(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
                        const int32_t *rev_off, const int32_t *rev_src, int32_t *succ, int2 *vloc,
                        int32_t *sinklist, int32_t *sinkcount, uint8_t *dirty, const int32_t *gate = nullptr,
-                       const uint8_t *tie = nullptr, uint8_t *need = nullptr);
+                       const uint8_t *tie = nullptr, uint8_t *need = nullptr, unsigned long long *stats = nullptr);
 // The same tour brought up to date from the previous one: only the parents
 // flagged in dirty (cleared here; dlist: n entries of scratch, dcount: one
 // counter) are relinked and the sink's list is rebuilt.  Returns a
 // cudaError_t value.  Both set need[v] wherever tie[v] is set (a full
-// evaluation: ChangeTrack), when tie is given.
+// evaluation: ChangeTrack), when tie is given.  With stats (3 words), both
+// add the parents they linked, the in-neighbour entries they scanned and the
+// children they linked.
 int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const uint8_t *solved,
                        const int32_t *rev_off, const int32_t *rev_src, uint8_t *dirty, int32_t *succ, int2 *vloc,
                        int32_t *sinklist, int32_t *sinkcount, int32_t *dlist, int32_t *dcount,
-                       const int32_t *gate = nullptr, const uint8_t *tie = nullptr, uint8_t *need = nullptr);
+                       const int32_t *gate = nullptr, const uint8_t *tie = nullptr, uint8_t *need = nullptr,
+                       unsigned long long *stats = nullptr);
 // Sublist walks; heads are the nodes j*stride (j < nsub-1) and the list start.
 // One thread per sublist, `block` threads per block (a multiple of 32, <= 1024).
 constexpr int kWalkBlock = 128;

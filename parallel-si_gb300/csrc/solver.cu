@@ -419,6 +419,9 @@ int Solver::sync_and_check(const char *what)
     if (rc) return rc;
     times_.patches = (int64_t)hw_->patch[0];
     times_.patched = (int64_t)hw_->patch[1];
+    times_.tour_parents = (int64_t)hw_->relink[0];
+    times_.tour_entries = (int64_t)hw_->relink[1];
+    times_.tour_children = (int64_t)hw_->relink[2];
     if (hw_->err) {
         uint32_t bits = hw_->err;
         cudaMemsetAsync(dw_, 0, sizeof(Words), stream_);
@@ -432,7 +435,8 @@ void Solver::reset_times()
 {
     times_ = SolverTimes();
     cudaMemsetAsync(dw_->patch, 0, sizeof(dw_->patch), stream_);
-    if (hw_) hw_->patch[0] = hw_->patch[1] = 0;
+    cudaMemsetAsync(dw_->relink, 0, sizeof(dw_->relink), stream_);
+    if (hw_) hw_->patch[0] = hw_->patch[1] = hw_->relink[0] = hw_->relink[1] = hw_->relink[2] = 0;
 }
 
 void Solver::reset_tracking()
@@ -541,10 +545,10 @@ int Solver::enqueue_full(bool timed)
     //    jA_ is free until the cycle pass: it holds the list of dirty parents
     begin(PH_TOUR);
     launch_tour_build(stream_, n_, strat_, solved_, rev_off_, rev_src_, succ_, vloc_, ulist_, &dw_->sinkcount, dirty_,
-                      &ctl_->full, tie_, need_);
+                      &ctl_->full, tie_, need_, dw_->relink);
     int ce = launch_tour_update(stream_, n_, strat_, solved_, rev_off_, rev_src_, dirty_, succ_, vloc_, ulist_,
                                 &dw_->sinkcount, reinterpret_cast<int32_t *>(jA_), &dw_->cnt[0], &ctl_->incr, tie_,
-                                need_);
+                                need_, dw_->relink);
     if (ce) return fail(PSI_ERR_CUDA, std::string("tour update: ") + cudaGetErrorString((cudaError_t)ce));
     end(PH_TOUR);
     // 2. Helman-JaJa sublists, then the reduced list ranked on the device

@@ -29,6 +29,8 @@ struct SolverTimes {
     int64_t unreached = 0, jump_rounds = 0;
     // incremental evaluations (patch_kernels.cu) and the vertices they re-evaluated
     int64_t patches = 0, patched = 0;
+    // tour build and upkeep: parents linked, in-neighbour entries scanned, children linked
+    int64_t tour_parents = 0, tour_entries = 0, tour_children = 0;
 };
 
 // Status word -> +1 / -1 / 0 as CPUParity's infinite[] (device_common.cuh:
@@ -227,6 +229,7 @@ private:
     struct Words {
         unsigned long long sw[4];   // switch counters (launch_switch)
         unsigned long long patch[2];   // patches, vertices they re-evaluated (since reset_times)
+        unsigned long long relink[3];  // tour kernels: parents, in-list entries, children linked (since reset_times)
         uint32_t err;
         int32_t ucount;             // vertices the sink did not reach
         int32_t sinkcount;          // children of the sink (tour build)

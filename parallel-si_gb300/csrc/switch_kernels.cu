@@ -414,69 +414,82 @@ __global__ void __launch_bounds__(kBlock) k_switch_warp(int32_t np, const int32_
         ScoreArg run = {sgn * kc0, cur0};
         int32_t moves = 0;
         bool tie = false, exact = false;
-        for (int32_t c = 0; c < total; c += 32) {
-            const int32_t t = c + lane;
-            const bool valid = t < total;
-            // the lane whose segment holds edge t: the last lane with base <= t
-            int32_t seg = 0;
+        // kRounds rounds of 32 edges at a time: every round's successor ids,
+        // then every round's keys, are loaded before any of them is used, so
+        // a warp has up to 32 * kRounds gathers in flight
+        constexpr int kRounds = 4;
+        for (int32_t c0 = 0; c0 < total; c0 += 32 * kRounds) {
+            int32_t us[kRounds], ks[kRounds], segs[kRounds];
 #pragma unroll
-            for (int step = 16; step; step >>= 1) {
-                const int32_t b = __shfl_sync(kAll, base, seg + step);
-                if (b <= t) seg += step;
-            }
-            const int32_t sb = __shfl_sync(kAll, base, seg), se0 = __shfl_sync(kAll, e0, seg);
-            int32_t u = -1, k = 0;
-            if (valid) {
-                u = __ldcs(&tgt[se0 + (t - sb)]);
-                k = key[u];
-            }
-            ScoreArg x = {valid ? sgn * k : INT_MIN, u};
-            // segmented inclusive scan (segments are runs of equal seg)
+            for (int r = 0; r < kRounds; r++) {
+                const int32_t t = c0 + 32 * r + lane;
+                // the lane whose segment holds edge t: the last lane with base <= t
+                int32_t seg = 0;
 #pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const int32_t osc = __shfl_up_sync(kAll, x.sc, o), ou = __shfl_up_sync(kAll, x.u, o);
-                const int32_t oseg = __shfl_up_sync(kAll, seg, o);
-                if (lane >= o && oseg == seg && osc >= x.sc) {
-                    x.sc = osc;
-                    x.u = ou;
+                for (int step = 16; step; step >>= 1) {
+                    const int32_t b = __shfl_sync(kAll, base, seg + step);
+                    if (b <= t) seg += step;
                 }
+                const int32_t sb = __shfl_sync(kAll, base, seg), se0 = __shfl_sync(kAll, e0, seg);
+                segs[r] = seg;
+                us[r] = (t < total) ? __ldcs(&tgt[se0 + (t - sb)]) : -1;
             }
-            // the running choice before this edge: the segment's carry, then
-            // the inclusive value of the previous lane of the same segment
-            const ScoreArg carry = {__shfl_sync(kAll, run.sc, seg), __shfl_sync(kAll, run.u, seg)};
-            const int32_t psc = __shfl_up_sync(kAll, x.sc, 1), pu = __shfl_up_sync(kAll, x.u, 1);
-            const int32_t pseg = __shfl_up_sync(kAll, seg, 1);
-            const bool first = (lane == 0) || (pseg != seg);
-            const ScoreArg excl = first ? carry : first_max(carry, ScoreArg{psc, pu});
-            const int32_t sc = valid ? sgn * k : INT_MIN;
-            const bool rec = valid && sc > excl.sc;
-            const bool eqd = valid && sc == excl.sc && u != excl.u;
-            const bool exd = eqd && !key_infinite(k);
-            const unsigned recm = __ballot_sync(kAll, rec), eqm = __ballot_sync(kAll, eqd);
-            const unsigned exm = __ballot_sync(kAll, exd);
-            const ScoreArg last = first_max(carry, x);   // inclusive, with the carry
-            // each vertex lane collects its segment's lanes of this round
-            const int32_t lo = base - c, hi = base + deg - c;   // [lo, hi) of this round's lanes
-            int32_t lastlane = 0;
-            unsigned segm = 0;
-            if (deg > 0 && hi > 0 && lo < 32) {
-                const int32_t a = lo > 0 ? lo : 0, b = hi < 32 ? hi : 32;
-                segm = (b - a == 32) ? kAll : (((1u << (b - a)) - 1u) << a);
-                lastlane = b - 1;
-            }
-            const int32_t lsc = __shfl_sync(kAll, last.sc, lastlane), lu = __shfl_sync(kAll, last.u, lastlane);
-            if (segm) {
-                const unsigned r = recm & segm;
-                moves += __popc(r);
-                if (r) {
-                    const int top = 31 - __clz(r);
-                    tie = (top < 31) && ((eqm & segm) >> (top + 1)) != 0;
-                } else {
-                    tie = tie || (eqm & segm) != 0;
+#pragma unroll
+            for (int r = 0; r < kRounds; r++) ks[r] = (us[r] >= 0) ? __ldg(&key[us[r]]) : 0;
+#pragma unroll
+            for (int r = 0; r < kRounds; r++) {
+                const int32_t c = c0 + 32 * r;
+                if (c >= total) break;   // warp-uniform
+                const int32_t seg = segs[r], u = us[r], k = ks[r];
+                const bool valid = u >= 0;
+                ScoreArg x = {valid ? sgn * k : INT_MIN, u};
+                // segmented inclusive scan (segments are runs of equal seg)
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int32_t osc = __shfl_up_sync(kAll, x.sc, o), ou = __shfl_up_sync(kAll, x.u, o);
+                    const int32_t oseg = __shfl_up_sync(kAll, seg, o);
+                    if (lane >= o && oseg == seg && osc >= x.sc) {
+                        x.sc = osc;
+                        x.u = ou;
+                    }
                 }
-                exact = exact || (exm & segm) != 0;
-                run.sc = lsc;
-                run.u = lu;
+                // the running choice before this edge: the segment's carry, then
+                // the inclusive value of the previous lane of the same segment
+                const ScoreArg carry = {__shfl_sync(kAll, run.sc, seg), __shfl_sync(kAll, run.u, seg)};
+                const int32_t psc = __shfl_up_sync(kAll, x.sc, 1), pu = __shfl_up_sync(kAll, x.u, 1);
+                const int32_t pseg = __shfl_up_sync(kAll, seg, 1);
+                const bool first = (lane == 0) || (pseg != seg);
+                const ScoreArg excl = first ? carry : first_max(carry, ScoreArg{psc, pu});
+                const int32_t sc = valid ? sgn * k : INT_MIN;
+                const bool rec = valid && sc > excl.sc;
+                const bool eqd = valid && sc == excl.sc && u != excl.u;
+                const bool exd = eqd && !key_infinite(k);
+                const unsigned recm = __ballot_sync(kAll, rec), eqm = __ballot_sync(kAll, eqd);
+                const unsigned exm = __ballot_sync(kAll, exd);
+                const ScoreArg last = first_max(carry, x);   // inclusive, with the carry
+                // each vertex lane collects its segment's lanes of this round
+                const int32_t lo = base - c, hi = base + deg - c;   // [lo, hi) of this round's lanes
+                int32_t lastlane = 0;
+                unsigned segm = 0;
+                if (deg > 0 && hi > 0 && lo < 32) {
+                    const int32_t a = lo > 0 ? lo : 0, b = hi < 32 ? hi : 32;
+                    segm = (b - a == 32) ? kAll : (((1u << (b - a)) - 1u) << a);
+                    lastlane = b - 1;
+                }
+                const int32_t lsc = __shfl_sync(kAll, last.sc, lastlane), lu = __shfl_sync(kAll, last.u, lastlane);
+                if (segm) {
+                    const unsigned rm = recm & segm;
+                    moves += __popc(rm);
+                    if (rm) {
+                        const int top = 31 - __clz(rm);
+                        tie = (top < 31) && ((eqm & segm) >> (top + 1)) != 0;
+                    } else {
+                        tie = tie || (eqm & segm) != 0;
+                    }
+                    exact = exact || (exm & segm) != 0;
+                    run.sc = lsc;
+                    run.u = lu;
+                }
             }
         }
         int32_t cur = run.u;

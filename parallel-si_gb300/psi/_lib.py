@@ -137,7 +137,7 @@ _SIGS = {
 }
 
 COUNTERS = ("evals", "switches", "sw_edges", "sw_loads", "sw_changed", "unreached", "jump_rounds", "patches",
-            "patched")
+            "patched", "tour_parents", "tour_entries", "tour_children")
 
 PHASES = ("eval", "switch", "tour", "sublist", "reduced", "broadcast", "cycles", "patch")
 

@@ -63,6 +63,9 @@ def test_phase_byte_formulas():
     L = 2 * n + 2
     assert bench.phase_bytes("sublist", n, 0, nsub, None, 1, 0, 0, 0, 0) == 4 * L + 8 * n + 8 * nsub
     assert bench.phase_bytes("tour", n, 0, nsub, None, 1, 0, 0, 0, 0) == 14 * n
+    t = {"tour_parents": 100, "tour_entries": 350, "tour_children": 120}
+    # two full evaluations: per-vertex scans plus half of the relink work each
+    assert bench.phase_bytes("tour", n, 0, nsub, t, 2, 0, 0, 0, 0) == 14 * n + (1700 + 2800 + 480) / 2
     assert bench.phase_bytes("broadcast", n, 0, nsub, None, 1, 0, 0, 0, 0) == 69 * n
     rounds = (nsub - 1).bit_length() + 1
     assert bench.phase_bytes("reduced", n, 0, nsub, None, 1, 0, 0, 0, 0) == 24 * nsub * rounds
