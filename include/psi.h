@@ -105,11 +105,13 @@ typedef struct {
                                 (the same results either way) */
 } psi_options;
 
-/* switch_kernel: PSI_SWITCH_WARP (default) -- a warp takes 32 vertices and
- * lays their successor lists end to end, one successor per lane per round,
- * the per-vertex choice by a segmented warp scan; PSI_SWITCH_THREAD -- one
- * thread per vertex walking its own successor list. */
-enum { PSI_SWITCH_WARP = 0, PSI_SWITCH_THREAD = 1 };
+/* switch_kernel: PSI_SWITCH_THREAD (default) -- one thread per vertex,
+ * its successors' keys gathered four at a time; PSI_SWITCH_WARP -- a warp
+ * takes 32 vertices and lays their successor lists end to end, one
+ * successor per lane per round, the per-vertex choice by a segmented warp
+ * scan.  Both give identical results; on GB300 the thread kernel measured
+ * 3-4% faster on the 2^24 random game. */
+enum { PSI_SWITCH_THREAD = 0, PSI_SWITCH_WARP = 1 };
 
 /* incremental: PSI_INCR_AUTO (default) patches after steps that changed at
  * most patch_limit strategies, giving up for a full evaluation when more

@@ -203,7 +203,7 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
                    unsigned long long *gcount, const int32_t *gmask, uint8_t *dirty, uint32_t *err,
                    const int32_t *gate = nullptr, uint8_t *need = nullptr, int32_t *list = nullptr,
                    int32_t *list_count = nullptr, ChangeList changes = ChangeList(), uint8_t *tie = nullptr,
-                   uint8_t *watch = nullptr, const int4 *skip = nullptr, bool warp = true);
+                   uint8_t *watch = nullptr, const int4 *skip = nullptr, bool warp = false);
 // ---- batches: per-game accounting of solve_si (state[g] = brs, iters,
 // odd_done, done; gcount[g] = strict improvements of the last switch step);
 // with gate, only when *gate is set

@@ -39,7 +39,7 @@ int check_options(const psi_options &opt)
     if (opt.patch_limit < 0) return fail(PSI_ERR_INVALID, "patch_limit must be >= 0");
     if (opt.walk_block != 0 && (opt.walk_block < 32 || opt.walk_block > 1024 || opt.walk_block % 32 != 0))
         return fail(PSI_ERR_INVALID, "walk_block must be 0 or a multiple of 32 in [32, 1024]");
-    if (opt.switch_kernel != PSI_SWITCH_WARP && opt.switch_kernel != PSI_SWITCH_THREAD)
+    if (opt.switch_kernel != PSI_SWITCH_THREAD && opt.switch_kernel != PSI_SWITCH_WARP)
         return fail(PSI_ERR_INVALID, "unknown switch_kernel");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);

@@ -220,7 +220,7 @@ private:
     int32_t incremental_ = 1;   // psi_options.incremental
     int32_t patch_limit_ = 0;   // psi_options.patch_limit
     int32_t walk_block_ = kWalkBlock;   // psi_options.walk_block (0 there: kWalkBlock)
-    bool switch_warp_ = true;           // psi_options.switch_kernel == PSI_SWITCH_WARP
+    bool switch_warp_ = false;          // psi_options.switch_kernel == PSI_SWITCH_WARP
     int32_t *clist_ = nullptr, *alist_ = nullptr, *apos_ = nullptr;
     int4 *pj_ = nullptr;
     int32_t ccap_ = 0, acap_ = 0, max_levels_ = 0;

@@ -47,9 +47,9 @@ def test_gpu_lockstep_with_oracle(fam, n, seed, reset):
 
 @pytest.mark.parametrize("fam,n,seed,reset", [("c2", 4000, 61, False), ("smallpri", 3000, 62, True),
                                                ("c1", 10000, 63, False), ("c3", 5000, 64, False)])
-def test_gpu_thread_per_vertex_switch_matches_oracle(fam, n, seed, reset):
-    """The thread-per-vertex switch kernel (psi_options.switch_kernel) gives
-    what the default warp-cooperative one gives: the oracle's steps."""
+def test_gpu_warp_cooperative_switch_matches_oracle(fam, n, seed, reset):
+    """The warp-cooperative switch kernel (psi_options.switch_kernel = 1)
+    gives what the default thread-per-vertex one gives: the oracle's steps."""
     g = make(fam, n, seed)
     gpu = psi.GPUList(g, switch_kernel=1)
     ref = oracle.Oracle(*g.csr())

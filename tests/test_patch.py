@@ -27,7 +27,7 @@ def test_options_layout_and_default():
     from psi._lib import Options
     assert C.sizeof(Options) == 36
     assert psi.default_options().incremental == AUTO
-    assert psi.default_options().switch_kernel == 0   # PSI_SWITCH_WARP
+    assert psi.default_options().switch_kernel == 0   # PSI_SWITCH_THREAD
 
 
 def test_unknown_incremental_mode_is_rejected_before_device_use():
