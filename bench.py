@@ -499,10 +499,13 @@ def run_gb300(args, rank, world, local):
     # launch options: chosen by the autotuner (trial solves of this game,
     # before the warm-up) unless --no-tune, then from the flags
     tuning = None
-    knobs = dict(sublist_len=args.sublist_len, patch_limit=args.patch_limit, walk_block=args.walk_block)
+    kernel = 1 if args.switch_kernel == "warp" else 0
+    knobs = dict(sublist_len=args.sublist_len, patch_limit=args.patch_limit, walk_block=args.walk_block,
+                 switch_kernel=kernel)
     if not args.no_tune:
-        o, tuning = psi.autotune(game, repeats=2, device=local, graph=int(not args.host_loop))
-        knobs = dict(sublist_len=o.sublist_len, patch_limit=o.patch_limit, walk_block=o.walk_block)
+        o, tuning = psi.autotune(game, repeats=2, device=local, graph=int(not args.host_loop), switch_kernel=kernel)
+        knobs = dict(sublist_len=o.sublist_len, patch_limit=o.patch_limit, walk_block=o.walk_block,
+                     switch_kernel=kernel)
     # the product path: psi_solve (the whole solve_si loop as one CUDA graph,
     # device-side loop control)
     solver = psi.GPUList(game, device=local, graph=int(not args.host_loop), **knobs)
@@ -949,6 +952,8 @@ def main():
     ap.add_argument("--patch-limit", type=int, default=0,
                     help="psi_options.patch_limit (0: the library default, max(1024, n/64))")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--switch-kernel", choices=("thread", "warp"), default="thread",
+                    help="psi_options.switch_kernel: thread-per-vertex (default) or warp-cooperative switch step")
     ap.add_argument("--host-loop", action="store_true",
                     help="time the host-driven solve loop instead of the default one-graph solve")
     ap.add_argument("--workload", choices=("single", "longpath", "c1", "batch", "serve"), default="single",
