@@ -422,6 +422,37 @@ def cpu_c1(seed, solves=3):
     return {"one_core": one, "all_cores": allc}
 
 
+def cpu_step_sample(family, n, seed, evals=4):
+    """A bounded CPU sample of a workload whose full CPU solve is too long
+    for the line: the first `evals` evaluations of its solve_si, each followed
+    by Odd's switch step, by the path-valuation restatement of CPUParity on
+    every host core; milliseconds per evaluation and per switch step."""
+    import oracle
+
+    csr = cpu_game(family, n, seed)
+    o = oracle.Sparse(*csr, threads=cpu_threads())
+    o.init_strat()
+    te = ts = 0.0
+    for _ in range(evals):
+        t0 = time.perf_counter()
+        o.compute_valuation()
+        t1 = time.perf_counter()
+        o.mark_solved(1)
+        k = o.switch_strategy(1)
+        t2 = time.perf_counter()
+        te += t1 - t0
+        ts += t2 - t1
+        if k == 0:
+            break
+    threads = o.threads
+    o.close()
+    return {"ms_per_evaluation": 1000 * te / evals, "ms_per_switch_step": 1000 * ts / evals, "cores": threads,
+            "kind": "port",
+            "sample": f"the first {evals} evaluations (each with Odd's switch step) of the solve of the same n={n} "
+                      f"game, by the exact path-valuation restatement of the reference's CPUParity on {threads} "
+                      f"host threads"}
+
+
 # ------------------------------------------------------------------ arms
 def run_reference(args, rank, world):
     """The reference arm: the reference algorithm's CPU implementation on the
@@ -726,8 +757,10 @@ def run_extras(args, dist, rank, world, local):
                  "e2e_speedup_vs_one_core": gpu["e2e"]["value"] / cpu["one_core"]["si_iters_per_s"]}
     del g
     g = make_game(psi, "longpath", LONGPATH_N, args.seed)
-    out["longpath"] = dict(gpu_solve_rate(psi, g, local, steps=5, warmup=2),
-                           config=workload_config(g.n, g.m, args.seed, "longpath"))
+    lp = gpu_solve_rate(psi, g, local, steps=5, warmup=2)
+    lp["config"] = workload_config(g.n, g.m, args.seed, "longpath")
+    lp["cpu_reference_port"] = cpu_step_sample("longpath", LONGPATH_N, args.seed)
+    out["longpath"] = lp
     del g
     b = batch_measure(args, dist, rank, world, local, steps=3, warmup=1)
     out["batch"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "config", "one_by_one",

@@ -220,6 +220,9 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
 {
     if (gate && !*gate) return;
     if (count) np = *count;
+    // a block past the list's end has nothing to count either (uniform per
+    // block: the block reduction below is never left waiting)
+    if ((int64_t)blockIdx.x * blockDim.x >= np) return;
     // Grid-stride over the list with a bounded grid: the work counters are
     // reduced once per block (a few thousand atomics per launch instead of a
     // set per 256 vertices).  A thread sees a few dozen vertices at most, so
@@ -381,6 +384,8 @@ __global__ void __launch_bounds__(kBlock) k_switch_warp(int32_t np, const int32_
 {
     if (gate && !*gate) return;
     if (count) np = *count;
+    // a block past the list's end has nothing to count either (uniform per block)
+    if ((int64_t)blockIdx.x * blockDim.x >= np) return;
     constexpr unsigned kAll = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
