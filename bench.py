@@ -419,7 +419,20 @@ def cpu_c1(seed, solves=3):
         o2.close()
     allc = {"games_per_s": t / dt, "si_iters_per_s": sum(r[0] for r in res) / dt, "cores": t,
             "how": f"{t} C1 games (seeds {seed}..{seed + t - 1}) solved at once, one dense solver per thread"}
-    return {"one_core": one, "all_cores": allc}
+    # the reference's Bellman-Ford solver (cpubf) on the same game: its first
+    # evaluation meets a cycle with an odd top priority, on which the
+    # reference prints a message and exits (cpu_bv.cpp:73-85)
+    b = oracle.BellmanFord(*csr)
+    t0 = time.perf_counter()
+    try:
+        it, br = b.solve()
+        bf = {"status": "solved", "iters": it, "bf_rounds": br}
+    except oracle.OddCycle:
+        bf = {"status": "exits", "why": "a strategy closes a cycle with an odd top priority (cpu_bv.cpp:73-85)"}
+    bf["ms"] = 1000 * (time.perf_counter() - t0)
+    bf["how"] = "the restatement of the reference's CPU_BellmanFord (psi_bf.c), one thread"
+    b.close()
+    return {"one_core": one, "all_cores": allc, "cpubf": bf}
 
 
 def cpu_step_sample(family, n, seed, evals=4):

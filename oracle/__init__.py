@@ -17,6 +17,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "_build", "libpsi_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libpsi_ref.so")
+REFBF_LIB = os.path.join(HERE, "_ref", "libpsi_refbf.so")
 # the reference's 10-vertex fixture game, placed beside REF_LIB by the recipe
 REF_FIXTURE = os.path.join(HERE, "_ref", "test2.gm")
 # Where the reference's sources are, when the caller names them; otherwise
@@ -93,6 +94,27 @@ def _oracle_lib():
         L.sparse_get_vals.argtypes = [vp, C.c_int, C.c_int, vp]
         L.sparse_get_vals.restype = None
         L.sparse_solve.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int64]
+        # Bellman-Ford best-response restatement (psi_bf.c)
+        L.bf_create.restype = vp
+        L.bf_create.argtypes = [C.c_int, vp, vp, vp, vp]
+        for f in ("bf_destroy", "bf_init_strat"):
+            getattr(L, f).argtypes = [vp]
+            getattr(L, f).restype = None
+        L.bf_max_pri.argtypes = [vp]
+        L.bf_compute_valuation.argtypes = [vp]
+        L.bf_mark_solved.argtypes = [vp, C.c_int]
+        L.bf_mark_solved.restype = None
+        L.bf_switch_strategy.argtypes = [vp, C.c_int]
+        L.bf_switch_strategy.restype = C.c_int64
+        L.bf_best_response.argtypes = [vp, C.POINTER(C.c_int)]
+        L.bf_solve.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]
+        L.bf_get_winning.argtypes = [vp, C.c_int, vp]
+        L.bf_get_winning.restype = C.c_int64
+        for f in ("bf_get_strategy", "bf_get_infinite", "bf_get_solved"):
+            getattr(L, f).argtypes = [vp, vp]
+            getattr(L, f).restype = None
+        L.bf_get_vals.argtypes = [vp, C.c_int, C.c_int, vp]
+        L.bf_get_vals.restype = None
         # workload generator (psi_gen.c)
         L.oracle_gen_random_edges.restype = C.c_int64
         L.oracle_gen_random_edges.argtypes = [C.c_int, C.c_int, C.c_int, C.c_uint64, vp]
@@ -106,6 +128,10 @@ def _oracle_lib():
 
 def ref_available() -> bool:
     return os.path.exists(REF_LIB)
+
+
+def refbf_available() -> bool:
+    return os.path.exists(REFBF_LIB)
 
 
 def _ref_lib():
@@ -422,6 +448,193 @@ class RefSolver:
             self.close()
         except Exception:
             pass
+
+
+class OddCycle(RuntimeError):
+    """The Bellman-Ford solver's evaluation closed a cycle whose top priority
+    is odd: the reference prints a message and exits (cpu_bv.cpp:73-85)."""
+
+
+class _BFState:
+    """Observation methods shared by the restatement and the reference driver."""
+
+    def _arr(self, f):
+        out = np.empty(self.n, np.int32)
+        f(self.h, _ptr(out))
+        return out
+
+    def get_valuation(self, v0=0, count=None):
+        count = self.n - v0 if count is None else count
+        out = np.empty((count, self.max_pri + 1), np.int32)
+        self._vals(self.h, v0, count, _ptr(out))
+        return out
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class BellmanFord(_BFState):
+    """The C restatement (psi_bf.c) of the reference's Bellman-Ford
+    best-response solver CPU_BellmanFord<ArrayVal> (cpu_bf.cpp on CPUBV,
+    cpu_bv.cpp) and of its driver solve_bf (main.cpp:58-76)."""
+
+    def __init__(self, owner, priority, offsets, targets):
+        self.L = _oracle_lib()
+        keep = [np.ascontiguousarray(a, dtype=np.int32) for a in (owner, priority, offsets, targets)]
+        self.n = len(keep[0])
+        self.h = self.L.bf_create(self.n, *[_ptr(a) for a in keep])
+        if not self.h:
+            raise MemoryError("bf_create failed (dense n*(max_pri+1) valuation table)")
+        self.max_pri = self.L.bf_max_pri(self.h)
+        self._vals = self.L.bf_get_vals
+
+    @staticmethod
+    def _ok(rc):
+        if rc != 0:
+            raise OddCycle("an evaluation closed a cycle with an odd top priority")
+
+    def init_strat(self):
+        self.L.bf_init_strat(self.h)
+
+    def compute_valuation(self):
+        self._ok(self.L.bf_compute_valuation(self.h))
+
+    def best_response(self):
+        """One best response; returns the Bellman-Ford rounds it took (0 for the
+        first, which is Odd's improvement loop)."""
+        br = C.c_int(0)
+        self._ok(self.L.bf_best_response(self.h, C.byref(br)))
+        return br.value
+
+    def mark_solved(self, p):
+        self.L.bf_mark_solved(self.h, p)
+
+    def switch_strategy(self, p):
+        return self.L.bf_switch_strategy(self.h, p)
+
+    def solve(self, max_iters=0):
+        it, br = C.c_int(), C.c_int()
+        self._ok(self.L.bf_solve(self.h, C.byref(it), C.byref(br), max_iters))
+        return it.value, br.value
+
+    def get_winning(self, p):
+        out = np.empty(self.n, np.int32)
+        return out[:self.L.bf_get_winning(self.h, p, _ptr(out))]
+
+    def get_strategy(self):
+        return self._arr(self.L.bf_get_strategy)
+
+    def get_infinite(self):
+        return self._arr(self.L.bf_get_infinite)
+
+    def get_solved(self):
+        return self._arr(self.L.bf_get_solved)
+
+    def close(self):
+        if self.h:
+            self.L.bf_destroy(self.h)
+            self.h = None
+
+
+_rbflib = None
+
+
+def _refbf_lib():
+    global _rbflib
+    if _rbflib is None:
+        L = C.CDLL(REFBF_LIB)
+        vp = C.c_void_p
+        L.ref_bf_create_from_gm.restype = vp
+        L.ref_bf_create_from_gm.argtypes = [C.c_char_p, C.c_char_p, C.c_int]
+        for f in ("ref_bf_destroy", "ref_bf_init_strat"):
+            getattr(L, f).argtypes = [vp]
+            getattr(L, f).restype = None
+        L.ref_bf_n.argtypes = [vp]
+        L.ref_bf_max_pri.argtypes = [vp]
+        L.ref_bf_best_response.argtypes = [vp, C.POINTER(C.c_int)]
+        L.ref_bf_best_response.restype = None
+        L.ref_bf_mark_solved.argtypes = [vp, C.c_int]
+        L.ref_bf_mark_solved.restype = None
+        L.ref_bf_switch_strategy.argtypes = [vp, C.c_int]
+        L.ref_bf_switch_strategy.restype = C.c_longlong
+        L.ref_bf_get_winning.argtypes = [vp, C.c_int, vp]
+        L.ref_bf_get_winning.restype = C.c_longlong
+        for f in ("ref_bf_get_strategy", "ref_bf_get_infinite", "ref_bf_get_solved"):
+            getattr(L, f).argtypes = [vp, vp]
+            getattr(L, f).restype = None
+        L.ref_bf_get_vals.argtypes = [vp, C.c_int, C.c_int, vp]
+        L.ref_bf_get_vals.restype = None
+        _rbflib = L
+    return _rbflib
+
+
+class RefBellmanFord(_BFState):
+    """The reference's own CPU_BellmanFord<ArrayVal> (compiled from its
+    sources), fed .gm text through the reference parser.  Games with a cycle
+    whose top priority is odd are refused (the reference would exit on them)."""
+
+    def __init__(self, gm_text: str):
+        self.L = _refbf_lib()
+        err = C.create_string_buffer(256)
+        self.h = self.L.ref_bf_create_from_gm(gm_text.encode(), err, 256)
+        if not self.h:
+            raise ValueError("reference Bellman-Ford solver: " + err.value.decode())
+        self.n = self.L.ref_bf_n(self.h)
+        self.max_pri = self.L.ref_bf_max_pri(self.h)
+        self._vals = self.L.ref_bf_get_vals
+
+    def init_strat(self):
+        self.L.ref_bf_init_strat(self.h)
+
+    def best_response(self):
+        br = C.c_int(0)
+        self.L.ref_bf_best_response(self.h, C.byref(br))
+        return br.value
+
+    def mark_solved(self, p):
+        self.L.ref_bf_mark_solved(self.h, p)
+
+    def switch_strategy(self, p):
+        return self.L.ref_bf_switch_strategy(self.h, p)
+
+    def get_winning(self, p):
+        out = np.empty(self.n, np.int32)
+        return out[:self.L.ref_bf_get_winning(self.h, p, _ptr(out))]
+
+    def get_strategy(self):
+        return self._arr(self.L.ref_bf_get_strategy)
+
+    def get_infinite(self):
+        return self._arr(self.L.ref_bf_get_infinite)
+
+    def get_solved(self):
+        return self._arr(self.L.ref_bf_get_solved)
+
+    def close(self):
+        if self.h:
+            self.L.ref_bf_destroy(self.h)
+            self.h = None
+
+
+def solve_bf(si, max_iters=0):
+    """solve_bf (main.cpp:58-76) over an object with the Bellman-Ford solver's
+    methods, yielding the state after every iteration: (iteration, Bellman-Ford
+    rounds so far, strategy, infinite flags) right after the best response and
+    before Even's switch step.  Returns nothing; the caller iterates."""
+    si.init_strat()
+    it = br = 0
+    while True:
+        br += si.best_response()
+        yield it, br, si.get_strategy(), si.get_infinite()
+        si.mark_solved(0)
+        it += 1
+        if si.switch_strategy(0) == 0:
+            return
+        if max_iters and it >= max_iters:
+            return
 
 
 def to_gm(owner, priority, offsets, targets) -> str:

@@ -5,6 +5,8 @@ finishes in seconds.  Families follow the measured configurations:
   c3       long-path game, priority U[0,1024), owner alternating (scaled n)
   c4       random game, out-degree U[2,8], priority U[0,n)      (one batch member)
   ring10   the 10-vertex game v -> v+1, v+2 (mod 10), priority = owner = v mod 2
+  evencyc  no cycle with an odd top priority (the precondition of the reference's
+           Bellman-Ford solver, cpu_bv.cpp:73-85): see evencyc_csr
 """
 import numpy as np
 
@@ -20,6 +22,51 @@ def ring10():
     return psi.Game.from_csr(owner, pri, off, tg)
 
 
+def _splitmix64(state):
+    """One step of splitmix64 over a one-element list holding the state."""
+    state[0] = (state[0] + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+    z = state[0]
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & 0xFFFFFFFFFFFFFFFF
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & 0xFFFFFFFFFFFFFFFF
+    return z ^ (z >> 31)
+
+
+def evencyc_csr(n: int, seed: int):
+    """A random game in which every cycle has an even top priority.  Hubs
+    (vertices [0, h), h = max(2, n/32)) carry the highest priorities, all
+    even; every other vertex has successors among higher ids and hubs only.
+    A cycle needs an edge to a lower id, so it passes through a hub, and its
+    top priority is a hub's.  Owner uniform, out-degree uniform in [2, 5]
+    (fewer where fewer successors are allowed), distinct non-self
+    successors, other priorities uniform in [0, 256).  Drawn from splitmix64
+    in plain Python, so the game is the same on every machine."""
+    st = [seed * 0xD1B54A32D192ED03 & 0xFFFFFFFFFFFFFFFF]
+    below = lambda k: (_splitmix64(st) >> 11) % k   # noqa: E731 (bias < 2^-40: irrelevant here)
+    h = max(2, n // 32)
+    base = 256
+    owner = np.array([below(2) for _ in range(n)], np.int32)
+    pri = np.array([below(base) for _ in range(n)], np.int32)
+    pri[:h] = base + 2 * np.arange(h)
+    off = [0]
+    tg = []
+    for v in range(n):
+        avail = n - 1 if v < h else (n - 1 - v) + h   # distinct choices there are
+        deg = min(2 + below(4), avail)
+        succ = []
+        while len(succ) < deg:
+            if v < h:
+                u = below(n)
+            elif v + 1 < n and below(4) != 0:
+                u = v + 1 + below(n - v - 1)
+            else:
+                u = below(h)
+            if u != v and u not in succ:
+                succ.append(u)
+        tg += succ
+        off.append(len(tg))
+    return owner, pri, np.array(off, np.int32), np.array(tg, np.int32)
+
+
 def make(family: str, n: int, seed: int):
     if family == "c1":
         return psi.Game.random(n, 2, 10, n, seed)
@@ -33,4 +80,6 @@ def make(family: str, n: int, seed: int):
         return psi.Game.random(n, 2, 5, 8, seed)
     if family == "ring10":
         return ring10()
+    if family == "evencyc":
+        return psi.Game.from_csr(*evencyc_csr(n, seed))
     raise ValueError(family)

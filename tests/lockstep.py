@@ -129,3 +129,74 @@ def traced_solve(si, reset=False, rows=True):
         if k == 0:
             break
     return iters, brs, tr.h
+
+
+def br_state(si):
+    """State after one of Odd's best responses: (strategy, infinite, solved,
+    dense rows with the rows of infinite or solved vertices zeroed)."""
+    inf = si.get_infinite()
+    sol = si.get_solved()
+    rows = si.get_valuation().copy()
+    rows[(inf != 0) | (sol != 0)] = 0
+    return si.get_strategy(), inf, sol, rows
+
+
+def si_best_responses(si):
+    """solve_si (main.cpp:20-55, plain variant) over a StrategyImprovement-
+    shaped solver, yielding br_state after each of Odd's best responses (the
+    inner loop has converged), before mark_solved(0) and Even's switch."""
+    si.init_strat()
+    first = True
+    while True:
+        while True:
+            if first:
+                si.compute_first_val()
+            else:
+                si.compute_valuation()
+            si.mark_solved(1)
+            if si.switch_strategy(1) == 0:
+                break
+        first = False
+        yield br_state(si)
+        si.mark_solved(0)
+        if si.switch_strategy(0) == 0:
+            return
+
+
+def bf_best_responses(bf):
+    """solve_bf (main.cpp:58-76) over a Bellman-Ford solver (oracle.BellmanFord
+    or oracle.RefBellmanFord), yielding (Bellman-Ford rounds so far, br_state)
+    after each best response."""
+    bf.init_strat()
+    rounds = 0
+    while True:
+        rounds += bf.best_response()
+        yield rounds, br_state(bf)
+        bf.mark_solved(0)
+        if bf.switch_strategy(0) == 0:
+            return
+
+
+def br_digest(owner, state, even_only=True):
+    """Digest of a best response's state: Even's strategy (every vertex's with
+    even_only False), infinite flags, solved flags and the finite rows."""
+    strat, inf, sol, rows = state
+    d = hashlib.sha256()
+    d.update(np.ascontiguousarray(strat[owner == 0] if even_only else strat).tobytes())
+    for a in (inf, sol, rows):
+        d.update(np.ascontiguousarray(a).tobytes())
+    return d.hexdigest()[:16]
+
+
+def compare_br(a, b, owner, where, odd_too=False):
+    """Two best-response states agree: Even's strategy (with odd_too also
+    Odd's), infinite and solved flags, and the rows of finite vertices."""
+    sa, ia, la, ra = a
+    sb, ib, lb, rb = b
+    ev = owner == 0
+    sel = np.ones_like(ev) if odd_too else ev
+    assert np.array_equal(sa[sel], sb[sel]), f"{where}: strategies differ at {np.nonzero(sel & (sa != sb))[0][:10]}"
+    assert np.array_equal(ia, ib), f"{where}: infinite flags differ at {np.nonzero(ia != ib)[0][:10]}"
+    assert np.array_equal(la, lb), f"{where}: solved flags differ at {np.nonzero(la != lb)[0][:10]}"
+    bad = np.nonzero((ra != rb).any(axis=1))[0]
+    assert bad.size == 0, f"{where}: valuations differ at vertices {bad[:10]}"
