@@ -127,6 +127,24 @@ __device__ __forceinline__ void add_relink_stats(unsigned long long *stats, int3
     }
 }
 
+// In-neighbours of a parent p in batches: the next kInBatch entries of its
+// reverse-CSR slice [eb, e1) and their strategies, all loads issued before any
+// is used (independent gathers in flight per thread); child[j] says whether
+// entry j is a child of p (strat[u] == p), false past the slice.
+constexpr int kInBatch = 4;
+__device__ __forceinline__ void in_batch(const int32_t *__restrict__ rev_src, const int32_t *__restrict__ strat,
+                                         int32_t eb, int32_t e1, int32_t p, int32_t (&us)[kInBatch],
+                                         bool (&child)[kInBatch])
+{
+#pragma unroll
+    for (int j = 0; j < kInBatch; j++) us[j] = (eb + j < e1) ? rev_src[eb + j] : -1;
+    int32_t ss[kInBatch];
+#pragma unroll
+    for (int j = 0; j < kInBatch; j++) ss[j] = (us[j] >= 0) ? strat[us[j]] : -1;
+#pragma unroll
+    for (int j = 0; j < kInBatch; j++) child[j] = us[j] >= 0 && ss[j] == p;
+}
+
 // Thread p: (a) if p is a live child of the sink, append it to the sink list;
 // (b) if p is live, link its children, found among its distinct in-neighbours
 // rev_src[rev_off[p] .. rev_off[p+1]), as
@@ -153,13 +171,19 @@ __global__ void k_tour_link(int32_t n, const int32_t *__restrict__ strat, const 
         const int32_t e0 = rev_off[p], e1 = rev_off[p + 1];
         t_parents++;
         t_entries += e1 - e0;
-        for (int32_t e = e0; e < e1; e++) {
-            int32_t u = rev_src[e];
-            if (strat[u] != p) continue;
-            if (prev < 0) succ[2 * (int64_t)p + 1] = 2 * u + 1;
-            else succ[2 * (int64_t)prev] = 2 * u + 1;
-            prev = u;
-            t_children++;
+        for (int32_t eb = e0; eb < e1; eb += kInBatch) {
+            int32_t us[kInBatch];
+            bool child[kInBatch];
+            in_batch(rev_src, strat, eb, e1, p, us, child);
+#pragma unroll
+            for (int j = 0; j < kInBatch; j++) {
+                if (!child[j]) continue;
+                const int32_t u = us[j];
+                if (prev < 0) succ[2 * (int64_t)p + 1] = 2 * u + 1;
+                else succ[2 * (int64_t)prev] = 2 * u + 1;
+                prev = u;
+                t_children++;
+            }
         }
         if (prev >= 0) succ[2 * (int64_t)prev] = 2 * p;
     }
@@ -217,17 +241,23 @@ __global__ void k_tour_relink(const int32_t *__restrict__ list, const int32_t *_
         const int32_t e0 = rev_off[p], e1 = rev_off[p + 1];
         t_parents++;
         t_entries += e1 - e0;
-        for (int32_t e = e0; e < e1; e++) {
-            int32_t u = rev_src[e];
-            if (strat[u] != p) continue;
-            t_children++;
-            if (!live) {
-                succ[2 * (int64_t)u] = 2 * u + 1;
-                continue;
+        for (int32_t eb = e0; eb < e1; eb += kInBatch) {
+            int32_t us[kInBatch];
+            bool child[kInBatch];
+            in_batch(rev_src, strat, eb, e1, p, us, child);
+#pragma unroll
+            for (int j = 0; j < kInBatch; j++) {
+                if (!child[j]) continue;
+                const int32_t u = us[j];
+                t_children++;
+                if (!live) {
+                    succ[2 * (int64_t)u] = 2 * u + 1;
+                    continue;
+                }
+                if (prev < 0) succ[2 * (int64_t)p + 1] = 2 * u + 1;
+                else succ[2 * (int64_t)prev] = 2 * u + 1;
+                prev = u;
             }
-            if (prev < 0) succ[2 * (int64_t)p + 1] = 2 * u + 1;
-            else succ[2 * (int64_t)prev] = 2 * u + 1;
-            prev = u;
         }
         if (prev >= 0) succ[2 * (int64_t)prev] = 2 * p;
         else succ[2 * (int64_t)p + 1] = 2 * p;

@@ -234,6 +234,7 @@ private:
         int32_t ucount;             // vertices the sink did not reach
         int32_t sinkcount;          // children of the sink (tour build)
         int32_t cnt[3];             // active-list counters of the cycle kernel
+        uint32_t claim;             // the switch kernel's work counter (launch_switch)
     };
     Words *dw_ = nullptr, *hw_ = nullptr;
     // graph-driven solve loop (solver_graph.cu)
