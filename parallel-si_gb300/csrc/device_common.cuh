@@ -275,6 +275,14 @@ __device__ __forceinline__ void block_append_k(const int32_t (&v)[K], int32_t *_
     __syncthreads();
 }
 
+// Sixteen byte flags as one 16-byte word (vector loads of flag arrays).
+union Bytes16 {
+    int4 q;
+    uint8_t b[16];
+};
+
+__device__ __forceinline__ bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
+
 // Warp-aggregated slot reservation: every lane of a converged warp calls it;
 // a lane with flag set gets base + its rank among the flagged lanes, where
 // base = atomicAdd(count, flagged lanes) (one atomic per warp); -1 otherwise.

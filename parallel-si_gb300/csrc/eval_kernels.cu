@@ -54,9 +54,12 @@ inline unsigned grid_for(int64_t items, int block = kBlock)
     return (unsigned)(g < 1 ? 1 : g);
 }
 
-// Scans of all vertices take kScanPer of them per thread and pass (blockDim
-// apart, so every load is coalesced).
-constexpr int kScanPer = 4;
+// The scans of all vertices that compact a list (dirty parents, the sink's
+// children) give each thread kVec consecutive vertices per pass: their byte
+// flags arrive in one 16-byte load, int32 fields in four, so a warp reads 512
+// contiguous bytes of each array per load; the ragged end of the range (and
+// arrays not 16-byte aligned) go one vertex at a time.
+constexpr int kVec = 16;
 
 __device__ __forceinline__ int ceil_log2_dev(int64_t x)
 {
@@ -205,20 +208,41 @@ __global__ void k_dirty_list(int32_t n, uint8_t *__restrict__ dirty, int32_t *__
                              const uint8_t *__restrict__ tie, uint8_t *__restrict__ need)
 {
     if (gate && !*gate) return;
-    const int64_t pass = (int64_t)kScanPer * blockDim.x;
+    const bool vec = aligned16(dirty) && aligned16(vloc) && (!tie || (aligned16(tie) && aligned16(need)));
+    const int64_t pass = (int64_t)kVec * blockDim.x;
     for (int64_t b0 = (int64_t)blockIdx.x * pass; b0 < n; b0 += (int64_t)gridDim.x * pass) {
-        int32_t v[kScanPer];
+        const int64_t v0 = b0 + (int64_t)kVec * threadIdx.x;
+        int32_t v[kVec];
+        if (vec && v0 + kVec <= n) {
+            Bytes16 d;
+            d.q = *reinterpret_cast<const int4 *>(dirty + v0);
+            if (d.q.x | d.q.y | d.q.z | d.q.w) *reinterpret_cast<int4 *>(dirty + v0) = make_int4(0, 0, 0, 0);
 #pragma unroll
-        for (int k = 0; k < kScanPer; k++) {
-            const int64_t i = b0 + (int64_t)k * blockDim.x + threadIdx.x;
-            v[k] = -1;
-            if (i < n) {
-                if (dirty[i]) {
-                    dirty[i] = 0;
-                    v[k] = (int32_t)i;
+            for (int k = 0; k < kVec; k++) v[k] = d.b[k] ? (int32_t)(v0 + k) : -1;
+            int4 *vl = reinterpret_cast<int4 *>(vloc + v0);   // on no walked sublist until the walk reaches it
+#pragma unroll
+            for (int k = 0; k < kVec / 2; k++) vl[k] = make_int4(-1, -1, -1, -1);
+            if (tie) {
+                const int4 t = *reinterpret_cast<const int4 *>(tie + v0);
+                if (t.x | t.y | t.z | t.w) {
+                    int4 *nd = reinterpret_cast<int4 *>(need + v0);
+                    const int4 o = *nd;
+                    *nd = make_int4(o.x | t.x, o.y | t.y, o.z | t.z, o.w | t.w);   // flags are 0 or 1
                 }
-                vloc[i] = make_int2(-1, -1);   // on no walked sublist until the walk reaches it
-                if (tie && tie[i]) need[i] = 1;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kVec; k++) {
+                const int64_t i = v0 + k;
+                v[k] = -1;
+                if (i < n) {
+                    if (dirty[i]) {
+                        dirty[i] = 0;
+                        v[k] = (int32_t)i;
+                    }
+                    vloc[i] = make_int2(-1, -1);
+                    if (tie && tie[i]) need[i] = 1;
+                }
             }
         }
         block_append_k(v, list, count);
@@ -271,13 +295,29 @@ __global__ void k_sink_list(int32_t n, const int32_t *__restrict__ strat, const 
                             const int32_t *__restrict__ gate)
 {
     if (gate && !*gate) return;
-    const int64_t pass = (int64_t)kScanPer * blockDim.x;
+    const bool vec = aligned16(strat) && aligned16(solved);
+    const int64_t pass = (int64_t)kVec * blockDim.x;
     for (int64_t b0 = (int64_t)blockIdx.x * pass; b0 < n; b0 += (int64_t)gridDim.x * pass) {
-        int32_t v[kScanPer];
+        const int64_t v0 = b0 + (int64_t)kVec * threadIdx.x;
+        int32_t v[kVec];
+        if (vec && v0 + kVec <= n) {
+            Bytes16 so;
+            so.q = *reinterpret_cast<const int4 *>(solved + v0);
+            const int4 *sp = reinterpret_cast<const int4 *>(strat + v0);
 #pragma unroll
-        for (int k = 0; k < kScanPer; k++) {
-            const int64_t i = b0 + (int64_t)k * blockDim.x + threadIdx.x;
-            v[k] = (i < n && strat[i] < 0 && !solved[i]) ? (int32_t)i : -1;
+            for (int k = 0; k < kVec / 4; k++) {
+                const int4 q = sp[k];
+                v[4 * k + 0] = (q.x < 0 && !so.b[4 * k + 0]) ? (int32_t)(v0 + 4 * k + 0) : -1;
+                v[4 * k + 1] = (q.y < 0 && !so.b[4 * k + 1]) ? (int32_t)(v0 + 4 * k + 1) : -1;
+                v[4 * k + 2] = (q.z < 0 && !so.b[4 * k + 2]) ? (int32_t)(v0 + 4 * k + 2) : -1;
+                v[4 * k + 3] = (q.w < 0 && !so.b[4 * k + 3]) ? (int32_t)(v0 + 4 * k + 3) : -1;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kVec; k++) {
+                const int64_t i = v0 + k;
+                v[k] = (i < n && strat[i] < 0 && !solved[i]) ? (int32_t)i : -1;
+            }
         }
         block_append_k(v, sinklist, sinkcount);
     }
@@ -731,14 +771,14 @@ int launch_tour_update(cudaStream_t s, int32_t n, const int32_t *strat, const ui
     cudaError_t e = cudaMemsetAsync(dcount, 0, sizeof(int32_t), s);
     if (e != cudaSuccess) return (int)e;
     count_launch();
-    k_dirty_list<<<capped_grid(ceil_div(n, kScanPer)), kBlock, 0, s>>>(n, dirty, dlist, dcount, vloc, gate, tie,
+    k_dirty_list<<<capped_grid(ceil_div(n, kVec)), kBlock, 0, s>>>(n, dirty, dlist, dcount, vloc, gate, tie,
                                                                         need);
     count_launch();
     unsigned g = grid_for(n);
     g = g < 1216u ? g : 1216u;
     k_tour_relink<<<g, kBlock, 0, s>>>(dlist, dcount, strat, solved, rev_off, rev_src, succ, gate, stats);
     count_launch();
-    k_sink_list<<<capped_grid(ceil_div(n, kScanPer)), kBlock, 0, s>>>(n, strat, solved, sinklist, sinkcount, gate);
+    k_sink_list<<<capped_grid(ceil_div(n, kVec)), kBlock, 0, s>>>(n, strat, solved, sinklist, sinkcount, gate);
     count_launch();
     k_sink_chain<<<g, kBlock, 0, s>>>(n, sinklist, sinkcount, succ, gate);
     return 0;

@@ -198,7 +198,9 @@ void launch_mark_solved(cudaStream_t s, const int32_t *ucount, const int32_t *ul
 // walk that a later evaluation may decide differently.  With changes.list,
 // every changed vertex is appended to it (ChangeList).  With claim (a device
 // word) and the need list, the thread kernel deals the list out to warps in
-// chunks through that counter instead of a fixed grid stride.
+// chunks through that counter instead of a fixed grid stride.  With owner
+// (and no gmask), the need list is collected from the n_all vertices' need
+// and owner bytes rather than through plist.
 void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t player,
                    const int32_t *off, const int32_t *tgt, int32_t *strat, const int32_t *st,
                    const int32_t *key, const PathNode *node, unsigned long long *stats, const int32_t *game_of,
@@ -206,7 +208,7 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
                    const int32_t *gate = nullptr, uint8_t *need = nullptr, int32_t *list = nullptr,
                    int32_t *list_count = nullptr, ChangeList changes = ChangeList(), uint8_t *tie = nullptr,
                    uint8_t *watch = nullptr, const int4 *skip = nullptr, bool warp = false,
-                   uint32_t *claim = nullptr);
+                   uint32_t *claim = nullptr, const int8_t *owner = nullptr, int32_t n_all = 0);
 // ---- batches: per-game accounting of solve_si (state[g] = brs, iters,
 // odd_done, done; gcount[g] = strict improvements of the last switch step);
 // with gate, only when *gate is set

@@ -633,7 +633,7 @@ int Solver::switch_strategy(int32_t player, int64_t *switched)
     // jB_ is free until the next cycle pass: it holds the list of vertices to examine
     launch_switch(stream_, np, pl, player, off_, tgt_, strat_, st_, key_, node_, dw_->sw, game_of_, gcount_, gmask_,
                   dirty_, &dw_->err, nullptr, need_, reinterpret_cast<int32_t *>(jB_), &dw_->cnt[2], changes(), tie_,
-                  watch_, skip_, switch_warp_, &dw_->claim);
+                  watch_, skip_, switch_warp_, &dw_->claim, arena_ ? nullptr : owner_, n_);
     phase_end(PH_SWITCH);
     rc = sync_and_check("switch_strategy");
     if (rc) return rc;

@@ -152,7 +152,7 @@ int Solver::enqueue_step(cudaGraph_t body, cudaGraphConditionalHandle loop, bool
     unsigned long long *gc = batch ? gcount_ : nullptr;
     launch_switch(stream_, np_ - np0_, plist_ + np0_, 1, off_, tgt_, strat_, st_, key_, node_, dw_->sw,
                   batch ? game_of_ : nullptr, gc, nullptr, dirty_, &dw_->err, nullptr, need_, todo, &dw_->cnt[2],
-                  changes(), tie_, watch_, skip_, switch_warp_, &dw_->claim);
+                  changes(), tie_, watch_, skip_, switch_warp_, &dw_->claim, arena_ ? nullptr : owner_, n_);
     if (batch) launch_batch_account(stream_, games_, 1, gstate_, gcount_);
     count_launch();
     k_ctl_odd<<<1, 1, 0, stream_>>>(ctl_, dw_->sw);
@@ -164,7 +164,8 @@ int Solver::enqueue_step(cudaGraph_t body, cudaGraphConditionalHandle loop, bool
     if (e != cudaSuccess) return abort_capture(fail(PSI_ERR_CUDA, std::string("memset: ") + cudaGetErrorString(e)));
     launch_switch(stream_, np0_, plist_, 0, off_, tgt_, strat_, st_, key_, node_, dw_->sw,
                   batch ? game_of_ : nullptr, gc, nullptr, dirty_, &dw_->err, &ctl_->even, need_, todo,
-                  &dw_->cnt[2], changes(), tie_, watch_, skip_, switch_warp_, &dw_->claim);
+                  &dw_->cnt[2], changes(), tie_, watch_, skip_, switch_warp_, &dw_->claim,
+                  arena_ ? nullptr : owner_, n_);
     if (batch) launch_batch_account(stream_, games_, 3, gstate_, gcount_, &ctl_->even);
     count_launch();
     k_ctl_even<<<1, 1, 0, stream_>>>(ctl_, dw_->sw, &dw_->err, loop, reset ? 1 : 0, eval_guard(n_));

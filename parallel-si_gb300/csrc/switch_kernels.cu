@@ -189,6 +189,41 @@ __global__ void k_need_list(int32_t np, const int32_t *__restrict__ plist, const
     }
 }
 
+// The same list from the vertex arrays themselves, for a single game or a
+// batch (every vertex of `player` is on plist): kVec consecutive vertices per
+// thread and pass, their need and owner bytes in one 16-byte load each, so the
+// scan streams 2n bytes instead of plist and a gather of need through it.
+// The list is in vertex order within a block pass, which is all the switch
+// kernel needs (each vertex is examined on its own).
+constexpr int kVec = 16;
+__global__ void k_need_ids(int32_t n, int32_t player, const int8_t *__restrict__ owner,
+                           const uint8_t *__restrict__ need, const int32_t *__restrict__ gate,
+                           int32_t *__restrict__ list, int32_t *__restrict__ count, uint32_t *__restrict__ claim)
+{
+    if (gate && !*gate) return;
+    if (claim && blockIdx.x == 0 && threadIdx.x == 0) *claim = 0;   // the switch kernel's work counter
+    const bool vec = aligned16(owner) && aligned16(need);
+    const int64_t pass = (int64_t)kVec * blockDim.x;
+    for (int64_t b0 = (int64_t)blockIdx.x * pass; b0 < n; b0 += (int64_t)gridDim.x * pass) {
+        const int64_t v0 = b0 + (int64_t)kVec * threadIdx.x;
+        int32_t v[kVec];
+        if (vec && v0 + kVec <= n) {
+            Bytes16 nd, ow;
+            nd.q = *reinterpret_cast<const int4 *>(need + v0);
+            ow.q = *reinterpret_cast<const int4 *>(owner + v0);
+#pragma unroll
+            for (int k = 0; k < kVec; k++) v[k] = (nd.b[k] && ow.b[k] == player) ? (int32_t)(v0 + k) : -1;
+        } else {
+#pragma unroll
+            for (int k = 0; k < kVec; k++) {
+                const int64_t i = v0 + k;
+                v[k] = (i < n && need[i] && owner[i] == player) ? (int32_t)i : -1;
+            }
+        }
+        block_append_k(v, list, count);
+    }
+}
+
 // One thread per vertex of the list (all owned by `player`; the list is plist
 // itself, np entries, or -- with count != nullptr -- the *count vertices
 // k_need_list selected).  Per compared edge the common case is one 4-byte
@@ -678,7 +713,7 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
                    unsigned long long *stats, const int32_t *game_of, unsigned long long *gcount,
                    const int32_t *gmask, uint8_t *dirty, uint32_t *err, const int32_t *gate, uint8_t *need,
                    int32_t *list, int32_t *list_count, ChangeList changes, uint8_t *tie, uint8_t *watch,
-                   const int4 *skip, bool warp, uint32_t *claim)
+                   const int4 *skip, bool warp, uint32_t *claim, const int8_t *owner, int32_t n_all)
 {
     if (np <= 0) return;
     const int blocks = per_device(g_switch_blocks, switch_grid);   // four waves of resident blocks
@@ -688,11 +723,18 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
     if (need && list && list_count) {
         // only the vertices whose need flag is set (ChangeTrack)
         cudaMemsetAsync(list_count, 0, sizeof(int32_t), s);
-        unsigned gn = grid_for(ceil_div(np, kNeedPer));
-        gn = gn < (unsigned)blocks ? gn : (unsigned)blocks;
         count_launch();
-        k_need_list<<<gn, kBlock, 0, s>>>(np, plist, need, game_of, gmask, gate, list, list_count,
-                                          warp ? nullptr : claim);
+        if (owner && !gmask) {
+            unsigned gn = grid_for(ceil_div(n_all, kVec));
+            gn = gn < (unsigned)blocks ? gn : (unsigned)blocks;
+            k_need_ids<<<gn, kBlock, 0, s>>>(n_all, player, owner, need, gate, list, list_count,
+                                             warp ? nullptr : claim);
+        } else {
+            unsigned gn = grid_for(ceil_div(np, kNeedPer));
+            gn = gn < (unsigned)blocks ? gn : (unsigned)blocks;
+            k_need_list<<<gn, kBlock, 0, s>>>(np, plist, need, game_of, gmask, gate, list, list_count,
+                                              warp ? nullptr : claim);
+        }
         items = list;
         count = list_count;
     }
