@@ -428,6 +428,22 @@ __global__ void __launch_bounds__(kBlock) k_rank_reduced(int32_t nsub, const int
 
 // Depth of a reached vertex = inclusive prefix of the tour at its up node =
 // -(suffix sum of its sublist) + local prefix (the whole tour sums to 0).
+// Four consecutive vertices per thread and pass: their fields arrive in
+// 16-byte loads and their four sublist gathers are in flight together.
+constexpr int kBcast = 4;
+__device__ __forceinline__ int32_t broadcast_one(int32_t v, bool sol, int2 loc, int2 r, int32_t sv, int32_t pv,
+                                                 int32_t &stv, PathNode *__restrict__ node)
+{
+    if (sol) return -1;   // frozen: status kept, not listed
+    if (loc.x >= 0 && r.x == TOUR_END) {
+        stv = loc.y - r.y;
+        node[v] = PathNode{sv, pv, RM_UNKNOWN, 0};
+        return -1;
+    }
+    stv = ST_UNRESOLVED;
+    return v;
+}
+
 __global__ void k_broadcast_depth(int32_t n, const int2 *__restrict__ vloc, const int2 *__restrict__ fin,
                                   const int32_t *__restrict__ strat, const int32_t *__restrict__ pri,
                                   const uint8_t *__restrict__ solved, int32_t *__restrict__ st,
@@ -435,22 +451,55 @@ __global__ void k_broadcast_depth(int32_t n, const int2 *__restrict__ vloc, cons
                                   int32_t *__restrict__ ucount, const int32_t *__restrict__ gate)
 {
     if (gate && !*gate) return;
-    // grid-stride with block-uniform passes (block_append needs every thread)
-    for (int64_t b0 = (int64_t)blockIdx.x * blockDim.x; b0 < n; b0 += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t v = (int32_t)(b0 + threadIdx.x);
-        bool unreached = false;
-        if (v < n && !solved[v]) {
-            int2 loc = vloc[v];
-            int2 r = (loc.x >= 0) ? fin[loc.x] : make_int2(0, 0);
-            if (loc.x >= 0 && r.x == TOUR_END) {
-                st[v] = loc.y - r.y;
-                node[v] = PathNode{strat[v], pri[v], RM_UNKNOWN, 0};
+    const bool vec = aligned16(vloc) && aligned16(strat) && aligned16(pri) && aligned16(st) &&
+                     ((uintptr_t)solved & 3) == 0;
+    // grid-stride with block-uniform passes (block_append_k needs every thread)
+    const int64_t pass = (int64_t)kBcast * blockDim.x;
+    for (int64_t b0 = (int64_t)blockIdx.x * pass; b0 < n; b0 += (int64_t)gridDim.x * pass) {
+        const int64_t v0 = b0 + (int64_t)kBcast * threadIdx.x;
+        int32_t u[kBcast];
+        if (vec && v0 + kBcast <= n) {
+            const uchar4 so = *reinterpret_cast<const uchar4 *>(solved + v0);
+            const bool sol[kBcast] = {so.x != 0, so.y != 0, so.z != 0, so.w != 0};
+            const int4 l01 = *reinterpret_cast<const int4 *>(vloc + v0);
+            const int4 l23 = *reinterpret_cast<const int4 *>(vloc + v0 + 2);
+            const int2 loc[kBcast] = {make_int2(l01.x, l01.y), make_int2(l01.z, l01.w), make_int2(l23.x, l23.y),
+                                      make_int2(l23.z, l23.w)};
+            int2 r[kBcast];
+#pragma unroll
+            for (int k = 0; k < kBcast; k++) r[k] = (!sol[k] && loc[k].x >= 0) ? fin[loc[k].x] : make_int2(0, 0);
+            const int4 sv = *reinterpret_cast<const int4 *>(strat + v0);
+            const int4 pv = *reinterpret_cast<const int4 *>(pri + v0);
+            int4 stv = make_int4(0, 0, 0, 0);
+            const int32_t v = (int32_t)v0;
+            u[0] = broadcast_one(v, sol[0], loc[0], r[0], sv.x, pv.x, stv.x, node);
+            u[1] = broadcast_one(v + 1, sol[1], loc[1], r[1], sv.y, pv.y, stv.y, node);
+            u[2] = broadcast_one(v + 2, sol[2], loc[2], r[2], sv.z, pv.z, stv.z, node);
+            u[3] = broadcast_one(v + 3, sol[3], loc[3], r[3], sv.w, pv.w, stv.w, node);
+            if (!(sol[0] | sol[1] | sol[2] | sol[3])) {
+                *reinterpret_cast<int4 *>(st + v0) = stv;
             } else {
-                st[v] = ST_UNRESOLVED;
-                unreached = true;
+                if (!sol[0]) st[v0] = stv.x;
+                if (!sol[1]) st[v0 + 1] = stv.y;
+                if (!sol[2]) st[v0 + 2] = stv.z;
+                if (!sol[3]) st[v0 + 3] = stv.w;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < kBcast; k++) {
+                const int64_t i = v0 + k;
+                u[k] = -1;
+                if (i < n) {
+                    const bool sol = solved[i] != 0;
+                    const int2 loc = sol ? make_int2(-1, 0) : vloc[i];
+                    const int2 r = (!sol && loc.x >= 0) ? fin[loc.x] : make_int2(0, 0);
+                    int32_t stv = 0;
+                    u[k] = broadcast_one((int32_t)i, sol, loc, r, sol ? 0 : strat[i], sol ? 0 : pri[i], stv, node);
+                    if (!sol) st[i] = stv;
+                }
             }
         }
-        block_append(unreached, v, ulist, ucount);
+        block_append_k(u, ulist, ucount);
     }
 }
 
@@ -816,8 +865,8 @@ void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const i
                             int32_t *st, PathNode *node, int32_t *ulist, int32_t *ucount, const int32_t *gate)
 {
     count_launch();
-    k_broadcast_depth<<<capped_grid(n), kBlock, 0, s>>>(n, vloc, fin, strat, pri, solved, st, node, ulist, ucount,
-                                                        gate);
+    k_broadcast_depth<<<capped_grid(ceil_div(n, kBcast)), kBlock, 0, s>>>(n, vloc, fin, strat, pri, solved, st, node,
+                                                                           ulist, ucount, gate);
 }
 
 void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *node, int32_t *key, uint32_t *err,
