@@ -585,9 +585,10 @@ __global__ void __launch_bounds__(kBlock, 8) k_rootinfo(int32_t n, const int32_t
 // window is longer than any path into a cycle plus the cycle, so each walk sits
 // on its final cycle (or on a solved vertex) and the window maximum from a
 // cycle vertex is the cycle's top priority.  A vertex whose window has reached
-// a solved vertex is settled: it leaves the active list (later rounds only
-// touch active vertices, and stop early when none is left) and its final entry
-// is stored in both buffers, so any later reader sees it.  A reader racing with
+// a solved vertex s is settled: its entry becomes (-2 - s, -), so no round
+// reads a solved flag; it leaves the active list (later rounds only touch
+// active vertices, and stop early when none is left) and its final entry is
+// stored in both buffers, so any later reader sees it.  A reader racing with
 // that store sees either the previous entry or the final one; both lead to the
 // same solved vertex.
 constexpr int kSmallCycles = 4096;   // up to this many: one block, no grid barrier
@@ -612,7 +613,7 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
             atomicOr(err, DERR_BAD_INPUT);
             t = u;
         }
-        int2 e = make_int2(t, pri[u]);
+        int2 e = make_int2(solved[t] ? -2 - t : t, pri[u]);
         ja[u] = e;
         jb[u] = e;
     }
@@ -639,13 +640,13 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
             if (i0 < na) {
                 u = act[i0];
                 int2 a = __ldcg(&in[u]);
-                if (solved[a.x]) {
+                if (a.x < 0) {
                     out[u] = a;                  // settled earlier: entry already final
                 } else {
                     int2 b = __ldcg(&in[a.x]);
                     int2 a2 = make_int2(b.x, max(a.y, b.y));
                     out[u] = a2;
-                    if (solved[a2.x]) in[u] = a2;   // settled now: final in both buffers
+                    if (a2.x < 0) in[u] = a2;    // settled now: final in both buffers
                     else keep = true;
                 }
             }
@@ -667,7 +668,7 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
         if (i < nu) {
             u = ulist[i];
             int32_t t = __ldcg(&in[u]).x;
-            int32_t su = solved[t] ? st[t] : ((__ldcg(&in[t]).y % 2 == 0) ? ST_POS_INF : ST_NEG_INF);
+            int32_t su = (t < 0) ? st[-2 - t] : ((__ldcg(&in[t]).y % 2 == 0) ? ST_POS_INF : ST_NEG_INF);
             st[u] = su;
             const int32_t k = (su == ST_POS_INF) ? KEY_POS_INF : KEY_NEG_INF;
             if (key && key[u] != k) {
