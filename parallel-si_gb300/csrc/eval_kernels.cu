@@ -426,6 +426,96 @@ __global__ void __launch_bounds__(kBlock) k_rank_reduced(int32_t nsub, const int
     }
 }
 
+// ---- the same ranking through a ruling set, for long reduced lists.  Items
+// j with j % kRuler == 0 and the list start (item nsub-1) are rulers.  Each
+// ruler walks its items up to the next ruler (or the end), recording for every
+// item its ruler and the sum of the weights from the ruler up to it (seg, in
+// buffer a); the rulers' reduced list (next ruler, segment total) is ranked
+// by Wyllie pointer jumping in buffer b, a list about kRuler times shorter,
+// so its rounds are short; then every item's suffix sum is its ruler's minus
+// its own prefix, and whether it reaches the end is its ruler's (fin, in
+// buffer a over seg).  An item that no ruler's walk covers lies on a cycle of
+// sublists without a ruler (a component the sink does not reach): it never
+// reaches the end.  The walks read the reduced list, a few MB that stay in
+// L2; with kRuler = 8 a walk takes 8 steps on average.
+constexpr int kRuler = 8;
+constexpr int32_t kNotEnd = -2;   // fin.x of an item that does not reach the end
+
+__device__ __forceinline__ bool is_ruler(int32_t j, int32_t nsub) { return j % kRuler == 0 || j == nsub - 1; }
+__device__ __forceinline__ int32_t ruler_index(int32_t j, int32_t nsub, int32_t nr)
+{
+    return j == nsub - 1 ? nr - 1 : j / kRuler;
+}
+
+__global__ void __launch_bounds__(kBlock) k_rank_ruled(int32_t nsub, const int2 *__restrict__ red,
+                                                       int2 *__restrict__ a, int2 *__restrict__ b,
+                                                       uint32_t *__restrict__ err, const int32_t *__restrict__ gate)
+{
+    if (gate && !*gate) return;   // every block returns: no grid barrier is left waiting
+    cg::grid_group g = cg::this_grid();
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+    const int32_t nr = (nsub - 1) / kRuler + 2;   // ruler slots; the last one is the list start's
+    int2 *ra = b, *rb = b + nr;
+    // 1. no item covered yet; ruler slots that hold no ruler never reach the end
+    for (int64_t j = tid; j < nsub; j += nth) a[j] = make_int2(-1, 0);
+    for (int64_t k = tid; k < nr; k += nth) ra[k] = make_int2(kNotEnd, 0);
+    g.sync();
+    // 2. each ruler walks its segment
+    for (int64_t k = tid; k < nr; k += nth) {
+        const int32_t j = (k == nr - 1) ? nsub - 1 : (int32_t)(k * kRuler);
+        if (j >= nsub || (k != nr - 1 && j == nsub - 1)) continue;   // no such ruler (or the list start's own slot)
+        int32_t x = j, acc = 0, next = kNotEnd;
+        for (int32_t steps = 0;; steps++) {
+            if (steps > nsub) {
+                atomicOr(err, DERR_SUBLIST_CAP);
+                break;
+            }
+            a[x] = make_int2((int32_t)k, acc);
+            const int2 r = __ldcg(&red[x]);
+            acc += r.y;
+            if (r.x == TOUR_END) {
+                next = TOUR_END;
+                break;
+            }
+            if (is_ruler(r.x, nsub)) {
+                next = ruler_index(r.x, nsub, nr);
+                break;
+            }
+            x = r.x;
+        }
+        ra[k] = make_int2(next, acc);
+    }
+    // 3. Wyllie over the rulers: ceil(log2 nr) + 1 rounds, ra -> rb -> ra ...
+    const int rounds = ceil_log2_dev(nr) + 1;
+    int2 *in = ra, *out = rb;
+    for (int r = 0; r < rounds; r++) {
+        g.sync();
+        for (int64_t k = tid; k < nr; k += nth) {
+            int2 x = __ldcg(&in[k]);
+            if (x.x >= 0) {
+                const int2 y = __ldcg(&in[x.x]);
+                x = make_int2(y.x, x.y + y.y);
+            }
+            out[k] = x;
+        }
+        int2 *t = in;
+        in = out;
+        out = t;
+    }
+    g.sync();
+    // 4. every item from its ruler
+    for (int64_t j = tid; j < nsub; j += nth) {
+        const int2 sj = __ldcg(&a[j]);
+        int2 f = make_int2(kNotEnd, 0);
+        if (sj.x >= 0) {
+            const int2 rk = __ldcg(&in[sj.x]);
+            f = make_int2(rk.x == TOUR_END ? TOUR_END : kNotEnd, rk.y - sj.y);
+        }
+        a[j] = f;
+    }
+}
+
 // Depth of a reached vertex = inclusive prefix of the tour at its up node =
 // -(suffix sum of its sublist) + local prefix (the whole tour sums to 0).
 // Four consecutive vertices per thread and pass: their fields arrive in
@@ -772,7 +862,9 @@ int device_blocks(const void *kernel, int block)
     return device_sms() * (per_sm > 0 ? per_sm : 1);
 }
 
-std::atomic<int> g_rank_blocks[kMaxCachedDevices], g_cycle_blocks[kMaxCachedDevices];
+std::atomic<int> g_rank_blocks[kMaxCachedDevices], g_cycle_blocks[kMaxCachedDevices], g_ruled_blocks[kMaxCachedDevices];
+// reduced lists at least this long are ranked through a ruling set
+constexpr int32_t kRulerMin = 4096;
 
 }  // namespace
 
@@ -846,8 +938,20 @@ void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, in
 }
 
 int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, int2 *b, const int2 **fin,
-                        const int32_t *gate)
+                        const int32_t *gate, uint32_t *err)
 {
+    if (err && nsub >= kRulerMin) {
+        // the ruling set: the rulers' two jump buffers (2 nr entries) fit in b
+        const int blocks =
+            per_device(g_ruled_blocks, [] { return device_blocks((const void *)k_rank_ruled, kBlock); });
+        int64_t need = ceil_div(nsub, kBlock);
+        int grid = (int)(need < blocks ? need : blocks);
+        *fin = a;
+        void *args[] = {(void *)&nsub, (void *)&red, (void *)&a, (void *)&b, (void *)&err, (void *)&gate};
+        count_launch();
+        cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_rank_ruled, dim3(grid), dim3(kBlock), args, 0, s);
+        return e == cudaSuccess ? 0 : (int)e;
+    }
     const int blocks = per_device(g_rank_blocks, [] { return device_blocks((const void *)k_rank_reduced, kBlock); });
     int64_t need = ceil_div(nsub, kBlock);
     int grid = (int)(need < blocks ? need : blocks);

@@ -151,12 +151,15 @@ constexpr int kWalkBlock = 128;
 void launch_walk_sublists(cudaStream_t s, int32_t nsub, int32_t n, int64_t L, int32_t stride, const int32_t *succ,
                           int2 *vloc, int2 *red, uint32_t *err, const int32_t *gate = nullptr,
                           int block = kWalkBlock);
-// Ranks the reduced list red[0..nsub) (next, weight) by Wyllie pointer jumping
-// (cooperative launch; a, b: nsub entries each).  *fin is set to the buffer
-// that will hold, per item, (TOUR_END if the list start reaches it, else >= 0;
-// inclusive suffix sum).  Returns a cudaError_t value.
+// Ranks the reduced list red[0..nsub) (next, weight) in one cooperative
+// launch (a, b: nsub entries each): by Wyllie pointer jumping over all items,
+// or, with err and at least 4,096 items, through a ruling set (every 8th
+// item and the list start walk to the next ruler, Wyllie over the rulers;
+// err receives DERR_SUBLIST_CAP if a walk overruns).  *fin is set to the
+// buffer that will hold, per item, (TOUR_END if the list start reaches it,
+// else another value; inclusive suffix sum).  Returns a cudaError_t value.
 int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, int2 *b, const int2 **fin,
-                        const int32_t *gate = nullptr);
+                        const int32_t *gate = nullptr, uint32_t *err = nullptr);
 void launch_broadcast_depth(cudaStream_t s, int32_t n, const int2 *vloc, const int2 *fin,
                             const int32_t *strat, const int32_t *pri, const uint8_t *solved,
                             int32_t *st, PathNode *node, int32_t *ulist, int32_t *ucount,

@@ -191,7 +191,7 @@ extern "C" int psi_evaluate_strategy_noalloc(int32_t n, const int32_t *strategy,
     k_na_sink_chain<<<g < 1216u ? g : 1216u, kBlock, 0, s>>>(n, list, &w->sinkcount, succ);
     launch_walk_sublists(s, nsub, n, L, kStride, succ, vloc, redA, &w->err);
     const int2 *fin = nullptr;
-    int re = launch_rank_reduced(s, nsub, redA, redB, redC, &fin);
+    int re = launch_rank_reduced(s, nsub, redA, redB, redC, &fin, nullptr, &w->err);
     if (re) return fail(PSI_ERR_CUDA, std::string("reduced-list kernel launch: ") + cudaGetErrorString((cudaError_t)re));
     launch_broadcast_depth(s, n, vloc, fin, strategy, priority, solved, status, node, list, &w->ucount);
     int32_t *la = reinterpret_cast<int32_t *>(vloc), *lb = la + n;

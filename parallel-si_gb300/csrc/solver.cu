@@ -558,7 +558,7 @@ int Solver::enqueue_full(bool timed)
     end(PH_SUBLIST);
     begin(PH_REDUCED);
     const int2 *fin = nullptr;
-    ce = launch_rank_reduced(stream_, nsub_, redA_, redB_, redC_, &fin, &ctl_->eval);
+    ce = launch_rank_reduced(stream_, nsub_, redA_, redB_, redC_, &fin, &ctl_->eval, &dw_->err);
     if (ce) return fail(PSI_ERR_CUDA, std::string("reduced-list kernel: ") + cudaGetErrorString((cudaError_t)ce));
     end(PH_REDUCED);
     // 3. broadcast depths; collect the vertices the sink does not reach
