@@ -294,11 +294,19 @@ def phase_bytes(phase, n, m, nsub, counters, calls, n_even, n_odd, iters, brs):
         # root-path summaries: status and PathNode in, summary and key out (32 B)
         return 69 * n
     if phase == "reduced":
+        if nsub >= RULER_MIN:
+            # ruling set: item entries in, (ruler, prefix) out and back in, the
+            # ruler's result gathered, fin out (48 B per item); Wyllie over the
+            # nr rulers (24 B per ruler and round) and their initial entries
+            nr = (nsub - 1) // 8 + 2
+            return 48 * nsub + 24 * nr * ((nr - 1).bit_length() + 2)
         rounds = (nsub - 1).bit_length() + 1
         return 24 * nsub * rounds
     return None
 
 
+# reduced lists at least this long are ranked through a ruling set (k_rank_ruled)
+RULER_MIN = 4096
 KERNEL_OF_PHASE = {"switch": "k_switch", "sublist": "k_walk_sublists", "tour": "k_tour_relink",
                    "broadcast": "k_broadcast_depth", "reduced": "k_rank_reduced", "cycles": "k_cycles"}
 # the kernels of a timed phase (for their DRAM traffic per launch)
