@@ -67,8 +67,14 @@ def test_phase_byte_formulas():
     # two full evaluations: per-vertex scans plus half of the relink work each
     assert bench.phase_bytes("tour", n, 0, nsub, t, 2, 0, 0, 0, 0) == 14 * n + (1700 + 2800 + 480) / 2
     assert bench.phase_bytes("broadcast", n, 0, nsub, None, 1, 0, 0, 0, 0) == 69 * n
-    rounds = (nsub - 1).bit_length() + 1
-    assert bench.phase_bytes("reduced", n, 0, nsub, None, 1, 0, 0, 0, 0) == 24 * nsub * rounds
+    # the ruling set at this size: 48 B per item, Wyllie over the rulers
+    nr = (nsub - 1) // 8 + 2
+    assert bench.phase_bytes("reduced", n, 0, nsub, None, 1, 0, 0, 0, 0) == 48 * nsub + 24 * nr * (
+        (nr - 1).bit_length() + 2)
+    # short reduced lists: Wyllie over all items
+    small = 1000
+    assert bench.phase_bytes("reduced", n, 0, small, None, 1, 0, 0, 0, 0) == 24 * small * (
+        (small - 1).bit_length() + 1)
     c = {"switches": 2, "sw_edges": 1000, "sw_loads": 10, "sw_changed": 7}
     # one Odd step of 300 vertices and one Even step of 200: (16*500 + 8*1000 + 8*10 + 6*7) / 2
     assert bench.phase_bytes("switch", n, 0, nsub, c, 2, 200, 300, 1, 1) == (16 * 500 + 8000 + 80 + 42) / 2
