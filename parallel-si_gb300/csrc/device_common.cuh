@@ -181,8 +181,12 @@ __device__ __forceinline__ void top2_add_n(Top2 &t, int32_t p, int32_t count)
 // segment from v up to the landmark, exclusive, and their counts packed as
 // c1 | c2 << 16; a segment holds at most SKIP_K vertices).  Written by the
 // root-summary pass of a full evaluation; a patch marks its vertices'
-// records unknown (the paths of all other vertices are unchanged).
-constexpr int32_t SKIP_K = 32;
+// records unknown (the paths of all other vertices are unchanged).  SKIP_K
+// measured on GB300 (graph solve of the 2^24 random game, long-path 2^23):
+// 64: 63.8, 57.8 ms; 32: 62.8, 57.8; 16: 62.0, 57.0; 8: 61.6, 55.5; 4: 61.8,
+// 55.5 ms: shorter segments shorten the steps after the last jump more than
+// they add jumps.
+constexpr int32_t SKIP_K = 8;
 constexpr int32_t SKIP_UNKNOWN = INT32_MIN;
 __host__ __device__ __forceinline__ int32_t skip_landmark_depth(int32_t d) { return ((d - 1) / SKIP_K) * SKIP_K; }
 __device__ __forceinline__ int4 skip_pack(int32_t anc, const Top2 &t)
