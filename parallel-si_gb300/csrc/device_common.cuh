@@ -213,6 +213,10 @@ __device__ __forceinline__ int32_t acquire_rmax(const PathNode *p)
     return x;
 }
 
+// Warps in the largest block (1,024 threads): the block-aggregated appends
+// keep one count per warp, for any block size the kernels use.
+constexpr int kMaxBlockWarps = 32;
+
 // Block-aggregated append: every thread of the block calls it (no early
 // return before); one atomic on the shared counter per block instead of one
 // per warp, which serialises when most warps append (the sink's children,
@@ -220,7 +224,7 @@ __device__ __forceinline__ int32_t acquire_rmax(const PathNode *p)
 __device__ __forceinline__ void block_append(bool flag, int32_t value, int32_t *__restrict__ list,
                                              int32_t *__restrict__ count)
 {
-    __shared__ int32_t warp_base[kBlock / 32];
+    __shared__ int32_t warp_base[kMaxBlockWarps];
     __shared__ int32_t block_base;
     const unsigned mask = __ballot_sync(0xffffffffu, flag);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -248,7 +252,7 @@ template <int K>
 __device__ __forceinline__ void block_append_k(const int32_t (&v)[K], int32_t *__restrict__ list,
                                                int32_t *__restrict__ count)
 {
-    __shared__ int32_t warp_base[kBlock / 32];
+    __shared__ int32_t warp_base[kMaxBlockWarps];
     __shared__ int32_t block_base;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int32_t mine = 0;

@@ -60,7 +60,10 @@ namespace psi {
 namespace {
 
 constexpr unsigned kAll = 0xffffffffu;
-constexpr int kPatchBlock = 256;
+// 1,024 threads: one block per SM for the cooperative launches (fewer blocks
+// at each grid barrier), and a solo block four times as wide (2^24 random
+// game: 61.5 -> 60.5 ms per solve against 256 threads)
+constexpr int kPatchBlock = 1024;
 constexpr int32_t kBackoffMax = 64;
 // the search goes on in one block once a level has at most this many vertices
 constexpr int32_t kSoloFrontier = 256;
@@ -438,9 +441,10 @@ int patch_blocks(const void *kernel)
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPatchBlock, 0);
     if (per_sm <= 0) per_sm = 1;
-    // two blocks per SM: a grid barrier costs ~1.2 us at 152-304 blocks
-    // against ~1.6 us at 608, and 77k threads cover the frontiers a patch
-    // sees (1 to 4 blocks per SM measured within 1% of each other)
+    // at most two blocks per SM: a grid barrier costs ~1.2 us at 152-304
+    // blocks against ~1.6 us at 608 (with 256-thread blocks, 1 to 4 blocks per
+    // SM measured within 1% of each other); 1,024-thread blocks at 48
+    // registers fit one per SM, 155k threads
     return sms * (per_sm < 2 ? per_sm : 2);
 }
 
