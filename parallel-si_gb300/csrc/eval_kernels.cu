@@ -400,7 +400,9 @@ __global__ void k_walk_sublists(int32_t nsub, int32_t n, int64_t L, int32_t stri
 // items on cycles (tours of components the sink does not reach) never do.
 // Round 0 reads red and writes a, then the rounds alternate a -> b -> a ...
 // Reads bypass L1 (each buffer is rewritten by other blocks between reads).
-__global__ void __launch_bounds__(kBlock) k_rank_reduced(int32_t nsub, const int2 *__restrict__ red,
+// threads per block of the cooperative ranking kernels
+constexpr int kRankBlock = kBlock;
+__global__ void __launch_bounds__(kRankBlock) k_rank_reduced(int32_t nsub, const int2 *__restrict__ red,
                                                          int2 *__restrict__ a, int2 *__restrict__ b,
                                                          const int32_t *__restrict__ gate)
 {
@@ -447,7 +449,7 @@ __device__ __forceinline__ int32_t ruler_index(int32_t j, int32_t nsub, int32_t 
     return j == nsub - 1 ? nr - 1 : j / kRuler;
 }
 
-__global__ void __launch_bounds__(kBlock) k_rank_ruled(int32_t nsub, const int2 *__restrict__ red,
+__global__ void __launch_bounds__(kRankBlock) k_rank_ruled(int32_t nsub, const int2 *__restrict__ red,
                                                        int2 *__restrict__ a, int2 *__restrict__ b,
                                                        uint32_t *__restrict__ err, const int32_t *__restrict__ gate)
 {
@@ -771,7 +773,8 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
 }
 
 // at most 40 registers: six co-resident blocks per SM for the cooperative launch
-__global__ void __launch_bounds__(kBlock, 6) k_cycles(const int32_t *__restrict__ ucount,
+constexpr int kCycleBlock = kBlock, kCycleMinBlocks = 6;
+__global__ void __launch_bounds__(kCycleBlock, kCycleMinBlocks) k_cycles(const int32_t *__restrict__ ucount,
                                                    const int32_t *__restrict__ ulist,
                                                    const int32_t *__restrict__ strat,
                                                    const int32_t *__restrict__ pri,
@@ -943,17 +946,19 @@ int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, 
     if (err && nsub >= kRulerMin) {
         // the ruling set: the rulers' two jump buffers (2 nr entries) fit in b
         const int blocks =
-            per_device(g_ruled_blocks, [] { return device_blocks((const void *)k_rank_ruled, kBlock); });
-        int64_t need = ceil_div(nsub, kBlock);
+            per_device(g_ruled_blocks, [] { return device_blocks((const void *)k_rank_ruled, kRankBlock); });
+        int64_t need = ceil_div(nsub, kRankBlock);
         int grid = (int)(need < blocks ? need : blocks);
         *fin = a;
         void *args[] = {(void *)&nsub, (void *)&red, (void *)&a, (void *)&b, (void *)&err, (void *)&gate};
         count_launch();
-        cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_rank_ruled, dim3(grid), dim3(kBlock), args, 0, s);
+        cudaError_t e =
+            cudaLaunchCooperativeKernel((const void *)k_rank_ruled, dim3(grid), dim3(kRankBlock), args, 0, s);
         return e == cudaSuccess ? 0 : (int)e;
     }
-    const int blocks = per_device(g_rank_blocks, [] { return device_blocks((const void *)k_rank_reduced, kBlock); });
-    int64_t need = ceil_div(nsub, kBlock);
+    const int blocks =
+        per_device(g_rank_blocks, [] { return device_blocks((const void *)k_rank_reduced, kRankBlock); });
+    int64_t need = ceil_div(nsub, kRankBlock);
     int grid = (int)(need < blocks ? need : blocks);
     int rounds = 0;
     while (((int64_t)1 << rounds) < nsub) rounds++;
@@ -961,7 +966,8 @@ int launch_rank_reduced(cudaStream_t s, int32_t nsub, const int2 *red, int2 *a, 
     *fin = (rounds % 2 == 1) ? a : b;
     void *args[] = {(void *)&nsub, (void *)&red, (void *)&a, (void *)&b, (void *)&gate};
     count_launch();
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_rank_reduced, dim3(grid), dim3(kBlock), args, 0, s);
+    cudaError_t e =
+        cudaLaunchCooperativeKernel((const void *)k_rank_reduced, dim3(grid), dim3(kRankBlock), args, 0, s);
     return e == cudaSuccess ? 0 : (int)e;
 }
 
@@ -985,12 +991,13 @@ int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, c
                   const int32_t *pri, const uint8_t *solved, int32_t *st, int32_t *key, int2 *ja, int2 *jb,
                   int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err, ChangeTrack track, const int32_t *gate)
 {
-    const int blocks = per_device(g_cycle_blocks, [] { return device_blocks((const void *)k_cycles, kBlock); });
+    const int blocks =
+        per_device(g_cycle_blocks, [] { return device_blocks((const void *)k_cycles, kCycleBlock); });
     void *args[] = {(void *)&ucount, (void *)&ulist, (void *)&strat, (void *)&pri, (void *)&solved,
                     (void *)&st, (void *)&key, (void *)&ja, (void *)&jb, (void *)&la, (void *)&lb, (void *)&cnt,
                     (void *)&err, (void *)&track, (void *)&gate};
     count_launch();
-    cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_cycles, dim3(blocks), dim3(kBlock), args, 0, s);
+    cudaError_t e = cudaLaunchCooperativeKernel((const void *)k_cycles, dim3(blocks), dim3(kCycleBlock), args, 0, s);
     return e == cudaSuccess ? 0 : (int)e;
 }
 
