@@ -298,8 +298,10 @@ __global__ void __launch_bounds__(kBlock) k_switch(int32_t np, const int32_t *__
             // Fast pass: successors in batches of kBatch -- all ids, then all
             // keys, before the comparisons (independent gathers in flight per
             // thread).  Equal keys of distinct finite vertices end it; the exact
-            // pass then redoes the vertex with summaries and walks.
-            constexpr int kBatch = 4;
+            // pass then redoes the vertex with summaries and walks.  Five
+            // per batch (one batch for out-degrees up to 5): switch steps
+            // 12.6 -> 12.1 ms per 2^24 solve against four; six the same as five.
+            constexpr int kBatch = 5;
             const int32_t cur0 = cur, kc0 = kc;
             bool exact = false;
             for (int32_t eb = e0; eb < e1 && !exact; eb += kBatch) {
