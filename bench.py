@@ -308,7 +308,7 @@ def phase_bytes(phase, n, m, nsub, counters, calls, n_even, n_odd, iters, brs):
 # reduced lists at least this long are ranked through a ruling set (k_rank_ruled)
 RULER_MIN = 4096
 KERNEL_OF_PHASE = {"switch": "k_switch", "sublist": "k_walk_sublists", "tour": "k_tour_relink",
-                   "broadcast": "k_broadcast_depth", "reduced": "k_rank_reduced", "cycles": "k_cycles"}
+                   "broadcast": "k_broadcast_depth", "reduced": "k_rank_ruled", "cycles": "k_cycles"}
 # the kernels of a timed phase (for their DRAM traffic per launch)
 PHASE_KERNELS = {"sublist": ("k_walk_sublists",), "tour": ("k_dirty_list", "k_tour_relink", "k_sink_list"),
                  "broadcast": ("k_broadcast_depth", "k_rootinfo")}
