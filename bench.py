@@ -615,10 +615,13 @@ def run_gb300(args, rank, world, local):
     roofline = None
     if bpc is not None and dom_calls:
         achieved = bpc / (dom_ms / dom_calls / 1e3) / 1e9
-        # the committed DRAM captures are of the random game: no figure for another workload
-        traffic = traffic_per_launch(KERNEL_OF_PHASE[dom], game.n) if args.workload == "single" else None
+        # the committed DRAM captures are of the random game: no figure for another workload;
+        # a phase of several kernels (the algorithmic bytes cover them all) sums their traffic
+        kernels = PHASE_KERNELS.get(dom, (KERNEL_OF_PHASE[dom],))
+        per_kernel = [traffic_per_launch(k, game.n) for k in kernels] if args.workload == "single" else [None]
+        traffic = sum(per_kernel) if all(t is not None for t in per_kernel) else None
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                    "traffic": traffic, "kernel": KERNEL_OF_PHASE[dom], "peak_source": peak_kind,
+                    "traffic": traffic, "kernel": " + ".join(kernels), "peak_source": peak_kind,
                     "algorithmic_bytes_per_launch": bpc, "ms_per_launch": dom_ms / dom_calls}
         if traffic:
             # what HBM actually moved per second (random 32-byte sectors count whole)
