@@ -730,8 +730,10 @@ void launch_switch(cudaStream_t s, int32_t np, const int32_t *plist, int32_t pla
         cudaMemsetAsync(list_count, 0, sizeof(int32_t), s);
         count_launch();
         if (owner && !gmask) {
+            // its own cap (four times the switch's one wave): the scan is one
+            // pass of streaming loads per block
             unsigned gn = grid_for(ceil_div(n_all, kVec));
-            gn = gn < (unsigned)blocks ? gn : (unsigned)blocks;
+            gn = gn < 4u * (unsigned)blocks ? gn : 4u * (unsigned)blocks;
             k_need_ids<<<gn, kBlock, 0, s>>>(n_all, player, owner, need, gate, list, list_count,
                                              warp ? nullptr : claim);
         } else {
