@@ -100,22 +100,22 @@ __device__ __forceinline__ void flag_in_neighbours(const ChangeTrack &t, int mod
     }
     const int32_t total = __shfl_sync(kAll, incl, 31);   // <= m: distinct vertices' in-edges
     const int32_t excl = incl - d;
-    for (int64_t j0 = 0; j0 < total; j0 += 32) {
-        const int64_t j = j0 + lane;
-        int64_t e = -1;
-        int all = 0;
-        for (unsigned s = lanes; s; s &= s - 1) {
-            const int l = __ffs(s) - 1;
-            const int32_t el = __shfl_sync(kAll, excl, l), dl = __shfl_sync(kAll, d, l), bl = __shfl_sync(kAll, b, l);
-            const int ml = __shfl_sync(kAll, mode, l);
-            if (j >= el && j < (int64_t)el + dl) {
-                e = bl + (j - el);
-                all = ml == 2;
-            }
+    for (int32_t j0 = 0; j0 < total; j0 += 32) {
+        const int32_t j = j0 + lane;
+        // owner lane of edge j: the number of lanes whose inclusive count is
+        // <= j (a binary search over the non-decreasing prefix, five rounds of
+        // shuffles; lanes without in-edges own none)
+        int l = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+            const int32_t y = __shfl_sync(kAll, incl, l + step - 1);
+            if (y <= j) l += step;
         }
-        if (e >= 0) {
-            const int32_t u = t.rev_src[e];
-            if (all || t.tie[u]) t.need[u] = 1;
+        const int32_t el = __shfl_sync(kAll, excl, l), bl = __shfl_sync(kAll, b, l);
+        const int ml = __shfl_sync(kAll, mode, l);
+        if (j < total) {
+            const int32_t u = t.rev_src[bl + (j - el)];
+            if (ml == 2 || t.tie[u]) t.need[u] = 1;
         }
     }
 }
