@@ -390,7 +390,7 @@ int psi_server_info(psi_server *s, int32_t *resident, int32_t *queued, int64_t *
  * on `stream` (a cudaStream_t; NULL = the legacy default stream) of the
  * current device, and returns when the result is ready.
  * It calls no cudaMalloc/cudaFree: its working memory is one fixed
- * __device__ array of 13.4 MiB (14,091,520 bytes) that every process loading the library
+ * __device__ array of 17.4 MiB (18,285,824 bytes) that every process loading the library
  * holds on each device it uses, until exit.  Hence the size limit: n may be at
  * most PSI_NOALLOC_MAX_VERTICES, larger n returns PSI_ERR_TOO_LARGE.
  * The first call on a device looks up that array's device address (once per

@@ -674,24 +674,41 @@ __global__ void __launch_bounds__(kBlock, 8) k_rootinfo(int32_t n, const int32_t
 }
 
 // ---- cycle parity of the unreached vertices
-// jmp[u] = (vertex 2^r steps ahead, maximum priority over those 2^r vertices
-// starting at u); solved vertices absorb.  After ceil(log2 |U|)+1 rounds every
-// window is longer than any path into a cycle plus the cycle, so each walk sits
-// on its final cycle (or on a solved vertex) and the window maximum from a
-// cycle vertex is the cycle's top priority.  A vertex whose window has reached
-// a solved vertex s is settled: its entry becomes (-2 - s, -), so no round
-// reads a solved flag; it leaves the active list (later rounds only touch
-// active vertices, and stop early when none is left) and its final entry is
-// stored in both buffers, so any later reader sees it.  A reader racing with
-// that store sees either the previous entry or the final one; both lead to the
-// same solved vertex.
+// Pointer jumping: after round r, jmp[u] = (the vertex 2^r steps ahead, the
+// largest (priority, vertex id) pair over the 2^r vertices starting at u, a
+// flag); solved vertices absorb.  After ceil(log2 |U|)+1 rounds every window
+// is longer than any path into a cycle plus the cycle, so each walk sits on its
+// final cycle (or on a solved vertex) and the window maximum from a cycle
+// vertex is the cycle's top priority.  Most walks end sooner, settled:
+//  - at a solved vertex s: once the window reaches s the entry becomes
+//    (-2 - s, ...), st[s] holds the answer, and no round reads a solved flag;
+//  - on a cycle: if the windows from u and from its target t (2^r vertices
+//    each, back to back) have the same top vertex x, the walk from u meets x
+//    twice, so x lies on a cycle shorter than 2^(r+1) and the walk is on that
+//    cycle from t on.  The new target t' (2^(r+1) steps ahead) is on it too,
+//    and t''s window after this round (2^(r+1) vertices) covers the cycle,
+//    so its top priority is the cycle's: u is flagged, and in the next round
+//    takes that priority's parity (entry kCycleEven / kCycleOdd).
+// A walk that meets a settled vertex settles the same way.  Trees hanging off
+// short cycles then take about log2(depth + cycle) + 3 rounds instead of
+// every round.  A settled vertex leaves the active list (later rounds only
+// touch active vertices, and stop early when none is left) and its final
+// entry is stored in both buffers, so any later reader sees it: the other
+// buffer gets only the settled word, one 4-byte store, and a reader racing
+// with it sees either the previous entry or the settled word, which lead to
+// the same answer.
+// Settled words: -2 - s (s solved, s < 2^30), kCycleEven, kCycleOdd.
+constexpr int32_t kCycleEven = INT_MIN, kCycleOdd = INT_MIN + 1;
+
+__device__ __forceinline__ int32_t cycle_code(int32_t top) { return (top & 1) == 0 ? kCycleEven : kCycleOdd; }
+
 constexpr int kSmallCycles = 4096;   // up to this many: one block, no grid barrier
 
 template <bool GRID>
 __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const int32_t *__restrict__ strat,
                             const int32_t *__restrict__ pri, const uint8_t *__restrict__ solved,
-                            int32_t *__restrict__ st, int32_t *__restrict__ key, int2 *__restrict__ ja,
-                            int2 *__restrict__ jb, int32_t *__restrict__ la, int32_t *__restrict__ lb,
+                            int32_t *__restrict__ st, int32_t *__restrict__ key, int4 *__restrict__ ja,
+                            int4 *__restrict__ jb, int32_t *__restrict__ la, int32_t *__restrict__ lb,
                             int32_t *__restrict__ cnt, uint32_t *__restrict__ err, const ChangeTrack &track)
 {
     const int64_t tid = GRID ? (int64_t)blockIdx.x * blockDim.x + threadIdx.x : threadIdx.x;
@@ -707,9 +724,8 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
             atomicOr(err, DERR_BAD_INPUT);
             t = u;
         }
-        int2 e = make_int2(solved[t] ? -2 - t : t, pri[u]);
-        ja[u] = e;
-        jb[u] = e;
+        // round 0 writes every entry of jb (a settled one as it is)
+        ja[u] = make_int4(solved[t] ? -2 - t : t, pri[u], u, 0);
     }
     if (tid == 0) {
         cnt[0] = 0;
@@ -719,7 +735,7 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
     barrier();
     const int32_t *act = ulist;
     int32_t na = nu;
-    int2 *in = ja, *out = jb;
+    int4 *in = ja, *out = jb;
     int32_t *next = la;
     const int rounds = ceil_log2_dev(nu) + 1;
     for (int r = 0; r < rounds && na > 0; r++) {
@@ -733,15 +749,22 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
             int32_t u = -1;
             if (i0 < na) {
                 u = act[i0];
-                int2 a = __ldcg(&in[u]);
+                const int4 a = __ldcg(&in[u]);
                 if (a.x < 0) {
-                    out[u] = a;                  // settled earlier: entry already final
+                    out[u] = a;                  // settled before the rounds: entry already final
                 } else {
-                    int2 b = __ldcg(&in[a.x]);
-                    int2 a2 = make_int2(b.x, max(a.y, b.y));
-                    out[u] = a2;
-                    if (a2.x < 0) in[u] = a2;    // settled now: final in both buffers
-                    else keep = true;
+                    const int4 b = __ldcg(&in[a.x]);
+                    if (b.x < 0 || a.w) {
+                        // settled now: where b is settled, or (flagged) on the cycle whose
+                        // top priority b's window holds; final in both buffers
+                        const int32_t code = b.x < 0 ? b.x : cycle_code(b.y);
+                        out[u] = make_int4(code, a.y, a.z, 0);
+                        reinterpret_cast<int32_t *>(in + u)[0] = code;
+                    } else {
+                        const bool top_a = a.y > b.y || (a.y == b.y && a.z > b.z);
+                        out[u] = make_int4(b.x, top_a ? a.y : b.y, top_a ? a.z : b.z, a.z == b.z ? 1 : 0);
+                        keep = true;
+                    }
                 }
             }
             block_append(keep, u, next, c);
@@ -750,7 +773,7 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
         na = *(volatile int32_t *)c;
         act = next;
         next = (next == la) ? lb : la;
-        int2 *t = in;
+        int4 *t = in;
         in = out;
         out = t;
     }
@@ -761,8 +784,13 @@ __device__ void cycles_body(int32_t nu, const int32_t *__restrict__ ulist, const
         int32_t u = -1;
         if (i < nu) {
             u = ulist[i];
-            int32_t t = __ldcg(&in[u]).x;
-            int32_t su = (t < 0) ? st[-2 - t] : ((__ldcg(&in[t]).y % 2 == 0) ? ST_POS_INF : ST_NEG_INF);
+            int32_t code = __ldcg(&in[u]).x;
+            if (code >= 0) {   // still walking after every round: its target is on the final cycle
+                const int4 e = __ldcg(&in[code]);
+                code = e.x < 0 ? e.x : cycle_code(e.y);
+            }
+            const int32_t su =
+                code <= kCycleOdd ? (code == kCycleEven ? ST_POS_INF : ST_NEG_INF) : st[-2 - code];
             st[u] = su;
             const int32_t k = (su == ST_POS_INF) ? KEY_POS_INF : KEY_NEG_INF;
             if (key && key[u] != k) {
@@ -784,8 +812,8 @@ __global__ void __launch_bounds__(kCycleBlock, kCycleMinBlocks) k_cycles(const i
                                                    const int32_t *__restrict__ strat,
                                                    const int32_t *__restrict__ pri,
                                                    const uint8_t *__restrict__ solved, int32_t *__restrict__ st,
-                                                   int32_t *__restrict__ key, int2 *__restrict__ ja,
-                                                   int2 *__restrict__ jb,
+                                                   int32_t *__restrict__ key, int4 *__restrict__ ja,
+                                                   int4 *__restrict__ jb,
                                                    int32_t *__restrict__ la, int32_t *__restrict__ lb,
                                                    int32_t *__restrict__ cnt, uint32_t *__restrict__ err,
                                                    ChangeTrack track, const int32_t *__restrict__ gate)
@@ -993,7 +1021,7 @@ void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *nod
 }
 
 int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, const int32_t *strat,
-                  const int32_t *pri, const uint8_t *solved, int32_t *st, int32_t *key, int2 *ja, int2 *jb,
+                  const int32_t *pri, const uint8_t *solved, int32_t *st, int32_t *key, int4 *ja, int4 *jb,
                   int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err, ChangeTrack track, const int32_t *gate)
 {
     const int blocks =

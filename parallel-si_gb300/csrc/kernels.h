@@ -174,7 +174,7 @@ void launch_rootinfo(cudaStream_t s, int32_t n, const int32_t *st, PathNode *nod
 // la, lb: n entries (active lists); cnt: 3 counters.  Returns a cudaError_t
 // value.
 int launch_cycles(cudaStream_t s, const int32_t *ucount, const int32_t *ulist, const int32_t *strat,
-                  const int32_t *pri, const uint8_t *solved, int32_t *st, int32_t *key, int2 *ja, int2 *jb,
+                  const int32_t *pri, const uint8_t *solved, int32_t *st, int32_t *key, int4 *ja, int4 *jb,
                   int32_t *la, int32_t *lb, int32_t *cnt, uint32_t *err, ChangeTrack track = ChangeTrack(),
                   const int32_t *gate = nullptr);
 // mark_solved over the last evaluation's unreached vertices (cpu_parity.cpp:265-274);

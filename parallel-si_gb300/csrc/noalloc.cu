@@ -43,8 +43,8 @@ struct Layout {
     static constexpr size_t node = align256(list + 4 * (size_t)kMaxN);
     static constexpr size_t solved = align256(node + sizeof(PathNode) * (size_t)kMaxN);
     static constexpr size_t ja = align256(solved + (size_t)kMaxN);
-    static constexpr size_t jb = align256(ja + 8 * (size_t)kMaxN);
-    static constexpr size_t redA = align256(jb + 8 * (size_t)kMaxN);
+    static constexpr size_t jb = align256(ja + 16 * (size_t)kMaxN);
+    static constexpr size_t redA = align256(jb + 16 * (size_t)kMaxN);
     static constexpr size_t redB = align256(redA + 8 * (size_t)kMaxSub);
     static constexpr size_t redC = align256(redB + 8 * (size_t)kMaxSub);
     static constexpr size_t total = align256(redC + 8 * (size_t)kMaxSub);
@@ -170,8 +170,8 @@ extern "C" int psi_evaluate_strategy_noalloc(int32_t n, const int32_t *strategy,
     int32_t *list = reinterpret_cast<int32_t *>(base + Layout::list);
     PathNode *node = reinterpret_cast<PathNode *>(base + Layout::node);
     uint8_t *solved = reinterpret_cast<uint8_t *>(base + Layout::solved);
-    int2 *ja = reinterpret_cast<int2 *>(base + Layout::ja);
-    int2 *jb = reinterpret_cast<int2 *>(base + Layout::jb);
+    int4 *ja = reinterpret_cast<int4 *>(base + Layout::ja);
+    int4 *jb = reinterpret_cast<int4 *>(base + Layout::jb);
     int2 *redA = reinterpret_cast<int2 *>(base + Layout::redA);
     int2 *redB = reinterpret_cast<int2 *>(base + Layout::redB);
     int2 *redC = reinterpret_cast<int2 *>(base + Layout::redC);

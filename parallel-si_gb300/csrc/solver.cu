@@ -255,8 +255,8 @@ int Solver::alloc_arrays(int64_t cap_n, int64_t cap_m)
         {(void **)&redA_, 8 * (size_t)cap_sub},
         {(void **)&redB_, 8 * (size_t)cap_sub},
         {(void **)&redC_, 8 * (size_t)cap_sub},
-        {(void **)&jA_, 8 * (size_t)cap_n},
-        {(void **)&jB_, 8 * (size_t)cap_n},
+        {(void **)&jA_, sizeof(int4) * (size_t)cap_n},
+        {(void **)&jB_, sizeof(int4) * (size_t)cap_n},
         {(void **)&dw_, sizeof(Words)},
         {(void **)&ctl_, sizeof(GraphCtl)},
     };

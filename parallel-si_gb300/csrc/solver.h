@@ -213,7 +213,8 @@ private:
     ChangeTrack track() const { return ChangeTrack{need_, rev_off_, rev_src_, &ctl_->quiet, tie_, watch_}; }
     void reset_tracking();       // every vertex to be examined (need = 1, quiet until the next evaluation)
     int32_t *rev_off_ = nullptr, *rev_src_ = nullptr;   // distinct in-neighbours (static)
-    int2 *vloc_ = nullptr, *redA_ = nullptr, *redB_ = nullptr, *jA_ = nullptr, *jB_ = nullptr;
+    int2 *vloc_ = nullptr, *redA_ = nullptr, *redB_ = nullptr;
+    int4 *jA_ = nullptr, *jB_ = nullptr;   // the cycle pass's jump entries
     int2 *redC_ = nullptr;
     // incremental evaluation (patch_kernels.cu): the switch steps' change
     // list, the re-evaluated set and its positions, the jump entries
