@@ -7,6 +7,8 @@ finishes in seconds.  Families follow the measured configurations:
   ring10   the 10-vertex game v -> v+1, v+2 (mod 10), priority = owner = v mod 2
   evencyc  no cycle with an odd top priority (the precondition of the reference's
            Bellman-Ford solver, cpu_bv.cpp:73-85): see evencyc_csr
+  cycles   Odd cycles of lengths 2^k - 1, 2^k, 2^k + 1 with trees hanging off them:
+           see cycle_forest
 """
 import numpy as np
 
@@ -67,6 +69,53 @@ def evencyc_csr(n: int, seed: int):
     return owner, pri, np.array(off, np.int32), np.array(tg, np.int32)
 
 
+CYCLE_LENGTHS = (1, 2, 3, 4, 5, 7, 8, 9, 15, 16, 17, 31, 32, 33, 63, 64, 65, 127, 128, 129, 255, 256, 257, 1000)
+
+
+def cycle_forest(scale, seed):
+    """Odd vertices whose first successors form cycles of the lengths above
+    (powers of two and their neighbours, where the cycle pass's doubling
+    windows just fit or just miss a cycle) with trees hanging off them, some
+    of them long chains; a quarter of the Odd vertices may also leave for an
+    Even vertex, and the Even vertices (an eighth of all) choose among random
+    vertices.  Vertex ids are shuffled and priorities lie in [0, 48), so
+    equal priorities are common.  In the first evaluation every Odd vertex is
+    unreached (its strategy stays in the forest); later ones also meet solved
+    vertices."""
+    rng = np.random.default_rng(seed)
+    succ = []
+    for c in CYCLE_LENGTHS[:scale]:
+        b = len(succ)
+        succ += [b + (i + 1) % c for i in range(c)]
+    n_cyc = len(succ)
+    for k in range(4):                      # long chains into random cycle vertices
+        prev = int(rng.integers(n_cyc))
+        for _ in range(50 + 150 * k):
+            succ.append(prev)
+            prev = len(succ) - 1
+    for _ in range(5 * n_cyc):              # random trees
+        succ.append(int(rng.integers(len(succ))))
+    n_odd = len(succ)
+    n_even = max(2, n_odd // 7)
+    n = n_odd + n_even
+    perm = rng.permutation(n)               # perm[i]: the id of construction vertex i
+    lists = [None] * n
+    for i, s in enumerate(succ):
+        out = [int(perm[s])]
+        if rng.random() < 0.25:
+            out.append(int(perm[n_odd + rng.integers(n_even)]))
+        lists[perm[i]] = out
+    for j in range(n_even):
+        lists[perm[n_odd + j]] = [int(x) for x in rng.integers(n, size=int(rng.integers(2, 4)))]
+    owner = np.zeros(n, np.int32)
+    owner[perm[:n_odd]] = 1
+    pri = rng.integers(0, 48, n).astype(np.int32)
+    off = np.zeros(n + 1, np.int32)
+    off[1:] = np.cumsum([len(x) for x in lists])
+    tgt = np.array([u for x in lists for u in x], np.int32)
+    return psi.Game.from_csr(owner, pri, off, tgt)
+
+
 def make(family: str, n: int, seed: int):
     if family == "c1":
         return psi.Game.random(n, 2, 10, n, seed)
@@ -82,4 +131,6 @@ def make(family: str, n: int, seed: int):
         return ring10()
     if family == "evencyc":
         return psi.Game.from_csr(*evencyc_csr(n, seed))
+    if family == "cycles":   # n: how many of CYCLE_LENGTHS
+        return cycle_forest(n, seed)
     raise ValueError(family)

@@ -7,6 +7,7 @@ import pytest
 
 import oracle
 import psi
+from games import CYCLE_LENGTHS, cycle_forest
 
 
 def c4_games(count, n_lo, n_hi, seed):
@@ -34,6 +35,23 @@ def test_batch_matches_solo_oracle():
         assert np.array_equal(b.get_strategy(k), o.get_strategy()), f"game {k}"
         assert np.array_equal(b.get_winning(k, 0), o.get_winning(0)), f"game {k}"
         assert np.array_equal(b.get_winning(k, 1), o.get_winning(1)), f"game {k}"
+
+
+@pytest.mark.gpu
+def test_batch_matches_solo_oracle_on_cycle_forests():
+    """Games whose first evaluation leaves most vertices on or above short
+    cycles (the cycle pass over the union, more than one block's worth),
+    between random games."""
+    games = ([cycle_forest(12, s) for s in (21, 22, 23)] + c4_games(4, 20, 2000, 13) +
+             [cycle_forest(len(CYCLE_LENGTHS), 24)])
+    b = psi.Batch(games)
+    it, br = b.solve()
+    for k, g in enumerate(games):
+        o = oracle.Oracle(*g.csr())
+        assert (it[k], br[k]) == o.solve(), f"game {k}"
+        assert np.array_equal(b.get_strategy(k), o.get_strategy()), f"game {k}"
+        assert np.array_equal(b.get_winning(k, 0), o.get_winning(0)), f"game {k}"
+        o.close()
 
 
 @pytest.mark.gpu

@@ -20,7 +20,8 @@ from lockstep import lockstep
 
 OFF, AUTO, ALWAYS = 0, 1, 2
 
-FAMILIES = [("c1", 3000, 1), ("c2", 4000, 2), ("c3", 2000, 3), ("c4", 3000, 4), ("smallpri", 3000, 5)]
+FAMILIES = [("c1", 3000, 1), ("c2", 4000, 2), ("c3", 2000, 3), ("c4", 3000, 4), ("smallpri", 3000, 5),
+            ("cycles", 12, 6)]
 
 
 def test_options_layout_and_default():

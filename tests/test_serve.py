@@ -37,7 +37,8 @@ def test_server_rejects_oversize_arena_before_touching_a_device():
 
 @pytest.mark.gpu
 def test_serve_staggered_arrivals_match_solo_oracle():
-    games = c4_games(30, 20, 3000, 13) + [psi.Game.longpath(400, 64, 5), ring10(), make("smallpri", 700, 2)]
+    games = c4_games(30, 20, 3000, 13) + [psi.Game.longpath(400, 64, 5), ring10(), make("smallpri", 700, 2),
+                                          make("cycles", 12, 7)]
     expected = [oracle_result(g) for g in games]
     srv = psi.Server(max_vertices=20000, max_edges=120000, max_games=12)
     tickets = {}
